@@ -1,0 +1,335 @@
+"""Benchmark: two-site H_eff matvec GFLOP/s at chi=1024 on the U(1) XXZ chain's mid bond.
+
+The workload is the local problem of the plain FP64 U(1) DMRG of the XXZ chain N=64, J=1,
+Delta=1, chi=1024 (2 S^z sectors -8..8 of dims 2, 29, 113, 231, 291, 228, 104, 24, 2 on both
+bonds of the two-site block, the converged chain's mid bond), with seeded random environments
+and block. One step = one H_eff matvec (the call Lanczos makes hundreds of times per bond).
+
+  value   GFLOP/s of the device matvec, FLOPs = 2 x the reference's algorithmic MAC count
+          (sum over its four block tensordots of R*K*C, tnkit/blocks.py:1089-1090)
+  e2e     the same through the C ABI tnk_apply_two_site_f64 with theta in pinned host memory:
+          host->device copy of theta, matvec, device->host copy of the result, every step
+  roofline  the dominant kernel (gemm_f64_kernel, the two grouped-GEMM stages) against the
+          FP64 peak measured in this run (cuBLAS DGEMM 8192^3 through torch)
+  cpu_baseline  the oracle's numpy restatement of the reference's block matvec on the host
+
+L2 is flushed (a 256 MiB write) before every timed step, outside the step's CUDA events.
+--impl reference times the oracle port (the reference's algorithm, numpy) on the host cores.
+Multi-GPU: replicas only (one independent matvec stream per rank, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "DMRG sweep s & H_eff GFLOP/s at chi=1024; mixed-TC vs FP64 GPU at |dE|<=1e-10"
+WORKLOAD = ("U(1) XXZ chain N=64, J=1, Delta=1, chi=1024: two-site H_eff matvec at the mid bond "
+            "(sectors 2Sz=-8..8, dims 2,29,113,231,291,228,104,24,2), FP64")
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def _clock_sampler(path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                              "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL)
+        return p, f
+    except (OSError, FileNotFoundError):
+        return None, None
+
+
+def _clock_summary(path, gpu_index):
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    try:
+        for line in open(path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+    except OSError:
+        pass
+    return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_matvec_baseline(th, L, W1, W2, R, budget_s=15.0, max_reps=40):
+    """Oracle (numpy) block matvec on the host: GFLOP/s over a bounded number of repetitions."""
+    from oracle.blocks_np import BT, Leg as OL
+    from oracle import dmrg_np as O
+
+    def ob(t):
+        return BT.from_flat([OL(tuple(l.charges), tuple(l.dims), l.sign) for l in t.legs],
+                            t.charge, t.numpy())
+    a = [ob(t) for t in (th, L, W1, W2, R)]
+    O.apply_two_site(*a)                       # warm (BLAS threads up)
+    reps, t0 = 0, time.perf_counter()
+    while reps < max_reps and (time.perf_counter() - t0 < budget_s or reps < 2):
+        O.apply_two_site(*a)
+        reps += 1
+    dt = (time.perf_counter() - t0) / reps
+    return dt, reps
+
+
+def host_threads():
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS"):
+        if os.environ.get(k):
+            return int(os.environ[k])
+    return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of the reference's block matvec on the host cores."""
+    if rank != 0:
+        return
+    from tnkit_gb300 import workloads, plan as P
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=3, device="cpu")
+    macs = P.two_site_ref_macs(th.layout, L.layout, W1.layout, W2.layout, R.layout)
+    from oracle.blocks_np import BT, Leg as OL
+    from oracle import dmrg_np as O
+
+    def ob(t):
+        return BT.from_flat([OL(tuple(l.charges), tuple(l.dims), l.sign) for l in t.legs],
+                            t.charge, t.numpy())
+    a = [ob(t) for t in (th, L, W1, W2, R)]
+    for _ in range(args.warmup):
+        O.apply_two_site(*a)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.apply_two_site(*a)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = 2 * macs / dt / 1e9
+    cores = host_threads()
+    line = {"metric": METRIC, "value": v, "unit": "GFLOP/s", "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "parallelism": "replicas only (host rank 0)"},
+            "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} full chi=1024 block matvecs (numpy oracle "
+                                       f"of tnkit apply_two_site)"},
+            "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def measure_dgemm_peak(torch, dev):
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2 * n ** 3 / best / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = _env_rank()
+
+    if args.impl == "reference":
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import ctypes as C
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    from tnkit_gb300 import build, ops, workloads, _lib, plan as P
+    build.build()
+    _lib.load()
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=3 + rank, device=dev)
+    op = ops.TwoSiteOperator(th.layout, L, W1, W2, R)
+    p = op.plan
+    hp = p.host
+    ref_macs = P.two_site_ref_macs(th.layout, L.layout, W1.layout, W2.layout, R.layout)
+    flops_ref = 2 * ref_macs
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    x = th.data
+    y = torch.empty_like(x)
+
+    for _ in range(args.warmup):
+        op(x, y)
+    torch.cuda.synchronize()
+
+    # --- device-resident timed region: K matvecs, L2 flushed before each ---
+    clk_path = os.path.join(HERE, "gpurun_out", f"clocks_rank{rank}.csv")
+    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    sampler, fh = _clock_sampler(clk_path)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        evs[i][0].record(stream)
+        op(x, y)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_steps = [a.elapsed_time(b) / 1e3 for a, b in evs]
+    t_dev = float(sum(t_steps))
+
+    # --- per-stage kernel timing (same stream, CUDA events around each launch) ---
+    lib = _lib.lib()
+    ws = op.ws
+    cplan = p.c
+    sp = _lib.stream_ptr()
+    t_g1 = t_c2 = t_g3 = 0.0
+    nrep = max(5, args.steps // 2)
+    import ctypes
+    for i in range(nrep):
+        flush.fill_(float(i))
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        slots = (ctypes.c_void_p * 4)()
+        e[0].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_f64(cplan.t1, cplan.s1, cplan.tiles1, cplan.n_tiles1,
+                                            L.data.data_ptr(), x.data_ptr(), R.data.data_ptr(),
+                                            ws.data_ptr(), ws.data_ptr(), sp), "gemm1")
+        e[1].record(stream)
+        _lib.check(lib.tnk_combine_f64(cplan.t2, cplan.c2, cplan.items2, cplan.n_items2,
+                                       ws.data_ptr(), ws.data_ptr(), sp), "comb")
+        e[2].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_f64(cplan.t3, cplan.s3, cplan.tiles3, cplan.n_tiles3,
+                                            L.data.data_ptr(), x.data_ptr(), R.data.data_ptr(),
+                                            ws.data_ptr(), y.data_ptr(), sp), "gemm3")
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        t_g1 += e[0].elapsed_time(e[1]) / 1e3
+        t_c2 += e[1].elapsed_time(e[2]) / 1e3
+        t_g3 += e[2].elapsed_time(e[3]) / 1e3
+    t_g1, t_c2, t_g3 = t_g1 / nrep, t_c2 / nrep, t_g3 / nrep
+
+    # --- end to end through the C ABI: pinned host theta in, pinned host result out ---
+    h_in = torch.empty(x.numel(), dtype=torch.float64, pin_memory=True)
+    h_in.copy_(x.cpu())
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    d_in = torch.empty_like(x)
+    d_out = torch.empty_like(x)
+    for _ in range(2):
+        d_in.copy_(h_in, non_blocking=True)
+        _lib.check(lib.tnk_apply_two_site_f64(C.byref(cplan), L.data.data_ptr(), d_in.data_ptr(),
+                                              R.data.data_ptr(), d_out.data_ptr(), ws.data_ptr(),
+                                              ws.numel(), sp), "e2e")
+        h_out.copy_(d_out, non_blocking=True)
+    torch.cuda.synchronize()
+    t_e2e = 0.0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        d_in.copy_(h_in, non_blocking=True)
+        _lib.check(lib.tnk_apply_two_site_f64(C.byref(cplan), L.data.data_ptr(), d_in.data_ptr(),
+                                              R.data.data_ptr(), d_out.data_ptr(), ws.data_ptr(),
+                                              ws.numel(), sp), "e2e")
+        h_out.copy_(d_out, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t_e2e += a.elapsed_time(b) / 1e3
+    if sampler is not None:
+        sampler.terminate()
+        sampler.wait()
+        fh.close()
+    err_e2e = float((h_out.to(dev) - y).abs().max() / y.abs().max())
+
+    # max over ranks
+    tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    t_dev, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        dist.barrier()
+        return
+
+    dgemm = measure_dgemm_peak(torch, dev)
+    ms = t_dev / args.steps * 1e3
+    value = world * flops_ref * args.steps / t_dev / 1e9
+    e2e = world * flops_ref * args.steps / t_e2e / 1e9
+    # dominant kernel: the grouped FP64 GEMM (stages 1 and 3); its algorithmic FLOPs are the
+    # reference's L.theta and R.x3 tensordots
+    parts = P.two_site_ref_macs(th.layout, L.layout, W1.layout, W2.layout, R.layout,
+                                parts=True)
+    gemm_flops = 2 * (parts[0] + parts[3])
+    t_gemm = t_g1 + t_g3
+    achieved = gemm_flops / t_gemm / 1e12
+    clocks = _clock_summary(clk_path, local)
+    line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random environments and block, chi=1024 sector dims)",
+            "config": {"workload": WORKLOAD, "l2": "flushed (256 MiB write) before every step",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "ref_gflop_per_matvec": flops_ref / 1e9,
+                       "exec_gflop_per_matvec": 2 * hp.macs / 1e9,
+                       "theta_entries": x.numel()},
+            "roofline": {"bound": "fp64", "kernel": "gemm_f64_kernel (stages 1+3)",
+                         "achieved": achieved, "peak": dgemm, "unit": "TFLOP/s",
+                         "frac": achieved / dgemm,
+                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (torch.matmul "
+                                        "float64); MEASURED_PEAKS.json has no FP64 figure",
+                         "traffic": None,
+                         "stage_ms": {"gemm1": t_g1 * 1e3, "comb": t_c2 * 1e3,
+                                      "gemm3": t_g3 * 1e3}},
+            "e2e": {"value": e2e, "unit": "GFLOP/s", "h2d_bytes_per_step": x.numel() * 8,
+                    "d2h_bytes_per_step": x.numel() * 8, "max_rel_err_vs_device": err_e2e},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks}
+    if not args.no_cpu:
+        dt, reps = cpu_matvec_baseline(th, L, W1, W2, R)
+        line["cpu_baseline"] = {"value": flops_ref / dt / 1e9, "unit": "GFLOP/s",
+                                "cores": host_threads(), "kind": "port",
+                                "sample": f"{reps} full chi=1024 block matvecs (numpy oracle of "
+                                          f"tnkit apply_two_site), {dt * 1e3:.1f} ms each"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

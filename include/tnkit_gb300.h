@@ -1,0 +1,187 @@
+/*
+ * tnkit_gb300 -- C ABI of the GB300 (sm_103a) DMRG/TDVP inner-loop kernels.
+ *
+ * Every entry point takes raw device pointers, 64-bit sizes and a cudaStream_t (passed as
+ * void*), launches asynchronously on that stream and returns an int status: TNK_OK (0) or a
+ * positive TNK_ERR_* code; it never aborts. tnk_last_error() gives a message for the calling
+ * thread's last failure. The library allocates no device memory on these paths: operands,
+ * outputs, task tables and workspace are owned by the caller (torch in the Python host code).
+ *
+ * The H_eff matvec and the environment updates of the reference are each three stages over
+ * charge blocks (dense tensors are the one-block case):
+ *   stage 1  grouped GEMM   W1 = op(x_a) * op(x_b)         (one GEMM per output block)
+ *   stage 2  combination    W2 = sum_t coef_t * W1[..]      (the MPO tensors, as scalars)
+ *   stage 3  grouped GEMM   out = sum_seg W2 * op(x_c)      (segmented K over sectors)
+ * The host builds the task tables of the three stages once per block layout from the
+ * reference's block metadata (`Struct` offsets and shapes) and uploads them; the kernels then
+ * read and write the reference's canonical flat block buffers in place.
+ */
+#ifndef TNKIT_GB300_H
+#define TNKIT_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TNK_OK 0
+#define TNK_ERR_ARG 1      /* a null pointer, a negative size, an unknown slot */
+#define TNK_ERR_CUDA 2     /* a CUDA launch or runtime call failed */
+#define TNK_ERR_SIZE 3     /* workspace or scratch too small for the plan */
+#define TNK_ERR_DEVICE 4   /* set-up failed on the current device */
+
+/* ----------------------------------------------------------------------------------------
+ * Task tables (device arrays built by the host planner). Layouts are fixed by static
+ * asserts in the .cu sources and by numpy dtypes in tnkit_gb300/plan.py.
+ * ---------------------------------------------------------------------------------------- */
+
+/* One output matrix of a grouped GEMM: C(i, j) at c_off + i*ldc + j, i < m, j < n.
+ * C = sum over segments [seg_begin, seg_end) of coef * A_seg * B_seg; with no segment the
+ * output is zero-filled. flags bit 0: accumulate into C instead of overwriting it. */
+typedef struct {
+    int64_t c_off;
+    int32_t ldc, m, n;
+    int32_t seg_begin, seg_end;
+    int32_t flags;
+} tnk_gemm_task;                     /* 32 bytes */
+
+/* One K segment: A(i, k) at buf[a_buf][a_off + i*a_rs + k*a_cs] (i < m, k < k_len),
+ * B(k, j) at buf[b_buf][b_off + k*b_rs + j*b_cs]. Buffer slots are 0..3 (see below). */
+typedef struct {
+    int64_t a_off, b_off;
+    int32_t a_rs, a_cs, b_rs, b_cs;
+    int32_t k;
+    int16_t a_buf, b_buf;
+    int32_t conj;                    /* bit 0: conjugate A, bit 1: conjugate B (complex) */
+    int32_t pad;
+    double coef;
+} tnk_gemm_seg;                      /* 56 bytes */
+
+/* One output tile: task index and the tile's first row/column. The host lists the tiles of
+ * every task, longest K first, so the block scheduler balances uneven sectors. */
+typedef struct {
+    int32_t task, m0, n0, pad;
+} tnk_gemm_tile;                     /* 16 bytes */
+
+/* Stage 2: dst(r, c) = sum over terms t of coef_t * src(r, c), r < rows, c < cols, with
+ * dst(r, c) at dst_off + r*dst_ld + c*dst_cs and src(r, c) at src_off + r*src_ld + c*src_cs.
+ * With no term the destination is zero-filled. */
+typedef struct {
+    int64_t dst_off;
+    int32_t rows, cols, dst_ld, dst_cs;
+    int32_t term_begin, term_end;
+} tnk_comb_task;                     /* 32 bytes */
+
+typedef struct {
+    int64_t src_off;
+    int32_t src_ld, src_cs;
+    double coef;
+} tnk_comb_term;                     /* 24 bytes */
+
+/* A chunk of rows [row0, row1) of one combination task: the launch grid. */
+typedef struct {
+    int32_t task, row0, row1, pad;
+} tnk_comb_item;                     /* 16 bytes */
+
+/* A three-stage contraction plan: device pointers to the tables above and their counts, plus
+ * the workspace it needs (elements of the stage-1 and stage-2 intermediates). Plain data,
+ * filled by the host; the library keeps no reference to it after a call returns. */
+typedef struct {
+    const tnk_gemm_task* t1; const tnk_gemm_seg* s1; const tnk_gemm_tile* tiles1; int64_t n_tiles1;
+    const tnk_comb_task* t2; const tnk_comb_term* c2; const tnk_comb_item* items2; int64_t n_items2;
+    const tnk_gemm_task* t3; const tnk_gemm_seg* s3; const tnk_gemm_tile* tiles3; int64_t n_tiles3;
+    int64_t ws1_elems;               /* stage-1 output: workspace elements [0, ws1_elems) */
+    int64_t ws2_elems;               /* stage-2 output: [ws1_elems, ws1_elems + ws2_elems) */
+    int64_t out_elems;               /* elements of the output buffer */
+} tnk_plan3;
+
+/* ----------------------------------------------------------------------------------------
+ * Library information
+ * ---------------------------------------------------------------------------------------- */
+const char* tnk_version(void);
+const char* tnk_last_error(void);
+/* Sizes of the table structs above, so a binding can check its own layout. */
+int tnk_struct_sizes(int64_t* out6);
+
+/* ----------------------------------------------------------------------------------------
+ * The hot path: H_eff matvecs and environment updates (FP64)
+ *
+ * Operand slots of a plan3: slot 0 = x0, slot 1 = x1, slot 2 = x2, slot 3 = the workspace.
+ * `ws` holds ws1_elems + ws2_elems doubles. All buffers are the reference's canonical flat
+ * block buffers (tnkit/blocks.py:243-252) or, for dense tensors, C-contiguous arrays.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Generic three-stage contraction. */
+int tnk_contract3_f64(const tnk_plan3* plan, const double* x0, const double* x1,
+                      const double* x2, double* out, double* ws, int64_t ws_elems,
+                      void* stream);
+
+/* (H_eff theta) for two sites: out[p,s,t,d] = sum L[p,w,q] th[q,i,j,b] W1[w,m,s,i]
+ * W2[m,r,t,j] R[d,r,b]. Replaces tnkit/_dmrg.py:162-169 (apply_two_site) and, for dense
+ * tensors, :172-189 (fused_two_site + apply_two_site_fused). W1, W2 are folded into the plan.
+ * x0 = L, x1 = theta, x2 = R. */
+int tnk_apply_two_site_f64(const tnk_plan3* plan, const double* L, const double* theta,
+                           const double* R, double* out, double* ws, int64_t ws_elems,
+                           void* stream);
+
+/* (H_eff M) for one site. Replaces tnkit/_dmrg.py:192-199 (apply_one_site). */
+int tnk_apply_one_site_f64(const tnk_plan3* plan, const double* L, const double* M,
+                           const double* R, double* out, double* ws, int64_t ws_elems,
+                           void* stream);
+
+/* L'[d,r,e] = sum L[p,w,q] conj(A[p,s,d]) W[w,r,s,y] A[q,y,e].
+ * Replaces tnkit/_dmrg.py:216-222 (update_left_env). x0 = A (read twice), x1 = L. */
+int tnk_update_left_env_f64(const tnk_plan3* plan, const double* L, const double* A,
+                            double* out, double* ws, int64_t ws_elems, void* stream);
+
+/* R'[u,w,v] = sum R[x,r,y] conj(B[u,s,x]) W[w,r,s,p] B[v,p,y].
+ * Replaces tnkit/_dmrg.py:225-231 (update_right_env). x0 = B (read twice), x1 = R. */
+int tnk_update_right_env_f64(const tnk_plan3* plan, const double* R, const double* B,
+                             double* out, double* ws, int64_t ws_elems, void* stream);
+
+/* One grouped GEMM stage on its own (a two-operand block contraction, e.g. theta = M_i M_i+1,
+ * tnkit/blocks.py:1156-1192 tensordot). Slots 0..3 = b0..b3; C is the output base. */
+int tnk_grouped_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
+                         const tnk_gemm_tile* tiles, int64_t n_tiles, const double* b0,
+                         const double* b1, const double* b2, const double* b3, double* C,
+                         void* stream);
+
+/* One combination stage on its own: block gathers, fuse and split of legs
+ * (tnkit/blocks.py:755-760, :822-838) are combinations with one unit term per piece. */
+int tnk_combine_f64(const tnk_comb_task* tasks, const tnk_comb_term* terms,
+                    const tnk_comb_item* items, int64_t n_items, const double* src,
+                    double* dst, void* stream);
+
+/* ----------------------------------------------------------------------------------------
+ * Lanczos vector kernels (FP64). Replace the reductions and CGS2 reorthogonalisation of
+ * tnkit/eigensolver.py:560-604 (vdot, norm, two classical Gram-Schmidt passes).
+ * `red` is a caller workspace of at least TNK_RED_ELEMS doubles for the two-phase reductions;
+ * results are written to device memory, so no call synchronises.
+ * ---------------------------------------------------------------------------------------- */
+#define TNK_RED_ELEMS 65536
+
+/* out[0] = sum_k x[k] y[k] (deterministic order). */
+int tnk_dot_f64(const double* x, const double* y, int64_t n, double* out, double* red,
+                void* stream);
+/* out[0] = ||x||_2. */
+int tnk_nrm2_f64(const double* x, int64_t n, double* out, double* red, void* stream);
+/* c[i] = sum_k V[i*ldv + k] w[k], i < nv (nv <= 64). */
+int tnk_multidot_f64(const double* V, int64_t ldv, int32_t nv, const double* w, int64_t n,
+                     double* c, double* red, void* stream);
+/* w[k] = w[k] - sum_i c[i] V[i*ldv + k], with c on the device (nv <= 64). */
+int tnk_gemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c, double* w,
+                     int64_t n, void* stream);
+/* y = a*x + b*y with the scalars a = sa[0]*fa, b = sb[0]*fb read from device memory when
+ * sa/sb are non-null (else 1): lets Lanczos use alpha/beta without a host round trip. */
+int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,
+                  const double* sb, double fb, void* stream);
+/* y = x * (f / s[0]) (normalisation by a device scalar). */
+int tnk_scale_div_f64(const double* x, double* y, int64_t n, const double* s, double f,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TNKIT_GB300_H */

@@ -1,0 +1,261 @@
+"""Generate the golden fixtures of this directory by running the reference tnkit itself.
+
+This script is test infrastructure. It imports the reference package read-only from the path
+given by ``--ref`` (default ``/root/reference``) and writes small JSON / NPZ fixtures next to
+itself. The fixtures are committed; the script is not needed at test time.
+
+usage:
+  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py small      # seconds
+  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py dmrg       # a few minutes
+  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py c2         # ~25 min on 8 cores
+
+Modes:
+  small  Block and dense local problems (L, W1, W2, R, theta) dumped from real reference DMRG
+         runs at small sizes, with the reference's own outputs of apply_two_site,
+         apply_one_site, update_left_env, update_right_env and truncated_svd, plus a thick-restart
+         Lanczos known answer.  -> local_problems.npz, local_problems.json
+  dmrg   Per-sweep energies of whole reference DMRG runs at small and medium sizes (TFIM N=10
+         chi=32 dense; XXZ N=12 U(1); XXZ N=64 U(1) at chi=64/128).  -> dmrg_small.json
+  c2     The XXZ N=64 U(1) chi=1024 six-sweep run: energies, sweep times, matvec counts and every
+         bond's sector dims.  -> c2_xxz_n64_chi1024.json
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _import_ref(path):
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, path)
+    import tnkit  # noqa: F401
+    return tnkit
+
+
+def xxz_bulk(delta=1.0):
+    """Bulk MPO of H = sum (S+S- + S-S+)/2 + delta SzSz (spin 1/2), channels (idle, S+, S-, Sz,
+    done): the MPO of the reference's bench/profile/fused_dmrg_check.py:48-53 at delta = 1."""
+    sp = np.array([[0.0, 1.0], [0.0, 0.0]])
+    sm = sp.T.copy()
+    sz = np.diag([0.5, -0.5])
+    i2 = np.eye(2)
+    W = np.zeros((5, 5, 2, 2))
+    W[0, 0], W[0, 1], W[0, 2], W[0, 3] = i2, sp, sm, sz
+    W[1, 4], W[2, 4], W[3, 4], W[4, 4] = 0.5 * sm, 0.5 * sp, delta * sz, i2
+    return W
+
+
+def open_chain(Wb, N):
+    D = Wb.shape[0]
+    return [Wb[0:1] if i == 0 else Wb[:, D - 1:D] if i == N - 1 else Wb for i in range(N)]
+
+
+def _legs_json(struct):
+    return [{"charges": [int(c) for c in leg.charges], "dims": [int(d) for d in leg.dims],
+             "sign": int(leg.sign)} for leg in struct.legs]
+
+
+def _bt(prefix, t, arrays, meta):
+    """Record a reference BlockTensor: canonical buffer into `arrays`, legs/charge into `meta`."""
+    t = t.canonical()
+    arrays[prefix] = np.asarray(t.data)
+    meta[prefix] = {"legs": _legs_json(t.struct), "charge": int(t.struct.charge)}
+
+
+def mode_small(ref):
+    from tnkit import dmrg, get_backend, U1, to_block_mpo
+    from tnkit import _dmrg as D
+    from tnkit.blocks import truncated_svd
+    from tnkit.legs import fuse
+    from tnkit.eigensolver import lanczos_ground_restart
+    from tnkit.models import tfim_mpo
+
+    arrays, meta = {}, {}
+    be = get_backend("numpy-real")
+    # --- U(1) XXZ N=12 chi=16: a converged state, local problem at bonds 5 (mid) and 0 (edge)
+    N = 12
+    W = open_chain(xxz_bulk(1.0), N)
+    Wb, _ = to_block_mpo(W, [[1, -1]] * N, be, sym=U1())
+    E, mps, info = dmrg(Wb, 16, charge=0, seed=1, n_sweeps=4, tol=0, rtol=0, expand=0,
+                        backend="numpy-real")
+    meta["xxz12"] = {"E": float(E), "energies": [float(e) for e in info["energies"]]}
+    bbe = D._block_backend("numpy-real", Wb, None)
+    M = list(mps)
+    Wd = [bbe.array(w) for w in Wb]
+    Ls = [None] * (N + 1)
+    Rs = [None] * (N + 1)
+    Ls[0], Rs[N] = D._edge_envs(M, Wd, bbe)
+    for i in range(N - 1, 0, -1):
+        Rs[i] = D.update_right_env(Rs[i + 1], M[i], Wd[i], bbe)
+    # move the centre right to bond `mid` with QR-free SVD splits in the reference itself
+    rng = np.random.default_rng(7)
+    for i in range(N - 1):
+        Ls[i + 1] = None
+    for bond in (0, 5):
+        # left envs up to `bond`: left-canonicalise by truncated_svd of the reference
+        M = list(mps)
+        Lc = Ls[0]
+        for i in range(bond):
+            th = bbe.einsum("asc,ctb->astb", M[i], M[i + 1])
+            mat, rec = fuse(th, ((0, 1), (2, 3)), bbe)
+            U, S, Vh, _ = truncated_svd(mat, 10 ** 6)
+            from tnkit.legs import split
+            M[i] = split(U, rec, bbe, legs=(0,))
+            M[i + 1] = split(Vh.scale(S, 0), rec, bbe, legs=(1,))
+            Lc = D.update_left_env(Lc, M[i], Wd[i], bbe)
+        th = bbe.einsum("asc,ctb->astb", M[bond], M[bond + 1])
+        # a random theta with the same layout makes the matvec test independent of the state
+        rnd = th.canonical()
+        rnd = type(rnd)(rnd.struct, rng.standard_normal(rnd.struct.size))
+        tag = f"xxz12_b{bond}"
+        _bt(f"{tag}_L", Lc, arrays, meta)
+        _bt(f"{tag}_R", Rs[bond + 2], arrays, meta)
+        _bt(f"{tag}_W1", Wd[bond], arrays, meta)
+        _bt(f"{tag}_W2", Wd[bond + 1], arrays, meta)
+        _bt(f"{tag}_theta", rnd, arrays, meta)
+        _bt(f"{tag}_H2theta", D.apply_two_site(rnd, Lc, Wd[bond], Wd[bond + 1], Rs[bond + 2],
+                                               bbe), arrays, meta)
+        # one-site matvec and environment growth on the left site tensor A = M[bond]
+        A = M[bond].canonical()
+        Ar = type(A)(A.struct, rng.standard_normal(A.struct.size))
+        _bt(f"{tag}_A", Ar, arrays, meta)
+        _bt(f"{tag}_R1", Rs[bond + 1], arrays, meta)
+        _bt(f"{tag}_H1A", D.apply_one_site(Ar, Lc, Wd[bond], Rs[bond + 1], bbe), arrays, meta)
+        _bt(f"{tag}_Lnext", D.update_left_env(Lc, Ar, Wd[bond], bbe), arrays, meta)
+        B = M[bond + 1].canonical()
+        Br = type(B)(B.struct, rng.standard_normal(B.struct.size))
+        _bt(f"{tag}_B", Br, arrays, meta)
+        _bt(f"{tag}_Rnext", D.update_right_env(Rs[bond + 2], Br, Wd[bond + 1], bbe), arrays,
+            meta)
+        # truncated SVD of the (real, converged) two-site block
+        mat, rec = fuse(th, ((0, 1), (2, 3)), bbe)
+        for chi in (4, 10 ** 6):
+            U, S, Vh, disc = truncated_svd(mat, chi)
+            _bt(f"{tag}_svdin", mat, arrays, meta)
+            arrays[f"{tag}_S_chi{chi}"] = np.asarray(S)
+            meta[f"{tag}_S_chi{chi}"] = {"disc": float(disc),
+                                         "bond": _legs_json(U.struct)[1]}
+    # --- dense TFIM N=10: local problem at bond 4 from a converged chi=32 state
+    Wt = [np.real(w) for w in tfim_mpo(10, 1.0)]
+    E, mps, info = dmrg(Wt, 32, n_sweeps=10, tol=0, rtol=0, seed=0, backend="numpy-real")
+    meta["tfim10"] = {"E": float(E), "energies": [float(e) for e in info["energies"]]}
+    M = list(mps)
+    Ls = [np.ones((1, 1, 1))]
+    Rs = [None] * 11
+    Rs[10] = np.ones((1, 1, 1))
+    for i in range(9, 0, -1):
+        Rs[i] = D.update_right_env(Rs[i + 1], M[i], Wt[i], be)
+    rng = np.random.default_rng(11)
+    L0 = np.ones((1, 1, 1))
+    Lc = L0
+    for i in range(4):
+        th = np.einsum("asc,ctb->astb", M[i], M[i + 1])
+        a, s, t, b = th.shape
+        U, S, Vh = np.linalg.svd(th.reshape(a * s, t * b), full_matrices=False)
+        k = min(32, len(S))
+        M[i] = U[:, :k].reshape(a, s, k)
+        M[i + 1] = (S[:k, None] * Vh[:k]).reshape(k, t, b)
+        Lc = D.update_left_env(Lc, M[i], Wt[i], be)
+    th = rng.standard_normal(np.einsum("asc,ctb->astb", M[4], M[5]).shape)
+    arrays["tfim10_b4_L"] = Lc
+    arrays["tfim10_b4_R"] = Rs[6]
+    arrays["tfim10_b4_W1"] = Wt[4]
+    arrays["tfim10_b4_W2"] = Wt[5]
+    arrays["tfim10_b4_theta"] = th
+    arrays["tfim10_b4_H2theta"] = D.apply_two_site(th, Lc, Wt[4], Wt[5], Rs[6], be)
+    A = rng.standard_normal(M[4].shape)
+    arrays["tfim10_b4_A"] = A
+    arrays["tfim10_b4_Lnext"] = D.update_left_env(Lc, A, Wt[4], be)
+    B = rng.standard_normal(M[5].shape)
+    arrays["tfim10_b4_B"] = B
+    arrays["tfim10_b4_Rnext"] = D.update_right_env(Rs[6], B, Wt[5], be)
+    # --- thick-restart Lanczos known answer on a fixed symmetric matrix (restarts exercised)
+    rng = np.random.default_rng(3)
+    n = 300
+    Q = rng.standard_normal((n, n))
+    Hs = 0.5 * (Q + Q.T) + np.diag(np.linspace(-3.0, 3.0, n))
+    v0 = rng.standard_normal(n)
+    e, x, linfo = lanczos_ground_restart(lambda v: Hs @ v, v0, be, tol=1e-10, max_iter=400,
+                                         m=20, k=5)
+    arrays["lanczos_H"] = Hs
+    arrays["lanczos_v0"] = v0
+    arrays["lanczos_x"] = np.asarray(x)
+    meta["lanczos"] = {"e": float(e), "iters": int(linfo["iters"]),
+                       "restarts": int(linfo["restarts"]), "m": 20, "k": 5, "tol": 1e-10,
+                       "max_iter": 400, "eigvalsh0": float(np.linalg.eigvalsh(Hs)[0])}
+    np.savez_compressed(os.path.join(HERE, "local_problems.npz"), **arrays)
+    with open(os.path.join(HERE, "local_problems.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print("wrote local_problems.{npz,json}:", len(arrays), "arrays")
+
+
+def mode_dmrg(ref):
+    from tnkit import dmrg, get_backend, U1, to_block_mpo
+    from tnkit.models import tfim_mpo
+    from tnkit.free_fermion import tfim_free_fermion_energy
+    out = {}
+    Wt = [np.real(w) for w in tfim_mpo(10, 1.0)]
+    t0 = time.perf_counter()
+    E, mps, info = dmrg(Wt, 32, n_sweeps=10, tol=0, rtol=0, seed=0, backend="numpy-real")
+    out["c1_tfim_n10_chi32"] = {"E": float(E), "energies": [float(e) for e in info["energies"]],
+                               "free_fermion": float(tfim_free_fermion_energy(10, 1.0)),
+                               "matvec_calls": int(info["matvec_calls"]),
+                               "discarded_weight": float(info["discarded_weight"]),
+                               "entropies": [float(s) for s in mps.entropies()],
+                               "wall_s": time.perf_counter() - t0}
+    be = get_backend("numpy-real")
+    for N, chi, sweeps in ((12, 16, 4), (12, 64, 4), (64, 64, 3), (64, 128, 3)):
+        W = open_chain(xxz_bulk(1.0), N)
+        Wb, _ = to_block_mpo(W, [[1, -1]] * N, be, sym=U1())
+        t0 = time.perf_counter()
+        E, mps, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=sweeps, tol=0, rtol=0,
+                            expand=0, backend="numpy-real")
+        out[f"xxz_n{N}_chi{chi}"] = {
+            "E": float(E), "energies": [float(e) for e in info["energies"]],
+            "matvec_calls": int(info["matvec_calls"]), "sweep_s": info["sweep_s"],
+            "discarded_weight": float(info["discarded_weight"]),
+            "bonds": [{"charges": [int(c) for c in m.legs[2].charges],
+                       "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
+            "wall_s": time.perf_counter() - t0}
+        print(N, chi, E, flush=True)
+    with open(os.path.join(HERE, "dmrg_small.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+def mode_c2(ref):
+    from tnkit import dmrg, get_backend, U1, to_block_mpo
+    N, chi = 64, 1024
+    be = get_backend("numpy-real")
+    W = open_chain(xxz_bulk(1.0), N)
+    Wb, _ = to_block_mpo(W, [[1, -1]] * N, be, sym=U1())
+    t0 = time.perf_counter()
+    E, mps, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=6, tol=0, rtol=0, expand=0,
+                        backend="numpy-real", verbose=True)
+    rec = {"E": float(E), "energies": [float(e) for e in info["energies"]],
+           "matvec_calls": int(info["matvec_calls"]), "sweep_s": info["sweep_s"],
+           "phase_time": info["phase_time"],
+           "discarded_weight": float(info["discarded_weight"]),
+           "bonds": [{"charges": [int(c) for c in m.legs[2].charges],
+                      "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
+           "host": {"cpu_count": os.cpu_count(),
+                    "omp": os.environ.get("OMP_NUM_THREADS")},
+           "wall_s": time.perf_counter() - t0}
+    with open(os.path.join(HERE, "c2_xxz_n64_chi1024.json"), "w") as f:
+        json.dump(rec, f, indent=1)
+    print("E", E)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("mode", choices=["small", "dmrg", "c2"])
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    ref = _import_ref(a.ref)
+    {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2}[a.mode](ref)

@@ -1,0 +1,66 @@
+"""A numpy interpreter of the kernel task tables (include/tnkit_gb300.h semantics).
+
+Test helper only: it lets the CPU suite check that the host planners emit correct tables
+(against the oracle and the reference's golden vectors) without a GPU. The product never runs it.
+"""
+import numpy as np
+from numpy.lib.stride_tricks import as_strided
+
+
+def _view(buf, off, shape, strides):
+    it = buf.itemsize
+    return as_strided(buf[int(off):], shape=tuple(int(s) for s in shape),
+                      strides=tuple(int(s) * it for s in strides), writeable=False)
+
+
+def run_gemm(tables, slots, C):
+    tasks, segs, tiles = tables
+    covered = np.zeros(len(tasks), bool)
+    for t in tiles:
+        covered[t["task"]] = True
+    for ti, t in enumerate(tasks):
+        m, n = int(t["m"]), int(t["n"])
+        assert covered[ti] or m == 0 or n == 0, "task without tiles"
+        acc = np.zeros((m, n))
+        for s in segs[int(t["seg_begin"]):int(t["seg_end"])]:
+            k = int(s["k"])
+            A = _view(slots[int(s["a_buf"])], s["a_off"], (m, k), (s["a_rs"], s["a_cs"]))
+            B = _view(slots[int(s["b_buf"])], s["b_off"], (k, n), (s["b_rs"], s["b_cs"]))
+            acc += float(s["coef"]) * (A @ B)
+        idx = int(t["c_off"]) + np.arange(m)[:, None] * int(t["ldc"]) + np.arange(n)[None, :]
+        if int(t["flags"]) & 1:
+            C[idx] += acc
+        else:
+            C[idx] = acc
+
+
+def run_comb(tables, src, dst):
+    tasks, terms, items = tables
+    for t in tasks:
+        rows, cols = int(t["rows"]), int(t["cols"])
+        acc = np.zeros((rows, cols))
+        for u in terms[int(t["term_begin"]):int(t["term_end"])]:
+            acc += float(u["coef"]) * _view(src, u["src_off"], (rows, cols),
+                                            (u["src_ld"], u["src_cs"]))
+        idx = (int(t["dst_off"]) + np.arange(rows)[:, None] * int(t["dst_ld"])
+               + np.arange(cols)[None, :] * int(t["dst_cs"]))
+        dst[idx] = acc
+    # every row of every task is in exactly one item
+    seen = {}
+    for it in items:
+        seen.setdefault(int(it["task"]), []).append((int(it["row0"]), int(it["row1"])))
+    for ti, t in enumerate(tasks):
+        rs = sorted(seen.get(ti, []))
+        if int(t["rows"]) and int(t["cols"]):
+            assert rs[0][0] == 0 and rs[-1][1] == int(t["rows"])
+            assert all(a[1] == b[0] for a, b in zip(rs, rs[1:]))
+
+
+def run_plan3(plan, x0, x1, x2):
+    ws = np.zeros(plan.ws1 + plan.ws2)
+    out = np.zeros(plan.out_layout.size)
+    slots = [x0, x1, x2, ws]
+    run_gemm(plan.g1, slots, ws)
+    run_comb(plan.c2, ws.copy(), ws)
+    run_gemm(plan.g3, slots, out)
+    return out

@@ -1,0 +1,108 @@
+"""Host planners (tnkit_gb300.plan) checked on the CPU: their task tables, run through a numpy
+interpreter of the kernel semantics, reproduce the reference's golden outputs and the oracle."""
+import numpy as np
+import pytest
+
+from tnkit_gb300 import plan as P
+from tnkit_gb300.layout import Leg, canonical, layout_of
+from oracle.blocks_np import BT
+from oracle import dmrg_np as O
+from table_interp import run_plan3, run_gemm, run_comb
+
+
+def lay(meta):
+    return layout_of([Leg(tuple(l["charges"]), tuple(l["dims"]), l["sign"]) for l in meta["legs"]],
+                     meta["charge"])
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("tag", ["xxz12_b0", "xxz12_b5"])
+def test_two_site_plan_matches_reference(golden, tag):
+    meta, A = golden
+    g = lambda k: (lay(meta[f"{tag}_{k}"]), A[f"{tag}_{k}"])
+    (Ll, Ld), (Rl, Rd), (W1l, W1d), (W2l, W2d), (Tl, Td) = (g(k) for k in ("L", "R", "W1", "W2", "theta"))
+    p = P.plan_apply(Tl, Ll, [(W1l, W1d), (W2l, W2d)], Rl)
+    assert p.out_layout.size == Tl.size and p.out_layout is Tl
+    out = run_plan3(p, Ld, Td, Rd)
+    assert _rel(out, A[f"{tag}_H2theta"]) <= 1e-13
+    ref_macs = P.two_site_ref_macs(Tl, Ll, W1l, W2l, Rl)
+    th = BT.from_json(meta[f"{tag}_theta"], Td)
+    L = BT.from_json(meta[f"{tag}_L"], Ld)
+    W1, W2 = BT.from_json(meta[f"{tag}_W1"], W1d), BT.from_json(meta[f"{tag}_W2"], W2d)
+    R = BT.from_json(meta[f"{tag}_R"], Rd)
+    assert ref_macs == O.two_site_macs(th, L, W1, W2, R)
+    assert p.macs <= ref_macs
+
+
+@pytest.mark.parametrize("tag", ["xxz12_b0", "xxz12_b5"])
+def test_one_site_and_env_plans_match_reference(golden, tag):
+    meta, A = golden
+    g = lambda k: (lay(meta[f"{tag}_{k}"]), A[f"{tag}_{k}"])
+    (Ll, Ld), (R1l, R1d), (Rl, Rd) = g("L"), g("R1"), g("R")
+    (W1l, W1d), (W2l, W2d), (Al, Ad), (Bl, Bd) = g("W1"), g("W2"), g("A"), g("B")
+    p1 = P.plan_apply(Al, Ll, [(W1l, W1d)], R1l)
+    assert _rel(run_plan3(p1, Ld, Ad, R1d), A[f"{tag}_H1A"]) <= 1e-13
+    pl = P.plan_left_env(Ll, Al, (W1l, W1d))
+    got = run_plan3(pl, Ad, Ld, Ad)
+    ref = BT.from_json(meta[f"{tag}_A"], Ad)
+    want = O.update_left_env(BT.from_json(meta[f"{tag}_L"], Ld), ref,
+                             BT.from_json(meta[f"{tag}_W1"], W1d))
+    assert [l.charges for l in pl.out_layout.legs] == [l.charges for l in want.legs]
+    assert _rel(got, A[f"{tag}_Lnext"]) <= 1e-13
+    pr = P.plan_right_env(Rl, Bl, (W2l, W2d))
+    assert _rel(run_plan3(pr, Bd, Rd, Bd), A[f"{tag}_Rnext"]) <= 1e-13
+
+
+def _dense_layout(shape, signs):
+    return canonical(tuple(Leg((0,), (n,), s) for n, s in zip(shape, signs)), 0)
+
+
+def test_dense_plans_match_reference(golden):
+    _, A = golden
+    th, L, W1, W2, R = (A[f"tfim10_b4_{k}"] for k in ("theta", "L", "W1", "W2", "R"))
+    Tl = _dense_layout(th.shape, (1, 1, 1, -1))
+    Ll = _dense_layout(L.shape, (1, -1, -1))
+    Rl = _dense_layout(R.shape, (-1, 1, 1))
+    W1l = _dense_layout(W1.shape, (1, -1, 1, -1))
+    W2l = _dense_layout(W2.shape, (1, -1, 1, -1))
+    p = P.plan_apply(Tl, Ll, [(W1l, W1.ravel()), (W2l, W2.ravel())], Rl)
+    out = run_plan3(p, L.ravel(), th.ravel(), R.ravel())
+    assert _rel(out, A["tfim10_b4_H2theta"].ravel()) <= 1e-13
+    Am, Bm = A["tfim10_b4_A"], A["tfim10_b4_B"]
+    Al = _dense_layout(Am.shape, (1, 1, -1))
+    Bl = _dense_layout(Bm.shape, (1, 1, -1))
+    pl = P.plan_left_env(Ll, Al, (W1l, W1.ravel()))
+    assert _rel(run_plan3(pl, Am.ravel(), L.ravel(), Am.ravel()),
+                A["tfim10_b4_Lnext"].ravel()) <= 1e-13
+    pr = P.plan_right_env(Rl, Bl, (W2l, W2.ravel()))
+    assert _rel(run_plan3(pr, Bm.ravel(), R.ravel(), Bm.ravel()),
+                A["tfim10_b4_Rnext"].ravel()) <= 1e-13
+
+
+def test_tensordot_fuse_split_plans(golden):
+    meta, A = golden
+    Al, Bl = lay(meta["xxz12_b5_A"]), lay(meta["xxz12_b5_B"])
+    # a theta from two site tensors with a matching bond: use A and a random right tensor
+    a = BT.from_json(meta["xxz12_b5_A"], A["xxz12_b5_A"])
+    rng = np.random.default_rng(0)
+    bl = canonical((Al.legs[2].flip(), Al.legs[1], Leg((-1, 1), (2, 3), -1)), 0)
+    bd = rng.standard_normal(bl.size)
+    pt = P.plan_tensordot(Al, bl, 1)
+    out = np.zeros(pt.out_layout.size)
+    run_gemm(pt.g, [A["xxz12_b5_A"], bd, None, None], out)
+    bo = BT.from_flat([Leg(l.charges, l.dims, l.sign) for l in bl.legs], 0, bd)
+    from oracle.blocks_np import Leg as OLeg, tensordot as otd, fuse as ofuse
+    bo = BT.from_flat([OLeg(tuple(l.charges), tuple(l.dims), l.sign) for l in bl.legs], 0, bd)
+    ref = otd(a, bo, (2,), (0,))
+    assert _rel(out, ref.flat()) <= 1e-13
+    # fuse the 4-leg result into a matrix and split rows/cols back
+    info = P.FuseInfo(pt.out_layout, 2)
+    pf = P.plan_fuse(info)
+    mat = np.zeros(info.matrix.size)
+    run_comb(pf.c, out, mat)
+    mref, _ = ofuse(ref, ((0, 1), (2, 3)))
+    assert np.array_equal(mat, mref.flat())
+    assert [l.dims for l in info.matrix.legs] == [l.dims for l in mref.legs]

@@ -1,0 +1,270 @@
+"""Device execution of the planned contractions through the C ABI.
+
+`DevicePlan3` uploads a host plan's tables to the GPU once (one byte buffer, 64-byte aligned
+sections) and launches the three stages with `tnk_*_f64`. The hot-path functions below mirror
+the reference's tnkit/_dmrg.py:162-231 signatures on `BlockTensor` operands and cache their
+plans per (layouts, MPO tensors). There is no fallback: without the library or a CUDA device they
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from collections import OrderedDict
+from typing import Dict, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import plan as P
+from .layout import Layout
+from .tensor import BlockTensor
+
+_ALIGN = 64
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64
+                and t.is_contiguous()):
+            raise TypeError("tnkit_gb300 kernels need contiguous float64 CUDA tensors")
+
+
+def _pack(arrays, device):
+    """Concatenate numpy arrays into one device byte buffer; return (buffer, byte offsets)."""
+    offs, total = [], 0
+    for a in arrays:
+        offs.append(total)
+        total += (a.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
+    host = np.zeros(max(total, _ALIGN), np.uint8)
+    for a, o in zip(arrays, offs):
+        if a.nbytes:
+            host[o:o + a.nbytes] = np.frombuffer(a.tobytes(), np.uint8)
+    buf = torch.from_numpy(host).to(device)
+    return buf, offs
+
+
+class DevicePlan3:
+    """A three-stage plan resident on the GPU."""
+
+    def __init__(self, hp: P.HostPlan3, device):
+        self.host = hp
+        (t1, s1, l1), (t2, c2, i2), (t3, s3, l3) = hp.g1, hp.c2, hp.g3
+        arrays = [t1, s1, l1, t2, c2, i2, t3, s3, l3]
+        self.buf, offs = _pack(arrays, device)
+        base = self.buf.data_ptr()
+        a = [base + o for o in offs]
+        self.c = _lib.Plan3(a[0], a[1], a[2], len(l1), a[3], a[4], a[5], len(i2),
+                            a[6], a[7], a[8], len(l3), hp.ws1, hp.ws2, hp.out_layout.size)
+        self.out_layout = hp.out_layout
+        self.ws_elems = hp.ws_elems
+        self.macs = hp.macs
+        self.ref_macs = hp.ref_macs
+
+    def run(self, fn: str, x0, x1, x2, out, ws, stream=None):
+        lib = _lib.lib()
+        if ws is None or ws.numel() < self.ws_elems:
+            ws = workspace(self.ws_elems, out.device)
+        f = getattr(lib, fn)
+        sp = _lib.stream_ptr(stream)
+        if fn in ("tnk_update_left_env_f64", "tnk_update_right_env_f64"):
+            # (plan, env, site tensor, out, ws, n, stream): x0 = site tensor, x1 = env
+            rc = f(C.byref(self.c), _lib.ptr(x1), _lib.ptr(x0), _lib.ptr(out), _lib.ptr(ws),
+                   ws.numel(), sp)
+        else:
+            rc = f(C.byref(self.c), _lib.ptr(x0), _lib.ptr(x1), _lib.ptr(x2), _lib.ptr(out),
+                   _lib.ptr(ws), ws.numel(), sp)
+        _lib.check(rc, fn)
+        return out
+
+
+class DeviceGemmPlan:
+    def __init__(self, hp: P.HostGemmPlan, device):
+        self.host = hp
+        t, s, l = hp.g
+        self.buf, offs = _pack([t, s, l], device)
+        base = self.buf.data_ptr()
+        self.ptrs = [base + o for o in offs]
+        self.n_tiles = len(l)
+        self.out_layout = hp.out_layout
+        self.macs = hp.macs
+
+    def run(self, a, b, out, stream=None):
+        rc = _lib.lib().tnk_grouped_gemm_f64(self.ptrs[0], self.ptrs[1], self.ptrs[2],
+                                             self.n_tiles, _lib.ptr(a), _lib.ptr(b), 0, 0,
+                                             _lib.ptr(out), _lib.stream_ptr(stream))
+        _lib.check(rc, "tnk_grouped_gemm_f64")
+        return out
+
+
+class DeviceCombPlan:
+    def __init__(self, hp: P.HostCombPlan, device):
+        self.host = hp
+        t, u, i = hp.c
+        self.buf, offs = _pack([t, u, i], device)
+        base = self.buf.data_ptr()
+        self.ptrs = [base + o for o in offs]
+        self.n_items = len(i)
+        self.out_layout = hp.out_layout
+
+    def run(self, src, dst, stream=None):
+        rc = _lib.lib().tnk_combine_f64(self.ptrs[0], self.ptrs[1], self.ptrs[2], self.n_items,
+                                        _lib.ptr(src), _lib.ptr(dst), _lib.stream_ptr(stream))
+        _lib.check(rc, "tnk_combine_f64")
+        return dst
+
+
+# --------------------------------------------------------------------------- #
+# workspace and plan caches
+# --------------------------------------------------------------------------- #
+_WS: Dict[torch.device, torch.Tensor] = {}
+
+
+def workspace(n: int, device) -> torch.Tensor:
+    """A grow-only float64 workspace per device (the caller's stream orders its reuse)."""
+    device = torch.device(device)
+    w = _WS.get(device)
+    if w is None or w.numel() < n:
+        w = torch.empty(max(n, 1 << 16), dtype=torch.float64, device=device)
+        _WS[device] = w
+    return w
+
+
+class _LRU(OrderedDict):
+    def __init__(self, cap):
+        super().__init__()
+        self.cap = cap
+
+    def get_or(self, key, build):
+        v = self.get(key)
+        if v is not None:
+            self.move_to_end(key)
+            return v
+        v = build()
+        self[key] = v
+        while len(self) > self.cap:
+            self.popitem(last=False)
+        return v
+
+
+_PLANS = _LRU(2048)
+
+
+def _mpo_key(W: BlockTensor):
+    # MPO tensors are fixed per site: identity plus the object itself keeps it alive in the key
+    return (id(W), W)
+
+
+def _host_of(W: BlockTensor) -> np.ndarray:
+    if W.host is None:
+        W.host = W.data.detach().cpu().numpy()
+    return W.host
+
+
+def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                  R: BlockTensor, device) -> DevicePlan3:
+    key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout, str(device))
+
+    def build():
+        hp = P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
+                          R.layout)
+        hp.ref_macs = P.two_site_ref_macs(theta, L.layout, W1.layout, W2.layout, R.layout)
+        return DevicePlan3(hp, device)
+    return _PLANS.get_or(key, build)
+
+
+def plan_one_site(M: Layout, L: BlockTensor, W: BlockTensor, R: BlockTensor,
+                  device) -> DevicePlan3:
+    key = ("apply1", M, L.layout, _mpo_key(W), R.layout, str(device))
+    return _PLANS.get_or(key, lambda: DevicePlan3(
+        P.plan_apply(M, L.layout, [(W.layout, _host_of(W))], R.layout), device))
+
+
+def plan_left(L: Layout, A: Layout, W: BlockTensor, device) -> DevicePlan3:
+    key = ("left", L, A, _mpo_key(W), str(device))
+    return _PLANS.get_or(key, lambda: DevicePlan3(
+        P.plan_left_env(L, A, (W.layout, _host_of(W))), device))
+
+
+def plan_right(R: Layout, B: Layout, W: BlockTensor, device) -> DevicePlan3:
+    key = ("right", R, B, _mpo_key(W), str(device))
+    return _PLANS.get_or(key, lambda: DevicePlan3(
+        P.plan_right_env(R, B, (W.layout, _host_of(W))), device))
+
+
+def plan_tdot(a: Layout, b: Layout, nc: int, device) -> DeviceGemmPlan:
+    key = ("tdot", a, b, nc, str(device))
+    return _PLANS.get_or(key, lambda: DeviceGemmPlan(P.plan_tensordot(a, b, nc), device))
+
+
+# --------------------------------------------------------------------------- #
+# the reference's hot-path functions on block tensors (tnkit/_dmrg.py:162-231)
+# --------------------------------------------------------------------------- #
+def apply_two_site(theta: BlockTensor, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                   R: BlockTensor, out: Optional[torch.Tensor] = None) -> BlockTensor:
+    _require_cuda(theta.data, L.data, R.data)
+    p = plan_two_site(theta.layout, L, W1, W2, R, theta.data.device)
+    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=theta.data.device) \
+        if out is None else out
+    p.run("tnk_apply_two_site_f64", L.data, theta.data, R.data, y, None)
+    return BlockTensor(p.out_layout, y)
+
+
+def apply_one_site(M: BlockTensor, L: BlockTensor, W: BlockTensor, R: BlockTensor,
+                   out: Optional[torch.Tensor] = None) -> BlockTensor:
+    _require_cuda(M.data, L.data, R.data)
+    p = plan_one_site(M.layout, L, W, R, M.data.device)
+    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=M.data.device) \
+        if out is None else out
+    p.run("tnk_apply_one_site_f64", L.data, M.data, R.data, y, None)
+    return BlockTensor(p.out_layout, y)
+
+
+def update_left_env(L: BlockTensor, A: BlockTensor, W: BlockTensor) -> BlockTensor:
+    _require_cuda(L.data, A.data)
+    p = plan_left(L.layout, A.layout, W, A.data.device)
+    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=A.data.device)
+    p.run("tnk_update_left_env_f64", A.data, L.data, A.data, y, None)
+    return BlockTensor(p.out_layout, y)
+
+
+def update_right_env(R: BlockTensor, B: BlockTensor, W: BlockTensor) -> BlockTensor:
+    _require_cuda(R.data, B.data)
+    p = plan_right(R.layout, B.layout, W, B.data.device)
+    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=B.data.device)
+    p.run("tnk_update_right_env_f64", B.data, R.data, B.data, y, None)
+    return BlockTensor(p.out_layout, y)
+
+
+def tensordot(a: BlockTensor, b: BlockTensor, nc: int = 1) -> BlockTensor:
+    """Contract the last `nc` legs of a with the first `nc` legs of b (e.g. "asc,ctb->astb")."""
+    _require_cuda(a.data, b.data)
+    p = plan_tdot(a.layout, b.layout, nc, a.data.device)
+    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=a.data.device)
+    p.run(a.data, b.data, y)
+    return BlockTensor(p.out_layout, y)
+
+
+class TwoSiteOperator:
+    """H_eff of one bond as a matvec on flat canonical buffers, for the Krylov solvers: the plan
+    and operands are bound once per local problem (tnkit/_dmrg.py:633-675 `matvec`)."""
+
+    def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                 R: BlockTensor):
+        _require_cuda(L.data, R.data)
+        self.L, self.R = L, R
+        self.device = L.data.device
+        self.plan = plan_two_site(theta_layout, L, W1, W2, R, self.device)
+        self.n = theta_layout.size
+        self.ws = workspace(self.plan.ws_elems, self.device)
+        self.calls = 0
+
+    @property
+    def macs(self):
+        return self.plan.macs
+
+    def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        y = torch.empty_like(x) if out is None else out
+        self.plan.run("tnk_apply_two_site_f64", self.L.data, x, self.R.data, y, self.ws)
+        self.calls += 1
+        return y

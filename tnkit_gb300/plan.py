@@ -1,0 +1,662 @@
+"""Host planners: block layouts -> task tables of the GB300 kernels.
+
+Every hot-path contraction is planned as three stages over charge blocks (include/tnkit_gb300.h):
+
+  two-site H_eff   Y[p,w,i,j,b] = L[p,w,q] th[q,i,j,b]                         (grouped GEMM)
+                   Z[p,s,t,r,b] = sum_{w,i,j} S[w,i,j,s,t,r] Y[p,w,i,j,b]        (combination)
+                   out[p,s,t,d] = sum_{r,b} Z[p,s,t,r,b] R[d,r,b]                (grouped GEMM)
+  with S = sum_m W1[w,m,s,i] W2[m,r,t,j]; the one-site matvec is the same with one physical leg;
+  left env         T[s,d,w,q] = sum_p conj(A[p,s,d]) L[p,w,q]
+                   U[d,r,q,y] = sum_{w,s} W[w,r,s,y] T[s,d,w,q]
+                   L'[d,r,e]  = sum_{q,y} U[d,r,q,y] A[q,y,e]
+  right env        T[u,s,r,y] = sum_x conj(B[u,s,x]) R[x,r,y]
+                   V[u,w,p,y] = sum_{r,s} W[w,r,s,p] T[u,s,r,y]
+                   R'[u,w,v]  = sum_{p,y} V[u,w,p,y] B[v,p,y]
+
+The intermediates are laid out so that every GEMM operand is a plain strided matrix of one block
+(no gathers), the MPO enters only as scalar coefficients of stage 2, and stage 3 sums the charge
+sectors of its contraction as K segments of one output tile. These are the contractions of the
+reference's tnkit/_dmrg.py:162-231; the planners enumerate the same block pairs its
+tnkit/blocks.py:_sym_plan does, from the same canonical layouts.
+"""
+from __future__ import annotations
+
+from collections import defaultdict
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from ._lib import (COMB_ITEM, COMB_TASK, COMB_TERM, GEMM_SEG, GEMM_TASK, GEMM_TILE)
+from .layout import Layout, Leg, canonical
+
+TILE_M = TILE_N = 64          # must match gemm_f64.cu
+COMB_CHUNK = 8192             # elements per combination CTA (at least one row)
+
+SLOT_X0, SLOT_X1, SLOT_X2, SLOT_WS = 0, 1, 2, 3
+
+
+class GemmTable:
+    """Tasks and segments of one grouped GEMM stage."""
+
+    def __init__(self):
+        self.tasks: List[tuple] = []
+        self.segs: List[tuple] = []
+        self.macs = 0
+
+    def add(self, c_off, ldc, m, n, segs, accumulate=False):
+        b = len(self.segs)
+        for s in segs:
+            # (a_off, b_off, a_rs, a_cs, b_rs, b_cs, k, a_buf, b_buf, conj, pad, coef)
+            self.segs.append(s)
+            self.macs += int(m) * int(n) * int(s[6])
+        self.tasks.append((c_off, ldc, m, n, b, len(self.segs), 1 if accumulate else 0))
+
+    def arrays(self):
+        tasks = np.array(self.tasks, dtype=GEMM_TASK) if self.tasks else np.zeros(0, GEMM_TASK)
+        segs = np.array(self.segs, dtype=GEMM_SEG) if self.segs else np.zeros(0, GEMM_SEG)
+        tiles, cost = [], []
+        for t, (c_off, ldc, m, n, sb, se, fl) in enumerate(self.tasks):
+            ktot = sum(int(s[6]) for s in self.segs[sb:se]) or 1
+            for m0 in range(0, m, TILE_M):
+                for n0 in range(0, n, TILE_N):
+                    tiles.append((t, m0, n0, 0))
+                    cost.append(ktot * min(TILE_M, m - m0) * min(TILE_N, n - n0))
+        order = np.argsort(-np.asarray(cost, np.int64), kind="stable") if tiles else []
+        tl = np.array([tiles[i] for i in order], dtype=GEMM_TILE) if tiles else np.zeros(0, GEMM_TILE)
+        return tasks, segs, tl
+
+
+def seg(a_off, a_rs, a_cs, a_buf, b_off, b_rs, b_cs, b_buf, k, coef=1.0, conj=0):
+    return (int(a_off), int(b_off), int(a_rs), int(a_cs), int(b_rs), int(b_cs), int(k),
+            int(a_buf), int(b_buf), int(conj), 0, float(coef))
+
+
+class CombTable:
+    """Tasks and terms of one combination stage."""
+
+    def __init__(self):
+        self.tasks: List[tuple] = []
+        self.terms: List[tuple] = []
+
+    def add(self, dst_off, rows, cols, dst_ld, dst_cs, terms):
+        b = len(self.terms)
+        self.terms.extend(terms)
+        self.tasks.append((dst_off, rows, cols, dst_ld, dst_cs, b, len(self.terms)))
+
+    def arrays(self):
+        tasks = np.array(self.tasks, dtype=COMB_TASK) if self.tasks else np.zeros(0, COMB_TASK)
+        terms = np.array(self.terms, dtype=COMB_TERM) if self.terms else np.zeros(0, COMB_TERM)
+        items = []
+        for t, (_, rows, cols, *_r) in enumerate(self.tasks):
+            step = max(1, COMB_CHUNK // max(1, cols))
+            for r0 in range(0, rows, step):
+                items.append((t, r0, min(rows, r0 + step), 0))
+        it = np.array(items, dtype=COMB_ITEM) if items else np.zeros(0, COMB_ITEM)
+        return tasks, terms, it
+
+
+def term(src_off, src_ld, src_cs, coef):
+    return (int(src_off), int(src_ld), int(src_cs), float(coef))
+
+
+class HostPlan3:
+    """A three-stage plan on the host: numpy tables plus sizes and MAC counts."""
+
+    def __init__(self, g1: GemmTable, c2: CombTable, g3: GemmTable, ws1, ws2, out_layout,
+                 ref_macs=None, kind=""):
+        self.g1, self.c2, self.g3 = g1.arrays(), c2.arrays(), g3.arrays()
+        self.ws1, self.ws2 = int(ws1), int(ws2)
+        self.out_layout = out_layout
+        self.macs = g1.macs + g3.macs
+        self.comb_terms = len(c2.terms)
+        self.ref_macs = ref_macs
+        self.kind = kind
+
+    @property
+    def ws_elems(self) -> int:
+        return self.ws1 + self.ws2
+
+
+def _check_contract(la: Leg, lb: Leg, what: str):
+    if la.charges != lb.charges or la.dims != lb.dims or la.sign != -lb.sign:
+        raise ValueError(f"{what}: cannot contract leg {la} with leg {lb}: the sectors must "
+                         f"match and the signs be opposite")
+
+
+def _dense_sector_order(layout: Layout, data: np.ndarray) -> np.ndarray:
+    from .layout import to_dense_np
+    return to_dense_np(layout, np.asarray(data))
+
+
+# --------------------------------------------------------------------------- #
+# H_eff matvec (one or two sites)
+# --------------------------------------------------------------------------- #
+def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]],
+               R: Layout) -> HostPlan3:
+    """Plan of (H_eff theta) for n = len(Ws) in {1, 2} sites. `Ws` holds (layout, flat host
+    data) of each MPO tensor, legs (wl, wr, s, s')."""
+    n = len(Ws)
+    if n not in (1, 2) or len(theta.legs) != n + 2:
+        raise ValueError("plan_apply: one or two sites")
+    WL = [w[0] for w in Ws]
+    _check_contract(L.legs[2], theta.legs[0], "L.ket/theta.left")
+    _check_contract(theta.legs[n + 1], R.legs[2], "theta.right/R.ket")
+    _check_contract(L.legs[1], WL[0].legs[0], "L.mpo/W.left")
+    _check_contract(WL[-1].legs[1], R.legs[1], "W.right/R.mpo")
+    for a in range(n):
+        _check_contract(theta.legs[1 + a], WL[a].legs[3], "theta.phys/W.in")
+    if n == 2:
+        _check_contract(WL[0].legs[1], WL[1].legs[0], "W1.right/W2.left")
+    # dense combined MPO S[w, i.., s.., r] over sector-ordered indices
+    Wd = [_dense_sector_order(l, d) for l, d in Ws]
+    if n == 1:
+        S = np.einsum("wrsi->wisr", Wd[0])
+    else:
+        S = np.einsum("wmsi,mrtj->wijstr", Wd[0], Wd[1])
+    wleg, rleg = WL[0].legs[0], WL[-1].legs[1]
+    ins = [WL[a].legs[3] for a in range(n)]
+    outs = [WL[a].legs[2] for a in range(n)]
+    wst, rst = wleg.starts(), rleg.starts()
+    ist, ost = [l.starts() for l in ins], [l.starts() for l in outs]
+
+    out_legs = (L.legs[0],) + tuple(outs) + (R.legs[0],)
+    out = canonical(out_legs, theta.charge)
+
+    # stage 1 candidates: Y[(p, w, phys.., b)] <- (L block, theta block)
+    th_by_q: Dict[int, List[int]] = defaultdict(list)
+    for k in range(theta.nblocks):
+        th_by_q[int(theta.blocks[k, 0])].append(k)
+    ycand: Dict[tuple, Tuple[int, int]] = {}
+    y_by_pb: Dict[Tuple[int, int], List[tuple]] = defaultdict(list)
+    for kl in range(L.nblocks):
+        p, w, q = L.key(kl)
+        for kt in th_by_q.get(q, ()):
+            tk = theta.key(kt)
+            yk = (p, w) + tk[1:]
+            ycand[yk] = (kl, kt)
+            y_by_pb[(p, tk[-1])].append(yk)
+
+    R_by_d: Dict[int, List[int]] = defaultdict(list)
+    for k in range(R.nblocks):
+        R_by_d[int(R.blocks[k, 0])].append(k)
+
+    g1, c2, g3 = GemmTable(), CombTable(), GemmTable()
+    y_off: Dict[tuple, int] = {}
+    ws1 = 0
+
+    def yblock(yk):
+        nonlocal ws1
+        if yk not in y_off:
+            kl, kt = ycand[yk]
+            P, Wd_, Q = L.shape(kl)
+            tsh = theta.shape(kt)
+            ncols = int(np.prod(tsh[1:]))
+            y_off[yk] = ws1
+            ws1 += P * Wd_ * ncols
+            g1.add(y_off[yk], ncols, P * Wd_, ncols,
+                   [seg(L.offsets[kl], Q, 1, SLOT_X0, theta.offsets[kt], ncols, 1, SLOT_X1, Q)])
+        return y_off[yk]
+
+    zdefs = []      # Z blocks: (key, P, PO, Rd, B, [(y key, coefficient sub-array)], R block)
+    tasks3 = []     # (out block, [indices into zdefs])
+    for ko in range(out.nblocks):
+        ok = out.key(ko)
+        p, phys_o, d = ok[0], ok[1:1 + n], ok[-1]
+        oshape = out.shape(ko)
+        P = oshape[0]
+        PO = int(np.prod(oshape[1:1 + n]))
+        segs3 = []
+        for kr in R_by_d.get(d, ()):
+            _, r, b = R.key(kr)
+            Rd, B = R.shape(kr)[1], R.shape(kr)[2]
+            slices = []
+            for yk in y_by_pb.get((p, b), ()):
+                w = yk[1]
+                phys_i = yk[2:2 + n]
+                sub = S[tuple([slice(wst[w], wst[w] + wleg.dims[w])]
+                              + [slice(ist[a][phys_i[a]], ist[a][phys_i[a]] + ins[a].dims[phys_i[a]])
+                                 for a in range(n)]
+                              + [slice(ost[a][phys_o[a]], ost[a][phys_o[a]] + outs[a].dims[phys_o[a]])
+                                 for a in range(n)]
+                              + [slice(rst[r], rst[r] + Rd)])]
+                if np.any(sub):
+                    slices.append((yk, sub))
+            if not slices:
+                continue
+            zdefs.append(((p,) + phys_o + (r, b), P, PO, Rd, B, slices, kr))
+            segs3.append(len(zdefs) - 1)
+        tasks3.append((ko, segs3))
+
+    # workspace: the Y blocks some Z block uses, then the Z blocks
+    for zd in zdefs:
+        for yk, _ in zd[5]:
+            yblock(yk)
+    ws2 = 0
+    z_off = []
+    for zk, P, PO, Rd, B, slices, kr in zdefs:
+        base = ws1 + ws2
+        z_off.append(base)
+        ws2 += P * PO * Rd * B
+        ld = PO * Rd * B
+        po_dims = [outs[a].dims[zk[1 + a]] for a in range(n)]
+        # one combination task per (phys_o', r') slice of this Z block
+        for po in np.ndindex(*po_dims):
+            po_flat = int(np.ravel_multi_index(po, po_dims))
+            for rr in range(Rd):
+                dst = base + (po_flat * Rd + rr) * B
+                terms = []
+                for yk, sub in slices:
+                    kl, kt = ycand[yk]
+                    Wd_ = L.shape(kl)[1]
+                    pi_dims = list(theta.shape(kt)[1:1 + n])
+                    ncols = int(np.prod(theta.shape(kt)[1:]))
+                    for ww in range(Wd_):
+                        for pi in np.ndindex(*pi_dims):
+                            c = sub[(ww,) + pi + po + (rr,)]
+                            if c == 0.0:
+                                continue
+                            pi_flat = int(np.ravel_multi_index(pi, pi_dims))
+                            src = y_off[yk] + ww * ncols + pi_flat * B
+                            terms.append(term(src, Wd_ * ncols, 1, c))
+                c2.add(dst, P, B, ld, 1, terms)
+    for ko, segs3 in tasks3:
+        oshape = out.shape(ko)
+        P, D = oshape[0], oshape[-1]
+        PO = int(np.prod(oshape[1:1 + n]))
+        segs = []
+        for zi in segs3:
+            _, _, _, Rd, B, _, kr = zdefs[zi]
+            K = Rd * B
+            segs.append(seg(z_off[zi], K, 1, SLOT_WS, R.offsets[kr], 1, K, SLOT_X2, K))
+        g3.add(out.offsets[ko], D, P * PO, D, segs)
+    return HostPlan3(g1, c2, g3, ws1, ws2, out, kind=f"apply{n}")
+
+
+# --------------------------------------------------------------------------- #
+# environment updates
+# --------------------------------------------------------------------------- #
+def plan_left_env(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """Plan of L'[d,r,e] = sum L[p,w,q] conj(A[p,s,d]) W[w,r,s,y] A[q,y,e]
+    (tnkit/_dmrg.py:216-222). Slots: x0 = A (conjugated), x1 = L, x2 = A."""
+    WL, wdata = W
+    # conj(A) legs carry flipped signs: its left leg meets L's bra leg (same signs as A's)
+    _check_contract(A.legs[0].flip(), L.legs[0], "conj(A).left/L.bra")
+    _check_contract(L.legs[2], A.legs[0], "L.ket/A.left")
+    _check_contract(L.legs[1], WL.legs[0], "L.mpo/W.left")
+    _check_contract(A.legs[1].flip(), WL.legs[2], "conj(A).phys/W.out")
+    _check_contract(WL.legs[3], A.legs[1], "W.in/A.phys")
+    Wd = _dense_sector_order(WL, wdata)          # [w, r, s, y]
+    wleg, rleg, sleg, yleg = WL.legs
+    wst, rst, sst, yst = (l.starts() for l in WL.legs)
+    out = canonical((A.legs[2].flip(), rleg, A.legs[2]), L.charge)
+
+    # stage 1: T[(s,d),(w,q)] per (A block (p,s,d), L block (p,w,q))
+    L_by_p: Dict[int, List[int]] = defaultdict(list)
+    for k in range(L.nblocks):
+        L_by_p[int(L.blocks[k, 0])].append(k)
+    tcand = {}
+    t_by_dq: Dict[Tuple[int, int], List[tuple]] = defaultdict(list)
+    for ka in range(A.nblocks):
+        p, s, d = A.key(ka)
+        for kl in L_by_p.get(p, ()):
+            _, w, q = L.key(kl)
+            tk = (s, d, w, q)
+            tcand[tk] = (ka, kl)
+            t_by_dq[(d, q)].append(tk)
+    A_by_e: Dict[int, List[int]] = defaultdict(list)
+    for k in range(A.nblocks):
+        A_by_e[int(A.blocks[k, 2])].append(k)
+
+    g1, c2, g3 = GemmTable(), CombTable(), GemmTable()
+    t_off, ws1 = {}, 0
+
+    def tblock(tk):
+        nonlocal ws1
+        if tk not in t_off:
+            ka, kl = tcand[tk]
+            P, S_, D = A.shape(ka)
+            _, Wd_, Q = L.shape(kl)
+            t_off[tk] = ws1
+            ws1 += S_ * D * Wd_ * Q
+            g1.add(t_off[tk], Wd_ * Q, S_ * D, Wd_ * Q,
+                   [seg(A.offsets[ka], 1, S_ * D, SLOT_X0, L.offsets[kl], Wd_ * Q, 1, SLOT_X1,
+                        P, conj=1)])
+        return t_off[tk]
+
+    udefs = []     # (key, D, Rd, Q, Y, contributions[(tk, sub W)], kq_e)
+    tasks3 = []
+    for ko in range(out.nblocks):
+        d, r, e = out.key(ko)
+        D, Rd, E = out.shape(ko)
+        segs3 = []
+        for ka2 in A_by_e.get(e, ()):
+            q, y, _ = A.key(ka2)
+            Q, Yd = A.shape(ka2)[0], A.shape(ka2)[1]
+            contrib = []
+            for tk in t_by_dq.get((d, q), ()):
+                s, _, w, _ = tk
+                sub = Wd[wst[w]:wst[w] + wleg.dims[w], rst[r]:rst[r] + Rd,
+                         sst[s]:sst[s] + sleg.dims[s], yst[y]:yst[y] + Yd]
+                if np.any(sub):
+                    contrib.append((tk, sub))
+            if not contrib:
+                continue
+            udefs.append(((d, r, q, y), D, Rd, Q, Yd, contrib, ka2))
+            segs3.append(len(udefs) - 1)
+        tasks3.append((ko, segs3))
+    for ud in udefs:
+        for tk, _ in ud[5]:
+            tblock(tk)
+    ws2, u_off = 0, {}
+    for i, (uk, D, Rd, Q, Yd, contrib, ka2) in enumerate(udefs):
+        u_off[i] = ws1 + ws2
+        ws2 += D * Rd * Q * Yd
+        for rr in range(Rd):
+            for yy in range(Yd):
+                dst = u_off[i] + rr * Q * Yd + yy
+                terms = []
+                for tk, sub in contrib:
+                    ka, kl = tcand[tk]
+                    S_, Dd = A.shape(ka)[1], A.shape(ka)[2]
+                    Wd_, Qd = L.shape(kl)[1], L.shape(kl)[2]
+                    for ww in range(Wd_):
+                        for ss in range(S_):
+                            c = sub[ww, rr, ss, yy]
+                            if c == 0.0:
+                                continue
+                            src = t_off[tk] + ss * Dd * Wd_ * Qd + ww * Qd
+                            terms.append(term(src, Wd_ * Qd, 1, c))
+                c2.add(dst, D, Q, Rd * Q * Yd, Yd, terms)
+    for ko, segs3 in tasks3:
+        D, Rd, E = out.shape(ko)
+        segs = []
+        for i in segs3:
+            _, _, _, Q, Yd, _, ka2 = udefs[i]
+            K = Q * Yd
+            segs.append(seg(u_off[i], K, 1, SLOT_WS, A.offsets[ka2], E, 1, SLOT_X2, K))
+        g3.add(out.offsets[ko], E, D * Rd, E, segs)
+    return HostPlan3(g1, c2, g3, ws1, ws2, out, kind="left_env")
+
+
+def plan_right_env(R: Layout, B: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """Plan of R'[u,w,v] = sum R[x,r,y] conj(B[u,s,x]) W[w,r,s,p] B[v,p,y]
+    (tnkit/_dmrg.py:225-231). Slots: x0 = B (conjugated), x1 = R, x2 = B."""
+    WL, wdata = W
+    _check_contract(B.legs[2].flip(), R.legs[0], "conj(B).right/R.bra")
+    _check_contract(B.legs[2], R.legs[2], "B.right/R.ket")
+    _check_contract(WL.legs[1], R.legs[1], "W.right/R.mpo")
+    _check_contract(B.legs[1].flip(), WL.legs[2], "conj(B).phys/W.out")
+    _check_contract(WL.legs[3], B.legs[1], "W.in/B.phys")
+    Wd = _dense_sector_order(WL, wdata)          # [w, r, s, p]
+    wleg, rleg, sleg, pleg = WL.legs
+    wst, rst, sst, pst = (l.starts() for l in WL.legs)
+    out = canonical((B.legs[0].flip(), wleg, B.legs[0]), R.charge)
+
+    R_by_x: Dict[int, List[int]] = defaultdict(list)
+    for k in range(R.nblocks):
+        R_by_x[int(R.blocks[k, 0])].append(k)
+    tcand = {}
+    t_by_uy: Dict[Tuple[int, int], List[tuple]] = defaultdict(list)
+    for kb in range(B.nblocks):
+        u, s, x = B.key(kb)
+        for kr in R_by_x.get(x, ()):
+            _, r, y = R.key(kr)
+            tk = (u, s, r, y)
+            tcand[tk] = (kb, kr)
+            t_by_uy[(u, y)].append(tk)
+    B_by_v: Dict[int, List[int]] = defaultdict(list)
+    for k in range(B.nblocks):
+        B_by_v[int(B.blocks[k, 0])].append(k)
+
+    g1, c2, g3 = GemmTable(), CombTable(), GemmTable()
+    t_off, ws1 = {}, 0
+
+    def tblock(tk):
+        nonlocal ws1
+        if tk not in t_off:
+            kb, kr = tcand[tk]
+            U, S_, X = B.shape(kb)
+            _, Rd, Yd = R.shape(kr)
+            t_off[tk] = ws1
+            ws1 += U * S_ * Rd * Yd
+            g1.add(t_off[tk], Rd * Yd, U * S_, Rd * Yd,
+                   [seg(B.offsets[kb], X, 1, SLOT_X0, R.offsets[kr], Rd * Yd, 1, SLOT_X1, X,
+                        conj=1)])
+        return t_off[tk]
+
+    vdefs, tasks3 = [], []
+    for ko in range(out.nblocks):
+        u, w, v = out.key(ko)
+        U, Wd_, V = out.shape(ko)
+        segs3 = []
+        for kb2 in B_by_v.get(v, ()):
+            _, p, y = B.key(kb2)
+            Pd, Yd = B.shape(kb2)[1], B.shape(kb2)[2]
+            contrib = []
+            for tk in t_by_uy.get((u, y), ()):
+                _, s, r, _ = tk
+                sub = Wd[wst[w]:wst[w] + Wd_, rst[r]:rst[r] + rleg.dims[r],
+                         sst[s]:sst[s] + sleg.dims[s], pst[p]:pst[p] + Pd]
+                if np.any(sub):
+                    contrib.append((tk, sub))
+            if not contrib:
+                continue
+            vdefs.append(((u, w, p, y), U, Wd_, Pd, Yd, contrib, kb2))
+            segs3.append(len(vdefs) - 1)
+        tasks3.append((ko, segs3))
+    for vd in vdefs:
+        for tk, _ in vd[5]:
+            tblock(tk)
+    ws2, v_off = 0, {}
+    for i, (vk, U, Wd_, Pd, Yd, contrib, kb2) in enumerate(vdefs):
+        v_off[i] = ws1 + ws2
+        ws2 += U * Wd_ * Pd * Yd
+        for ww in range(Wd_):
+            for pp in range(Pd):
+                dst = v_off[i] + (ww * Pd + pp) * Yd
+                terms = []
+                for tk, sub in contrib:
+                    kb, kr = tcand[tk]
+                    S_ = B.shape(kb)[1]
+                    Rd = R.shape(kr)[1]
+                    for ss in range(S_):
+                        for rr in range(Rd):
+                            c = sub[ww, rr, ss, pp]
+                            if c == 0.0:
+                                continue
+                            src = t_off[tk] + (ss * Rd + rr) * Yd
+                            terms.append(term(src, S_ * Rd * Yd, 1, c))
+                c2.add(dst, U, Yd, Wd_ * Pd * Yd, 1, terms)
+    for ko, segs3 in tasks3:
+        U, Wd_, V = out.shape(ko)
+        segs = []
+        for i in segs3:
+            _, _, _, Pd, Yd, _, kb2 = vdefs[i]
+            K = Pd * Yd
+            segs.append(seg(v_off[i], K, 1, SLOT_WS, B.offsets[kb2], 1, K, SLOT_X2, K))
+        g3.add(out.offsets[ko], V, U * Wd_, V, segs)
+    return HostPlan3(g1, c2, g3, ws1, ws2, out, kind="right_env")
+
+
+# --------------------------------------------------------------------------- #
+# single-stage plans: tensordot over trailing/leading legs, fuse and split
+# --------------------------------------------------------------------------- #
+class HostGemmPlan:
+    def __init__(self, g: GemmTable, out_layout: Layout):
+        self.g = g.arrays()
+        self.macs = g.macs
+        self.out_layout = out_layout
+
+
+def plan_tensordot(a: Layout, b: Layout, nc: int) -> HostGemmPlan:
+    """out = a . b contracting the last `nc` legs of a with the first `nc` legs of b; output legs
+    = free legs of a then free legs of b (tnkit/blocks.py:1156-1192 for this leg order).
+    Slots: x0 = a, x1 = b."""
+    na, nb = len(a.legs), len(b.legs)
+    for i in range(nc):
+        _check_contract(a.legs[na - nc + i], b.legs[i], "tensordot")
+    out = canonical(a.legs[:na - nc] + b.legs[nc:], _add_charge(a.charge, b.charge))
+    b_by_k: Dict[tuple, List[int]] = defaultdict(list)
+    for k in range(b.nblocks):
+        b_by_k[b.key(k)[:nc]].append(k)
+    a_by_free: Dict[tuple, List[int]] = defaultdict(list)
+    for k in range(a.nblocks):
+        a_by_free[a.key(k)[:na - nc]].append(k)
+    g = GemmTable()
+    for ko in range(out.nblocks):
+        okey = out.key(ko)
+        fa, fb = okey[:na - nc], okey[na - nc:]
+        shp = out.shape(ko)
+        M = int(np.prod(shp[:na - nc]))
+        N = int(np.prod(shp[na - nc:]))
+        segs = []
+        for ka in a_by_free.get(fa, ()):
+            kc = a.key(ka)[na - nc:]
+            for kb in b_by_k.get(kc, ()):
+                if b.key(kb)[nc:] != fb:
+                    continue
+                K = int(np.prod(a.shape(ka)[na - nc:]))
+                segs.append(seg(a.offsets[ka], K, 1, SLOT_X0, b.offsets[kb], N, 1, SLOT_X1, K))
+        g.add(out.offsets[ko], N, M, N, segs)
+    return HostGemmPlan(g, out)
+
+
+def _add_charge(a, b):
+    if isinstance(a, tuple):
+        return tuple(x + y for x, y in zip(a, b))
+    return a + b
+
+
+class HostCombPlan:
+    def __init__(self, c: CombTable, out_layout: Layout, extra=None):
+        self.c = c.arrays()
+        self.out_layout = out_layout
+        self.extra = extra
+
+
+class FuseInfo:
+    """Fused legs of a split of the legs into (rows, cols) at `nrow`: per fused leg the sorted
+    signed-total charges and, per fused sector, its sub-sector tuples with row offsets
+    (tnkit/blocks.py:1196-1223 for consecutive groups)."""
+
+    def __init__(self, layout: Layout, nrow: int):
+        self.layout, self.nrow = layout, nrow
+        legs = layout.legs
+        groups = (tuple(range(nrow)), tuple(range(nrow, len(legs))))
+        self.groups = groups
+        self.fused, self.subs = [], []
+        for g in groups:
+            by_q: Dict = defaultdict(list)
+            import itertools
+            for t in itertools.product(*(range(len(legs[a].charges)) for a in g)):
+                qs = [np.asarray(legs[a].charges[s]) * legs[a].sign for a, s in zip(g, t)]
+                tot = sum(qs[1:], qs[0])
+                key = tuple(int(v) for v in np.ravel(tot)) if np.ndim(tot) else int(tot)
+                by_q[key].append(t)
+            qs = sorted(by_q)
+            subs, dims = [], []
+            for q in qs:
+                off, items = 0, {}
+                for t in by_q[q]:
+                    nn = int(np.prod([legs[a].dims[s] for a, s in zip(g, t)]))
+                    items[t] = (off, nn)
+                    off += nn
+                subs.append(items)
+                dims.append(off)
+            self.fused.append(Leg(tuple(qs), tuple(dims), 1))
+            self.subs.append(subs)
+        self.sector_of = [{t: (k, o, nn) for k, items in enumerate(subs)
+                           for t, (o, nn) in items.items()} for subs in self.subs]
+        self.matrix = canonical(tuple(self.fused), layout.charge)
+
+
+def plan_fuse(info: FuseInfo) -> HostCombPlan:
+    """Copy every block of `info.layout` into its place in the fused matrix."""
+    lay, mat = info.layout, info.matrix
+    c = CombTable()
+    nr = info.nrow
+    for k in range(lay.nblocks):
+        key = lay.key(k)
+        r_sec, r_off, r_n = info.sector_of[0][key[:nr]]
+        c_sec, c_off, c_n = info.sector_of[1][key[nr:]]
+        km = mat.index[(r_sec, c_sec)]
+        ncols = mat.shape(km)[1]
+        dst = int(mat.offsets[km]) + r_off * ncols + c_off
+        c.add(dst, r_n, c_n, ncols, 1, [term(lay.offsets[k], c_n, 1, 1.0)])
+    return HostCombPlan(c, mat)
+
+
+def plan_split_rows(info: FuseInfo, m: Layout) -> HostCombPlan:
+    """Split the fused row leg of a matrix layout `m` (legs (F0, k)) back into info's row legs:
+    result legs = row legs + (k,)."""
+    nr = info.nrow
+    rows = info.layout.legs[:nr]
+    out = canonical(tuple(rows) + (m.legs[1],), _charge_of_rows(info, m))
+    c = CombTable()
+    for ko in range(out.nblocks):
+        key = out.key(ko)
+        r_sec, r_off, r_n = info.sector_of[0][key[:nr]]
+        km = m.index.get((r_sec, key[nr]))
+        ncols = out.shape(ko)[-1]
+        if km is None:
+            c.add(out.offsets[ko], r_n, ncols, ncols, 1, [])
+            continue
+        src = int(m.offsets[km]) + r_off * ncols
+        c.add(out.offsets[ko], r_n, ncols, ncols, 1, [term(src, ncols, 1, 1.0)])
+    return HostCombPlan(c, out)
+
+
+def _charge_of_rows(info, m):
+    return m.charge
+
+
+def plan_split_cols(info: FuseInfo, m: Layout) -> HostCombPlan:
+    """Split the fused column leg of a matrix layout `m` (legs (k, F1)) back into info's column
+    legs: result legs = (k,) + col legs."""
+    nr = info.nrow
+    cols = info.layout.legs[nr:]
+    out = canonical((m.legs[0],) + tuple(cols), m.charge)
+    c = CombTable()
+    for ko in range(out.nblocks):
+        key = out.key(ko)
+        c_sec, c_off, c_n = info.sector_of[1][key[1:]]
+        km = m.index.get((key[0], c_sec))
+        nrows = out.shape(ko)[0]
+        if km is None:
+            c.add(out.offsets[ko], nrows, c_n, c_n, 1, [])
+            continue
+        ld = m.shape(km)[1]
+        src = int(m.offsets[km]) + c_off
+        c.add(out.offsets[ko], nrows, c_n, c_n, 1, [term(src, ld, 1, 1.0)])
+    return HostCombPlan(c, out)
+
+
+def two_site_ref_macs(theta: Layout, L: Layout, W1: Layout, W2: Layout, R: Layout,
+                      parts: bool = False):
+    """The reference's algorithmic MAC count of one block `apply_two_site`: the sum over its four
+    tensordots of R*K*C per contracted charge (tnkit/blocks.py:1089-1090), i.e. over every
+    contributing block pair, |free(a)| * |contracted| * |free(b)|."""
+    def tdot(a: Layout, ax_a, b: Layout, ax_b):
+        fa = [i for i in range(len(a.legs)) if i not in ax_a]
+        fb = [j for j in range(len(b.legs)) if j not in ax_b]
+        by = defaultdict(list)
+        for kb in range(b.nblocks):
+            by[tuple(int(b.blocks[kb, j]) for j in ax_b)].append(kb)
+        macs = 0
+        outk = set()
+        for ka in range(a.nblocks):
+            kc = tuple(int(a.blocks[ka, i]) for i in ax_a)
+            for kb in by.get(kc, ()):
+                macs += int(a.sizes[ka]) * int(np.prod([b.shapes[kb, j] for j in fb]))
+                outk.add(tuple(int(a.blocks[ka, i]) for i in fa)
+                         + tuple(int(b.blocks[kb, j]) for j in fb))
+        legs = tuple(a.legs[i] for i in fa) + tuple(b.legs[j] for j in fb)
+        return macs, legs
+    m1, l1 = tdot(L, (2,), theta, (0,))            # x1 (p,w,i,j,b)
+    x1 = canonical(l1, theta.charge)
+    m2, l2 = tdot(W1, (0, 3), x1, (1, 2))          # (m,s,p,j,b)
+    x2 = canonical(l2, theta.charge)
+    m3, l3 = tdot(W2, (0, 3), x2, (0, 3))          # (r,t,s,p,b) ordering as tensordot yields
+    x3 = canonical(l3, theta.charge)
+    m4, _ = tdot(R, (1, 2), x3, (0, 4))
+    return [m1, m2, m3, m4] if parts else m1 + m2 + m3 + m4
