@@ -141,6 +141,21 @@ int tnk_update_left_env_f64(const tnk_plan3* plan, const double* L, const double
 int tnk_update_right_env_f64(const tnk_plan3* plan, const double* R, const double* B,
                              double* out, double* ws, int64_t ws_elems, void* stream);
 
+/* The two-site matvec above for callers that cannot allocate device memory (code in a host
+ * callback or signal-safe section, a fixed pre-sized memory pool, an embedding or binding with
+ * no device allocator): no counterpart in the reference. Instead of a caller workspace it uses
+ * one fixed scratch array in the library's device memory, TNK_NOALLOC_SCRATCH_ELEMS doubles
+ * (64 MiB, enough for the chi=1024 U(1) XXZ mid bond, which needs 6.5 M), held on every GPU that
+ * loads the library until the process exits. Plans needing more scratch get TNK_ERR_SIZE. The
+ * first call on each device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture. All calls share the array, so
+ * calls that overlap on the GPU race; order them on one stream. Allocates nothing. */
+#define TNK_NOALLOC_SCRATCH_ELEMS 8388608
+int tnk_apply_two_site_f64_noalloc(const tnk_plan3* plan, const double* L, const double* theta,
+                                   const double* R, double* out, void* stream);
+/* out[0] = TNK_NOALLOC_SCRATCH_ELEMS, as compiled into the library. */
+int tnk_noalloc_scratch_elems(int64_t* out);
+
 /* One grouped GEMM stage on its own (a two-operand block contraction, e.g. theta = M_i M_i+1,
  * tnkit/blocks.py:1156-1192 tensordot). Slots 0..3 = b0..b3; C is the output base. */
 int tnk_grouped_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
