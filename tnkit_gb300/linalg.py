@@ -1,0 +1,156 @@
+"""Block linear algebra on the GPU around the hot path: fuse/split of legs, the block truncated
+SVD with the global cut across sectors, the per-block LQ of the initial canonicalisation, norms.
+
+  fuse_matrix / split_*   tnkit/blocks.py:1196-1286 (consecutive leg groups), as one
+                          tnk_combine_f64 launch each (one unit term per block piece)
+  truncated_svd           tnkit/blocks.py:1380-1462 (svd_tol = 0, degenerate_tol = 0): per-sector
+                          SVD, the chi largest values over all sectors in the stable order of
+                          (-sigma, position), new bond sectors labelled by the row charge
+  lq                      tnkit/blocks.py:1465-1495 (right=True)
+
+The per-sector factorisations call cuSOLVER through torch.linalg (svd, qr): the truncation is
+kept in FP64 on the GPU; only the singular values cross to the host, once per bond.
+"""
+from __future__ import annotations
+
+from typing import Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import plan as P
+from .layout import Layout, Leg, canonical
+from .ops import DeviceCombPlan, _PLANS
+from .tensor import BlockTensor
+
+
+def _fuse_info(layout: Layout, nrow: int) -> P.FuseInfo:
+    return _PLANS.get_or(("fuseinfo", layout, nrow), lambda: P.FuseInfo(layout, nrow))
+
+
+def fuse_matrix(t: BlockTensor, nrow: int) -> Tuple[BlockTensor, P.FuseInfo]:
+    """Fuse legs [0, nrow) and [nrow, n) of `t` into a two-leg block matrix."""
+    info = _fuse_info(t.layout, nrow)
+    dev = t.data.device
+    p = _PLANS.get_or(("fuse", t.layout, nrow, str(dev)),
+                      lambda: DeviceCombPlan(P.plan_fuse(info), dev))
+    out = torch.empty(info.matrix.size, dtype=torch.float64, device=dev)
+    p.run(t.data, out)
+    return BlockTensor(info.matrix, out), info
+
+
+def split_rows(m: BlockTensor, info: P.FuseInfo) -> BlockTensor:
+    dev = m.data.device
+    p = _PLANS.get_or(("split_r", info.layout, info.nrow, m.layout, str(dev)),
+                      lambda: DeviceCombPlan(P.plan_split_rows(info, m.layout), dev))
+    out = torch.empty(p.out_layout.size, dtype=torch.float64, device=dev)
+    p.run(m.data, out)
+    return BlockTensor(p.out_layout, out)
+
+
+def split_cols(m: BlockTensor, info: P.FuseInfo) -> BlockTensor:
+    dev = m.data.device
+    p = _PLANS.get_or(("split_c", info.layout, info.nrow, m.layout, str(dev)),
+                      lambda: DeviceCombPlan(P.plan_split_cols(info, m.layout), dev))
+    out = torch.empty(p.out_layout.size, dtype=torch.float64, device=dev)
+    p.run(m.data, out)
+    return BlockTensor(p.out_layout, out)
+
+
+def _blocks(m: BlockTensor):
+    lay = m.layout
+    for k in range(lay.nblocks):
+        r, c = lay.key(k)
+        R, Cc = lay.shape(k)
+        o = int(lay.offsets[k])
+        yield r, c, m.data[o:o + R * Cc].view(R, Cc)
+
+
+def _row_label(leg: Leg, r: int):
+    q = leg.charges[r]
+    if leg.sign > 0:
+        return q
+    return tuple(-x for x in q) if isinstance(q, tuple) else -q
+
+
+def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None):
+    """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
+    all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
+    'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
+    Returns U, S (device vector, normalised when scale != 'none'), Vh, disc (absolute)."""
+    if chi < 1:
+        raise ValueError(f"chi must be at least 1, got {chi}")
+    lr, lc = m.layout.legs
+    parts = []
+    for r, c, M in _blocks(m):
+        U, S, Vh = torch.linalg.svd(M, full_matrices=False, driver=driver)
+        parts.append((r, c, U, S, Vh))
+    if not parts:
+        raise ValueError("the matrix has no allowed blocks")
+    s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
+    owner = np.concatenate([np.full(len(p[3]), j) for j, p in enumerate(parts)])
+    order = np.lexsort((np.arange(s_host.size), -s_host))
+    k = min(int(chi), s_host.size)
+    kept = np.bincount(owner[order[:k]], minlength=len(parts))
+    disc = float(np.sum(s_host[order[k:]] ** 2))
+    norm = float(np.sqrt(np.sum(s_host[order[:k]] ** 2))) or 1.0
+    new = [(_row_label(lr, r), r, c, U[:, :n], S[:n], Vh[:n])
+           for (r, c, U, S, Vh), n in zip(parts, kept.tolist()) if n]
+    new.sort(key=lambda x: (x[0], x[1]))
+    bond = Leg(tuple(x[0] for x in new), tuple(int(x[4].shape[0]) for x in new), 1)
+    if scale != "none":
+        new = [(q, r, c, U, S / norm, Vh) for (q, r, c, U, S, Vh) in new]
+    Ub, Vb = [], []
+    for q, r, c, U, S, Vh in sorted(new, key=lambda x: x[1]):
+        Ub.append((U * S[None, :] if scale == "left" else U).reshape(-1))
+    for q, r, c, U, S, Vh in new:
+        Vb.append((Vh * S[:, None] if scale == "right" else Vh).reshape(-1))
+    S = torch.cat([x[4] for x in new])
+    Ul = canonical((lr, bond.flip()), _zero_like(m.layout.charge))
+    Vl = canonical((bond, lc), m.layout.charge)
+    return (BlockTensor(Ul, torch.cat(Ub).contiguous()), S,
+            BlockTensor(Vl, torch.cat(Vb).contiguous()), disc)
+
+
+def _zero_like(q):
+    return tuple(0 for _ in q) if isinstance(q, tuple) else 0
+
+
+def lq(m: BlockTensor):
+    """m = L Q per block, Q with orthonormal rows (the new bond labelled by the row charge)."""
+    lr, lc = m.layout.legs
+    new = []
+    for r, c, M in _blocks(m):
+        q, t = torch.linalg.qr(M.transpose(0, 1))
+        new.append((_row_label(lr, r), r, c, t.transpose(0, 1).contiguous(),
+                    q.transpose(0, 1).contiguous()))
+    new.sort(key=lambda x: x[0])
+    bond = Leg(tuple(x[0] for x in new), tuple(int(x[3].shape[1]) for x in new), 1)
+    A = torch.cat([a.reshape(-1) for _, _, _, a, _ in sorted(new, key=lambda x: x[1])])
+    B = torch.cat([b.reshape(-1) for _, _, _, _, b in new])
+    return (BlockTensor(canonical((lr, bond.flip()), _zero_like(m.layout.charge)), A),
+            BlockTensor(canonical((bond, lc), m.layout.charge), B))
+
+
+class Scalars:
+    """Norms and scalings of flat device buffers through the library's reduction kernels."""
+
+    def __init__(self, device):
+        self.red = torch.empty(_lib.TNK_RED_ELEMS, dtype=torch.float64, device=device)
+        self.sc = torch.zeros(4, dtype=torch.float64, device=device)
+        self.lib = _lib.lib()
+
+    def normalize_(self, x: torch.Tensor) -> torch.Tensor:
+        sp = _lib.stream_ptr()
+        _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.sc.data_ptr(),
+                                         self.red.data_ptr(), sp), "nrm2")
+        _lib.check(self.lib.tnk_scale_div_f64(x.data_ptr(), x.data_ptr(), x.numel(),
+                                              self.sc.data_ptr(), 1.0, sp), "scale_div")
+        return x
+
+    def norm(self, x: torch.Tensor) -> float:
+        sp = _lib.stream_ptr()
+        _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.sc.data_ptr(),
+                                         self.red.data_ptr(), sp), "nrm2")
+        return float(self.sc[0].item())
