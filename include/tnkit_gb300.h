@@ -170,6 +170,67 @@ int tnk_combine_f64(const tnk_comb_task* tasks, const tnk_comb_term* terms,
                     double* dst, void* stream);
 
 /* ----------------------------------------------------------------------------------------
+ * Mixed precision: the two-site matvec on the tcgen05 tensor cores (TF32 inputs, FP32
+ * accumulation in TMEM), FP64 in and out. Replaces, for the bulk Lanczos iterations, the
+ * low-precision matvec of tnkit/_dmrg.py:691-695 (eig='lanczos-mixed', there complex64 einsums).
+ * passes = 3 splits every operand into TF32 hi/lo parts (~1e-6 relative error); passes = 1 is
+ * plain TF32 (~1e-3).
+ * ---------------------------------------------------------------------------------------- */
+
+/* A tensor-core GEMM segment: operand tensor maps (hi parts at index 2*map, lo at 2*map+1). */
+typedef struct {
+    int32_t a_map, b_map, k, pad;
+} tnk_tc_seg;                        /* 16 bytes */
+
+/* Staging of one FP64 block into the FP32 operand layout: source rows x cols (row stride
+ * src_ld) -> destination (transposed when `transpose`: cols x rows) with row stride dst_ld. */
+typedef struct {
+    int64_t src_off, dst_off;
+    int32_t rows, cols, src_ld, dst_ld;
+    int32_t transpose, pad;
+} tnk_cvt_task;                      /* 40 bytes */
+
+typedef struct {
+    int32_t task, r0, c0, pad;       /* one 32 x 32 source tile */
+} tnk_cvt_item;                      /* 16 bytes */
+
+/* The tensor-core two-site plan. `stage` is one FP32 buffer holding every staged operand (L, R,
+ * theta^T, Z) at the tables' offsets, hi parts first and lo parts at +lo_off; `y32` holds the
+ * stage-1 output. `maps` are the CUtensorMaps (128 bytes each, 64-byte aligned) of the staged
+ * blocks; `err` is a device word that a kernel sets (nonzero) if a bounded wait timed out. */
+typedef struct {
+    const tnk_cvt_task* cvt; const tnk_cvt_item* cvt_items; int64_t n_cvt_items;
+    const tnk_gemm_task* t1; const tnk_tc_seg* s1; const tnk_gemm_tile* tiles1; int64_t n_tiles1;
+    const tnk_comb_task* t2; const tnk_comb_term* c2; const tnk_comb_item* items2; int64_t n_items2;
+    const tnk_gemm_task* t3; const tnk_tc_seg* s3; const tnk_gemm_tile* tiles3; int64_t n_tiles3;
+    const void* maps;
+    float* stage; int64_t lo_off;
+    float* y32;
+    int* err;
+    int32_t passes, pad;
+} tnk_tc_plan;
+
+/* out = H_eff theta (FP64 canonical buffers) through the tensor cores: stage theta, two tcgen05
+ * grouped GEMMs around the FP32 MPO combination. L and R must have been staged into the plan's
+ * buffer with tnk_stage_f32 (once per local problem). */
+int tnk_apply_two_site_tc(const tnk_tc_plan* plan, const double* theta, double* out,
+                          void* stream);
+/* Stage FP64 blocks into FP32 (split into hi/lo parts when `split`). */
+int tnk_stage_f32(const tnk_cvt_task* tasks, const tnk_cvt_item* items, int64_t n_items,
+                  const double* src, float* dst, int64_t lo_off, int32_t split, void* stream);
+/* Encode n 2-D FP32 tensor maps (host side; needs the CUDA driver): desc4 holds (element offset
+ * from `base`, rows, cols, row stride) per map; out receives n * 128 bytes. */
+int tnk_tc_encode_tmaps(const float* base, const int64_t* desc4, int64_t n, void* out);
+/* One tensor-core grouped GEMM stage (flags bit 1 of a task: FP64 output, else FP32). */
+int tnk_grouped_gemm_tc(const tnk_gemm_task* tasks, const tnk_tc_seg* segs,
+                        const tnk_gemm_tile* tiles, int64_t n_tiles, const void* maps, void* C,
+                        int* err, int32_t passes, void* stream);
+/* Stage 2 on FP32 data (hi/lo split of the result when `split`). */
+int tnk_combine_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
+                    const tnk_comb_item* items, int64_t n_items, const float* src, float* dst,
+                    int64_t lo_off, int32_t split, void* stream);
+
+/* ----------------------------------------------------------------------------------------
  * Lanczos vector kernels (FP64). Replace the reductions and CGS2 reorthogonalisation of
  * tnkit/eigensolver.py:560-604 (vdot, norm, two classical Gram-Schmidt passes).
  * `red` is a caller workspace of at least TNK_RED_ELEMS doubles for the two-phase reductions;

@@ -1,0 +1,80 @@
+"""The tensor-core (tcgen05, TF32) two-site matvec and the mixed-precision local solve.
+
+Tolerances: the split-TF32 matvec (three MMAs of TF32 hi/lo parts, FP32 accumulation) agrees with
+the FP64 matvec to 1e-4 relative to the largest entry (typically ~1e-6); plain TF32 to 3e-2.
+The mixed local solve (tensor-core Lanczos, then FP64 polish to the same residual tolerance) must
+reach the FP64 solve's eigenvalue to |dE| <= 1e-10."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tnkit_gb300 import build
+    build.build()
+
+
+def _rel(a, b):
+    return float((a - b).abs().max() / b.abs().max())
+
+
+@pytest.mark.parametrize("scale", [8, 2, 1])
+@pytest.mark.parametrize("passes,tol", [(3, 1e-4), (1, 3e-2)])
+def test_tc_matvec_matches_fp64(scale, passes, tol):
+    from tnkit_gb300 import ops, workloads
+    from tnkit_gb300.mixed import TwoSiteOperatorTC
+    dims = [max(1, d // scale) for d in workloads.C2_MID_DIMS]
+    th, L, W1, W2, R = workloads.mid_bond_problem(dims=dims, seed=20 + scale)
+    op64 = ops.TwoSiteOperator(th.layout, L, W1, W2, R)
+    optc = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=passes)
+    ref = op64(th.data)
+    for _ in range(2):                  # twice: staging buffers are reused between calls
+        got = optc(th.data)
+    torch.cuda.synchronize()
+    optc.check_device_error()
+    assert torch.isfinite(got).all()
+    assert _rel(got, ref) <= tol, _rel(got, ref)
+
+
+def test_tc_matvec_golden_problem(golden):
+    """The reference's own (converged-state) XXZ N=12 local problem."""
+    from tnkit_gb300 import BlockTensor, Leg, layout_of
+    from tnkit_gb300.mixed import TwoSiteOperatorTC
+    meta, A = golden
+
+    def bt(key):
+        m = meta[key]
+        lay = layout_of([Leg(tuple(l["charges"]), tuple(l["dims"]), l["sign"]) for l in m["legs"]],
+                        m["charge"])
+        h = np.ascontiguousarray(A[key], dtype=np.float64)
+        return BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    tag = "xxz12_b5"
+    th, L, W1, W2, R = (bt(f"{tag}_{k}") for k in ("theta", "L", "W1", "W2", "R"))
+    got = TwoSiteOperatorTC(th.layout, L, W1, W2, R)(th.data)
+    ref = torch.as_tensor(A[f"{tag}_H2theta"], device="cuda")
+    assert _rel(got, ref) <= 1e-4
+
+
+def _xxz_blocks(N):
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.mpo import to_block_mpo
+    return to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
+
+
+@pytest.mark.parametrize("N,chi,sweeps", [(12, 16, 4), (32, 64, 3)])
+def test_mixed_dmrg_matches_fp64_dmrg(N, chi, sweeps):
+    """Whole sweeps with tensor-core Lanczos + FP64 polish against the plain FP64 sweep from
+    the same start: |dE| <= 1e-10 at every sweep, and most matvecs on the tensor cores."""
+    from tnkit_gb300.dmrg import dmrg
+    kw = dict(charge=0, seed=1, n_sweeps=sweeps, tol=0, rtol=0, expand=0)
+    E64, _, i64 = dmrg(_xxz_blocks(N), chi, **kw)
+    Em, _, im = dmrg(_xxz_blocks(N), chi, precision="mixed", **kw)
+    assert abs(Em - E64) <= 1e-10, (Em, E64)
+    assert np.allclose(im["energies"], i64["energies"], rtol=0, atol=1e-10)
+    assert im["mixed_counts"]["lo"] > 0

@@ -106,3 +106,21 @@ def test_tensordot_fuse_split_plans(golden):
     mref, _ = ofuse(ref, ((0, 1), (2, 3)))
     assert np.array_equal(mat, mref.flat())
     assert [l.dims for l in info.matrix.legs] == [l.dims for l in mref.legs]
+
+
+@pytest.mark.parametrize("passes,tol", [(3, 2e-5), (1, 3e-2)])
+def test_tensor_core_plan_relayout(passes, tol):
+    """The tensor-core re-layout (staged K-major blocks, transposed theta, padded Z) reproduces
+    the FP64 matvec to the accuracy of split / plain TF32, on uneven scaled mid-bond sectors."""
+    from tnkit_gb300 import workloads
+    from table_interp import run_tc_plan
+    dims = [max(1, d // 8) for d in workloads.C2_MID_DIMS]
+    th, L, W1, W2, R = workloads.mid_bond_problem(dims=dims, seed=5, device="cpu")
+    hp = P.plan_apply(th.layout, L.layout, [(W1.layout, W1.host), (W2.layout, W2.host)], R.layout)
+    ref = run_plan3(hp, L.host, th.host, R.host)
+    tc = P.HostPlanTC(hp, th.layout, L.layout, R.layout)
+    got = run_tc_plan(tc, L.host, th.host, R.host, passes=passes)
+    assert _rel(got, ref) <= tol
+    for off, r, c, ld in tc.maps:
+        assert off % P.TC_ALIGN == 0 and (ld * 4) % 16 == 0 and ld >= c
+    assert tc.stage_elems % P.TC_ALIGN == 0

@@ -42,6 +42,10 @@ COMB_TASK = np.dtype([("dst_off", "<i8"), ("rows", "<i4"), ("cols", "<i4"), ("ds
 COMB_TERM = np.dtype([("src_off", "<i8"), ("src_ld", "<i4"), ("src_cs", "<i4"),
                       ("coef", "<f8")])
 COMB_ITEM = np.dtype([("task", "<i4"), ("row0", "<i4"), ("row1", "<i4"), ("pad", "<i4")])
+TC_SEG = np.dtype([("a_map", "<i4"), ("b_map", "<i4"), ("k", "<i4"), ("pad", "<i4")])
+CVT_TASK = np.dtype([("src_off", "<i8"), ("dst_off", "<i8"), ("rows", "<i4"), ("cols", "<i4"),
+                     ("src_ld", "<i4"), ("dst_ld", "<i4"), ("transpose", "<i4"), ("pad", "<i4")])
+CVT_ITEM = np.dtype([("task", "<i4"), ("r0", "<i4"), ("c0", "<i4"), ("pad", "<i4")])
 
 
 class Plan3(C.Structure):
@@ -52,6 +56,19 @@ class Plan3(C.Structure):
                 ("t3", C.c_void_p), ("s3", C.c_void_p), ("tiles3", C.c_void_p),
                 ("n_tiles3", C.c_int64),
                 ("ws1_elems", C.c_int64), ("ws2_elems", C.c_int64), ("out_elems", C.c_int64)]
+
+
+class TcPlan(C.Structure):
+    _fields_ = [("cvt", C.c_void_p), ("cvt_items", C.c_void_p), ("n_cvt_items", C.c_int64),
+                ("t1", C.c_void_p), ("s1", C.c_void_p), ("tiles1", C.c_void_p),
+                ("n_tiles1", C.c_int64),
+                ("t2", C.c_void_p), ("c2", C.c_void_p), ("items2", C.c_void_p),
+                ("n_items2", C.c_int64),
+                ("t3", C.c_void_p), ("s3", C.c_void_p), ("tiles3", C.c_void_p),
+                ("n_tiles3", C.c_int64),
+                ("maps", C.c_void_p), ("stage", C.c_void_p), ("lo_off", C.c_int64),
+                ("y32", C.c_void_p), ("err", C.c_void_p), ("passes", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 _P, _I64, _I32, _D = C.c_void_p, C.c_int64, C.c_int32, C.c_double
@@ -74,6 +91,11 @@ _SIGS = {
     "tnk_scale_div_f64": ([_P, _P, _I64, _P, _D, _P], C.c_int),
     "tnk_apply_two_site_f64_noalloc": ([_P, _P, _P, _P, _P, _P], C.c_int),
     "tnk_noalloc_scratch_elems": ([_P], C.c_int),
+    "tnk_apply_two_site_tc": ([_P, _P, _P, _P], C.c_int),
+    "tnk_stage_f32": ([_P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
+    "tnk_tc_encode_tmaps": ([_P, _P, _I64, _P], C.c_int),
+    "tnk_grouped_gemm_tc": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _P], C.c_int),
+    "tnk_combine_f32": ([_P, _P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
 }
 
 _lib = None

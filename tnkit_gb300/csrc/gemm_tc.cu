@@ -1,0 +1,376 @@
+// Grouped GEMM over charge blocks on the 5th-generation tensor cores (tcgen05, kind::tf32).
+//
+// One CTA computes one 128 x 128 output tile of one task, C = sum_seg A_seg * B_seg^T, where
+// every operand is a K-major FP32 block staged by the host planner in a 16-byte-aligned padded
+// layout. Operand tiles (128 rows x 32 FP32 = one 128-byte swizzle atom) arrive by TMA
+// (cp.async.bulk.tensor.2d, SWIZZLE_128B, out-of-bounds rows/columns zero-filled, so ragged
+// sector blocks need no masking) into a 3-stage shared-memory ring; one elected thread issues
+// tcgen05.mma with the accumulator in TMEM and releases each stage with tcgen05.commit; the
+// epilogue moves the accumulator TMEM -> registers (tcgen05.ld 32x32b) -> global, as FP32 (the
+// next stage's input) or FP64 (the Lanczos vector).
+//
+// PASSES = 3 is the split-precision product A*B ~ Ah*Bh + Ah*Bl + Al*Bh of TF32 "hi" and "lo"
+// parts (each operand stored twice: hi = tf32(x), lo = tf32(x - hi)), accurate to ~1e-6
+// relative with FP32 accumulation; PASSES = 1 is plain TF32.
+//
+// Every mbarrier wait is bounded; on a timeout the CTA records an error code in `err`, skips
+// the rest of its work, waits (bounded) for its own issued operations and frees its TMEM.
+#include <cuda.h>
+
+#include "tnk_internal.cuh"
+
+namespace tnk {
+
+// Segment of the tensor-core grouped GEMM: operand tensor maps (hi at index 2i, lo at 2i+1).
+struct TcSeg {
+    int32_t a_map, b_map, k, pad;
+};
+static_assert(sizeof(TcSeg) == 16, "TcSeg layout");
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int STAGES = 3;
+constexpr int NT = 128;
+constexpr int TILE_BYTES = BM * BK * 4;     // 16 KiB (BN == BM)
+constexpr unsigned WAIT_LIMIT = 1u << 26;   // tries per mbarrier wait (well over a second)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Bounded parity wait: true when the phase completed, false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned i = 0; i < WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Make host-written tensor maps in global memory visible to the tensor-map proxy.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                     reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(const void* p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = 0;
+    d |= (addr & 0x3FFFFull) >> 4;             // start address (16-byte units), bits 0-13
+    d |= (uint64_t)0 << 16;                    // leading byte offset: one swizzle atom on K
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset between 8-row groups
+    d |= (uint64_t)1 << 46;                    // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                    // layout: SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor of kind::tf32: D = F32, A = B = TF32, both K-major, M = 128, N = 128.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+template <int PASSES>
+__global__ void __launch_bounds__(NT, 1)
+gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict__ segs,
+               const tnk_gemm_tile* __restrict__ tiles, const CUtensorMap* __restrict__ maps,
+               void* __restrict__ Cout, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    constexpr int NTILE = (PASSES == 3) ? 4 : 2;        // Ah, Bh (, Al, Bl) per stage
+    uint8_t* base = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* stage_mem = base;
+    uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * NTILE * TILE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* done = empty + STAGES;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+    const tnk_gemm_tile tile = tiles[blockIdx.x];
+    const tnk_gemm_task task = tasks[tile.task];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // total K steps over all segments
+    int nk = 0;
+    for (int s = task.seg_begin; s < task.seg_end; ++s) nk += (segs[s].k + BK - 1) / BK;
+
+    if (threadIdx.x == 0 && nk > 0) {
+        // load cursor over (segment, k0)
+        int ls = task.seg_begin, lk = 0, issued = 0;
+        auto issue = [&](int slot) {
+            while (lk >= segs[ls].k) { ++ls; lk = 0; }
+            const TcSeg g = segs[ls];
+            if (lk == 0) {
+                tmap_acquire(&maps[2 * g.a_map]);
+                tmap_acquire(&maps[2 * g.b_map]);
+                if (PASSES == 3) {
+                    tmap_acquire(&maps[2 * g.a_map + 1]);
+                    tmap_acquire(&maps[2 * g.b_map + 1]);
+                }
+            }
+            uint8_t* st = stage_mem + slot * NTILE * TILE_BYTES;
+            mbar_expect_tx(&full[slot], NTILE * TILE_BYTES);
+            tma_load_2d(st, &maps[2 * g.a_map], &full[slot], lk, tile.m0);
+            tma_load_2d(st + TILE_BYTES, &maps[2 * g.b_map], &full[slot], lk, tile.n0);
+            if (PASSES == 3) {
+                tma_load_2d(st + 2 * TILE_BYTES, &maps[2 * g.a_map + 1], &full[slot], lk, tile.m0);
+                tma_load_2d(st + 3 * TILE_BYTES, &maps[2 * g.b_map + 1], &full[slot], lk, tile.n0);
+            }
+            lk += BK;
+            ++issued;
+        };
+        for (int s = 0; s < STAGES && s < nk; ++s) issue(s);
+        bool ok = true;
+        int consumed = 0;
+        for (int i = 0; i < nk; ++i) {
+            const int slot = i % STAGES;
+            const unsigned ph = (i / STAGES) & 1;
+            if (!mbar_wait(&full[slot], ph)) { ok = false; atomicExch(err, 1); break; }
+            consumed = i + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint8_t* st = stage_mem + slot * NTILE * TILE_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {
+                const uint64_t ah = smem_desc(st + kk * 32);
+                const uint64_t bh = smem_desc(st + TILE_BYTES + kk * 32);
+                mma_tf32(tmem, ah, bh, (i > 0 || kk > 0) ? 1u : 0u);
+                if (PASSES == 3) {
+                    const uint64_t al = smem_desc(st + 2 * TILE_BYTES + kk * 32);
+                    const uint64_t bl = smem_desc(st + 3 * TILE_BYTES + kk * 32);
+                    mma_tf32(tmem, ah, bl, 1u);
+                    mma_tf32(tmem, al, bh, 1u);
+                }
+            }
+            mma_commit(&empty[slot]);
+            if (issued < nk) {
+                if (!mbar_wait(&empty[slot], ph)) { ok = false; atomicExch(err, 2); break; }
+                issue(slot);
+            }
+        }
+        if (!ok) {
+            *abort_flag = 1;
+            // drain: wait (bounded) for the TMA copies this CTA issued and did not consume, so
+            // none lands in shared memory after the CTA has exited
+            for (int j = consumed; j < issued; ++j)
+                mbar_wait(&full[j % STAGES], (j / STAGES) & 1);
+        }
+        mma_commit(done);       // arrives once every MMA issued above has completed
+    }
+    __syncthreads();
+    const bool have_acc = nk > 0;
+    bool acc_ready = true;
+    if (have_acc) acc_ready = mbar_wait(done, 0);
+    if (!acc_ready) atomicExch(err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // CTA-uniform: TMEM loads are .sync.aligned and must be issued by whole warps
+    const int bad = __syncthreads_or((*abort_flag != 0) || !acc_ready);
+
+    // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes)
+    const int row = tile.m0 + warp * 32 + lane;
+    const bool f64 = (task.flags & 2) != 0;
+    const bool row_ok = !bad && row < task.m;
+    const int64_t rbase = task.c_off + (int64_t)row * task.ldc;
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0u;
+        if (have_acc && !bad) {
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                  "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        }
+        if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = tile.n0 + c0 + j;
+                if (col < task.n) {
+                    const float x = __uint_as_float(v[j]);
+                    if (f64)
+                        reinterpret_cast<double*>(Cout)[rbase + col] = (double)x;
+                    else
+                        reinterpret_cast<float*>(Cout)[rbase + col] = x;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(BN)
+                     : "memory");
+    }
+}
+
+constexpr size_t smem_bytes(int passes) {
+    return 1024 + (size_t)STAGES * ((passes == 3) ? 4 : 2) * TILE_BYTES + 256;
+}
+
+}  // namespace
+
+int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
+                   int64_t n_tiles, const void* maps, void* C, int* err, int passes,
+                   cudaStream_t stream) {
+    if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3)) {
+        set_error("tc gemm: bad tile count %lld or passes %d", (long long)n_tiles, passes);
+        return TNK_ERR_ARG;
+    }
+    if (n_tiles == 0) return TNK_OK;
+    if (!tasks || !segs || !tiles || !maps || !C || !err) {
+        set_error("tc gemm: null argument");
+        return TNK_ERR_ARG;
+    }
+    if ((reinterpret_cast<uintptr_t>(maps) & 63) != 0) {
+        set_error("tc gemm: tensor maps must be 64-byte aligned");
+        return TNK_ERR_ARG;
+    }
+    const size_t sm = smem_bytes(passes);
+    cudaError_t e;
+    if (passes == 3) {
+        e = cudaFuncSetAttribute(gemm_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm);
+        if (e != cudaSuccess) {
+            set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
+            return TNK_ERR_CUDA;
+        }
+        gemm_tc_kernel<3><<<(unsigned)n_tiles, NT, sm, stream>>>(
+            tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
+    } else {
+        e = cudaFuncSetAttribute(gemm_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm);
+        if (e != cudaSuccess) {
+            set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
+            return TNK_ERR_CUDA;
+        }
+        gemm_tc_kernel<1><<<(unsigned)n_tiles, NT, sm, stream>>>(
+            tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
+    }
+    return check_launch("gemm_tc_kernel");
+}
+
+// --------------------------------------------------------------------------------------------
+// Tensor-map encoding (host): one 2-D map per staged operand block, FP32, box 32 x 128,
+// SWIZZLE_128B, zero fill out of bounds. The driver entry point is looked up once.
+// --------------------------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn get_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out) {
+    EncodeTiledFn enc = get_encoder();
+    if (!enc) {
+        set_error("tensor maps: cuTensorMapEncodeTiled is unavailable");
+        return TNK_ERR_DEVICE;
+    }
+    CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(out);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t off = desc[4 * i], rows = desc[4 * i + 1], cols = desc[4 * i + 2],
+                      ld = desc[4 * i + 3];
+        const float* p = base + off;
+        if ((reinterpret_cast<uintptr_t>(p) & 15) != 0 || (ld * 4) % 16 != 0 || rows < 1 ||
+            cols < 1 || ld < cols) {
+            set_error("tensor map %lld: misaligned or bad extents (off %lld, ld %lld)",
+                      (long long)i, (long long)off, (long long)ld);
+            return TNK_ERR_ARG;
+        }
+        cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+        cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+        cuuint32_t box[2] = {BK, BM};
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = enc(&maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)p, dims, strides,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            set_error("tensor map %lld: cuTensorMapEncodeTiled error %d", (long long)i, (int)r);
+            return TNK_ERR_ARG;
+        }
+    }
+    return TNK_OK;
+}
+
+}  // namespace tnk

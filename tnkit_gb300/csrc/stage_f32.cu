@@ -1,0 +1,148 @@
+// Staging kernels of the tensor-core matvec (sm_103a):
+//
+//  * cvt_split_kernel: FP64 canonical blocks -> FP32 TF32-split operands in the padded, K-major
+//    layout the TMA loads (optionally transposing a block), hi = tf32(x) at dst, lo =
+//    tf32(x - hi) at dst + lo_off. 32 x 32 tiles through shared memory keep both the FP64 reads
+//    and the FP32 writes coalesced when a block is transposed.
+//  * comb_f32_kernel: stage 2 of the mixed matvec (the MPO coefficients) on FP32 data, writing
+//    the hi/lo split of its result when the next stage is a split-precision GEMM.
+#include "tnk_internal.cuh"
+
+namespace tnk {
+
+// One staged block: source (rows x cols, row stride src_ld) -> destination (cols x rows when
+// transposed, row stride dst_ld).
+struct CvtTask {
+    int64_t src_off, dst_off;
+    int32_t rows, cols, src_ld, dst_ld;
+    int32_t transpose, pad;
+};
+static_assert(sizeof(CvtTask) == 40, "CvtTask layout");
+
+struct CvtItem {
+    int32_t task, r0, c0, pad;
+};
+
+namespace {
+
+__device__ __forceinline__ float tf32_hi(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// grid: one CTA per 32 x 32 source tile (items); 32 x 8 threads
+__global__ void __launch_bounds__(256)
+cvt_split_kernel(const CvtTask* __restrict__ tasks, const CvtItem* __restrict__ items,
+                 const double* __restrict__ src, float* __restrict__ dst, int64_t lo_off,
+                 int split) {
+    __shared__ double tile[32][33];
+    const CvtItem it = items[blockIdx.x];
+    const CvtTask t = tasks[it.task];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    // load 32 x 32 source tile (rows r0.., cols c0..), coalesced along columns
+    for (int i = ty; i < 32; i += 8) {
+        const int r = it.r0 + i, c = it.c0 + tx;
+        tile[i][tx] = (r < t.rows && c < t.cols) ? src[t.src_off + (int64_t)r * t.src_ld + c]
+                                                 : 0.0;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+        int r, c;
+        double x;
+        if (t.transpose) {      // destination row = source column
+            r = it.c0 + i;      // dst row
+            c = it.r0 + tx;     // dst col
+            if (r >= t.cols || c >= t.rows) continue;
+            x = tile[tx][i];
+        } else {
+            r = it.r0 + i;
+            c = it.c0 + tx;
+            if (r >= t.rows || c >= t.cols) continue;
+            x = tile[i][tx];
+        }
+        const int64_t o = t.dst_off + (int64_t)r * t.dst_ld + c;
+        const float h = split ? tf32_hi((float)x) : (float)x;
+        dst[o] = h;
+        if (split) dst[lo_off + o] = tf32_hi((float)(x - (double)h));
+    }
+}
+
+constexpr int NT = 256;
+constexpr int TERMS_SMEM = 64;
+
+__global__ void __launch_bounds__(NT)
+comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __restrict__ terms,
+                const tnk_comb_item* __restrict__ items, const float* __restrict__ src,
+                float* __restrict__ dst, int64_t lo_off, int split) {
+    __shared__ tnk_comb_term st[TERMS_SMEM];
+    const tnk_comb_item item = items[blockIdx.x];
+    const tnk_comb_task t = tasks[item.task];
+    const int cols = t.cols;
+    const int64_t nel = (int64_t)(item.row1 - item.row0) * cols;
+    const int nterm = t.term_end - t.term_begin;
+    // accumulate in FP32 registers per element over all terms (chunks of TERMS_SMEM)
+    for (int64_t e0 = 0; e0 < nel; e0 += NT) {
+        const int64_t e = e0 + threadIdx.x;
+        const bool live = e < nel;
+        const int r = live ? item.row0 + (int)(e / cols) : 0;
+        const int c = live ? (int)(e % cols) : 0;
+        float acc = 0.f;
+        for (int t0 = 0; t0 < nterm; t0 += TERMS_SMEM) {
+            const int nt = min(TERMS_SMEM, nterm - t0);
+            __syncthreads();
+            if (threadIdx.x < nt) st[threadIdx.x] = terms[t.term_begin + t0 + threadIdx.x];
+            __syncthreads();
+            if (live)
+                for (int q = 0; q < nt; ++q)
+                    acc = fmaf((float)st[q].coef,
+                               src[st[q].src_off + (int64_t)r * st[q].src_ld +
+                                   (int64_t)c * st[q].src_cs],
+                               acc);
+        }
+        if (live) {
+            const int64_t o = t.dst_off + (int64_t)r * t.dst_ld + (int64_t)c * t.dst_cs;
+            const float h = split ? tf32_hi(acc) : acc;
+            dst[o] = h;
+            if (split) dst[lo_off + o] = tf32_hi(acc - h);
+        }
+    }
+}
+
+}  // namespace
+
+int launch_cvt_split(const CvtTask* tasks, const CvtItem* items, int64_t n_items,
+                     const double* src, float* dst, int64_t lo_off, int split,
+                     cudaStream_t stream) {
+    if (n_items < 0 || n_items > 0x7fffffff) {
+        set_error("convert: bad item count");
+        return TNK_ERR_ARG;
+    }
+    if (n_items == 0) return TNK_OK;
+    if (!tasks || !items || !src || !dst) {
+        set_error("convert: null argument");
+        return TNK_ERR_ARG;
+    }
+    cvt_split_kernel<<<(unsigned)n_items, 256, 0, stream>>>(tasks, items, src, dst, lo_off,
+                                                            split);
+    return check_launch("cvt_split_kernel");
+}
+
+int launch_comb_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
+                    const tnk_comb_item* items, int64_t n_items, const float* src, float* dst,
+                    int64_t lo_off, int split, cudaStream_t stream) {
+    if (n_items < 0 || n_items > 0x7fffffff) {
+        set_error("combine f32: bad item count");
+        return TNK_ERR_ARG;
+    }
+    if (n_items == 0) return TNK_OK;
+    if (!tasks || !items || !src || !dst) {
+        set_error("combine f32: null argument");
+        return TNK_ERR_ARG;
+    }
+    comb_f32_kernel<<<(unsigned)n_items, NT, 0, stream>>>(tasks, terms, items, src, dst, lo_off,
+                                                          split);
+    return check_launch("comb_f32_kernel");
+}
+
+}  // namespace tnk

@@ -101,9 +101,13 @@ class _Dev:
 
 def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8,
                            max_iter: int = 200, m: int = 40, k: int = 10,
-                           timers: Optional[dict] = None, basis: Optional[torch.Tensor] = None):
+                           timers: Optional[dict] = None, basis: Optional[torch.Tensor] = None,
+                           stall: int = 0):
     """Lowest eigenpair of the operator `matvec(x, out) -> out` from the start `v0` (float64
-    CUDA vector). Returns (theta, x, info) like the reference; x is normalised."""
+    CUDA vector). Returns (theta, x, info) like the reference; x is normalised.
+
+    stall > 0 also stops when the Ritz residual has improved by less than 10 % over the last
+    `stall` iterations (info["stalled"]): the floor of a low-precision operator."""
     if k >= m:
         k = max(1, m // 2)
     if m + 1 > _MAXNV:
@@ -128,6 +132,8 @@ def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8
     theta, y = 0.0, np.array([1.0])
     converged, restarts, it, j = False, 0, 0, 0
     keep = []
+    hist = []
+    stalled = False
     tm = timers if timers is not None else None
     while it < max_iter:
         t0 = time.perf_counter() if tm is not None else 0.0
@@ -162,6 +168,11 @@ def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8
         if breakdown or res < tol:
             converged = True
             break
+        if stall:
+            hist.append(res)
+            if len(hist) > stall and res > 0.9 * hist[-stall - 1]:
+                stalled = True
+                break
         if cur >= m:                                 # thick restart
             ev, evec = np.linalg.eigh(T[:cur, :cur])
             kk = min(k, cur - 1)
@@ -194,4 +205,5 @@ def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8
     D.nrm2(x, 3)
     D.scale_div(x, x, 3)
     del keep
-    return theta, x, {"iters": it, "converged": converged, "restarts": restarts}
+    return theta, x, {"iters": it, "converged": converged, "restarts": restarts,
+                      "stalled": stalled, "residual": res if it else None}

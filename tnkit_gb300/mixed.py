@@ -1,0 +1,136 @@
+"""Mixed-precision local solve: tensor-core matvecs for the bulk of Lanczos, FP64 polish.
+
+The two-site H_eff is applied on the tcgen05 tensor cores (TF32 inputs, FP32 accumulation in
+TMEM; by default each operand split into TF32 hi/lo parts, three MMAs per product, ~1e-6
+relative), with FP64 vectors in and out. Lanczos itself -- reorthogonalisation, the projected
+eigenproblem, norms and dot products -- stays FP64, as in the reference's
+`lanczos_ground_mixed` (tnkit/eigensolver.py:677-725): stage 1 converges the Ritz residual with
+the cheap matvec to `tol_lo` (or until the residual stops improving, the floor the TF32 operator
+allows), stage 2 restarts FP64 Lanczos from that vector to `tol` (at most `polish` iterations
+when given). The reference refuses this mode on block tensors (tnkit/_dmrg.py:531-532); here it
+runs on the U(1) block layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import plan as P
+from .lanczos import lanczos_ground_restart
+from .layout import Layout
+from .ops import _host_of, _pack, plan_two_site
+from .tensor import BlockTensor
+
+
+class TwoSiteOperatorTC:
+    """H_eff of one bond on the tensor cores, as `op(x, out)` on FP64 canonical buffers."""
+
+    def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                 R: BlockTensor, passes: int = 3):
+        if passes not in (1, 3):
+            raise ValueError("passes must be 1 (TF32) or 3 (split TF32)")
+        dev = L.data.device
+        self.device = dev
+        self.passes = passes
+        p64 = plan_two_site(theta_layout, L, W1, W2, R, dev)
+        tc = P.HostPlanTC(p64.host, theta_layout, L.layout, R.layout)
+        self.host = tc
+        self.macs = tc.macs
+        self.n = theta_layout.size
+        self.stage = torch.empty(2 * tc.stage_elems, dtype=torch.float32, device=dev)
+        self.y32 = torch.empty(max(tc.y32_elems, 1), dtype=torch.float32, device=dev)
+        self.err = torch.zeros(16, dtype=torch.int32, device=dev)
+        lib = _lib.lib()
+        desc = np.ascontiguousarray(tc.map_desc())
+        nmaps = desc.shape[0]
+        maps_host = np.zeros(max(nmaps, 1) * 128, np.uint8)
+        _lib.check(lib.tnk_tc_encode_tmaps(self.stage.data_ptr(), desc.ctypes.data, nmaps,
+                                           maps_host.ctypes.data), "tnk_tc_encode_tmaps")
+        arrays = [maps_host, tc.cvt["T"], tc.cvt_items["T"], tc.t1, tc.s1, tc.tiles1, tc.t2,
+                  tc.c2, tc.items2, tc.t3, tc.s3, tc.tiles3, tc.cvt["L"], tc.cvt_items["L"],
+                  tc.cvt["R"], tc.cvt_items["R"]]
+        self.buf, offs = _pack(arrays, dev)
+        a = [self.buf.data_ptr() + o for o in offs]
+        self.c = _lib.TcPlan(a[1], a[2], len(tc.cvt_items["T"]),
+                             a[3], a[4], a[5], len(tc.tiles1),
+                             a[6], a[7], a[8], len(tc.items2),
+                             a[9], a[10], a[11], len(tc.tiles3),
+                             a[0], self.stage.data_ptr(), tc.stage_elems,
+                             self.y32.data_ptr(), self.err.data_ptr(), passes, 0)
+        sp = _lib.stream_ptr()
+        split = 1 if passes == 3 else 0
+        _lib.check(lib.tnk_stage_f32(a[12], a[13], len(tc.cvt_items["L"]), L.data.data_ptr(),
+                                     self.stage.data_ptr(), tc.stage_elems, split, sp),
+                   "stage L")
+        _lib.check(lib.tnk_stage_f32(a[14], a[15], len(tc.cvt_items["R"]), R.data.data_ptr(),
+                                     self.stage.data_ptr(), tc.stage_elems, split, sp),
+                   "stage R")
+        self.L, self.R = L, R        # staged copies were taken; keep the sources alive anyway
+        self.calls = 0
+
+    def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        y = torch.empty_like(x) if out is None else out
+        _lib.check(_lib.lib().tnk_apply_two_site_tc(C.byref(self.c), x.data_ptr(), y.data_ptr(),
+                                                    _lib.stream_ptr()), "tnk_apply_two_site_tc")
+        self.calls += 1
+        return y
+
+    def check_device_error(self):
+        """Raise if a kernel of this operator recorded a timed-out wait (reads one word)."""
+        e = int(self.err[0].item())
+        if e:
+            raise _lib.TnkError(_lib.TNK_ERR_CUDA, "tcgen05 grouped GEMM",
+                                f"a bounded wait timed out (code {e}); results are invalid")
+
+
+def _fp64_residual(op64, v: torch.Tensor):
+    """(rayleigh quotient, residual norm) of v in FP64: one FP64 matvec."""
+    w = op64(v)
+    nv = float(torch.linalg.vector_norm(v))
+    th = float(torch.dot(v, w)) / (nv * nv)
+    r = float(torch.linalg.vector_norm(w - th * v)) / nv
+    return th, r
+
+
+def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                 R: BlockTensor, op64, v0: torch.Tensor, tol: float = 1e-9,
+                 max_iter: int = 200, m: int = 40, k: int = 10, tol_lo: float = 1e-4,
+                 basis=None, counts=None, passes: int = 3, polish: Optional[int] = None,
+                 switch: float = 10.0):
+    """Lowest eigenpair of H_eff: tensor-core Lanczos to tol_lo, then FP64 Lanczos to tol.
+
+    The warm start's FP64 residual is checked first (one FP64 matvec): a start already within
+    `switch` * tol_lo of convergence -- late sweeps -- goes straight to the FP64 solve, which
+    needs few iterations there and which the tensor-core operator (relative accuracy ~1e-6)
+    could not improve; a start farther out -- the opening sweeps, bond growth -- spends its
+    many iterations on the tensor cores."""
+    c0 = getattr(op64, "calls", 0)
+    th0, r0 = _fp64_residual(op64, v0)
+    n_lo = 0
+    e_lo = th0
+    x = v0
+    if r0 < tol:
+        e, info_hi = th0, {"iters": 0, "converged": True}
+        nrm = torch.linalg.vector_norm(v0)
+        x = v0 / nrm
+    else:
+        if r0 >= switch * tol_lo:
+            op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
+            e_lo, x, info_lo = lanczos_ground_restart(op_lo, v0, tol=max(tol_lo, tol),
+                                                      max_iter=max_iter, m=m, k=k, basis=basis,
+                                                      stall=8)
+            op_lo.check_device_error()
+            n_lo = op_lo.calls
+        e, x, info_hi = lanczos_ground_restart(op64, x, tol=tol,
+                                               max_iter=max_iter if polish is None else polish,
+                                               m=m, k=k, basis=basis)
+    n_hi = getattr(op64, "calls", 0) - c0
+    if counts is not None:
+        counts["lo"] = counts.get("lo", 0) + n_lo
+        counts["hi"] = counts.get("hi", 0) + n_hi
+    return e, x, {"iters": info_hi["iters"], "converged": info_hi["converged"], "e_lo": e_lo,
+                  "r0": r0, "n_lo": n_lo, "n_hi": n_hi, "matvecs": n_lo + n_hi}

@@ -660,3 +660,145 @@ def two_site_ref_macs(theta: Layout, L: Layout, W1: Layout, W2: Layout, R: Layou
     x3 = canonical(l3, theta.charge)
     m4, _ = tdot(R, (1, 2), x3, (0, 4))
     return [m1, m2, m3, m4] if parts else m1 + m2 + m3 + m4
+
+
+# --------------------------------------------------------------------------- #
+# tensor-core (tcgen05, TF32) version of the two-site plan
+# --------------------------------------------------------------------------- #
+TC_TILE = 128             # must match gemm_tc.cu
+TC_ALIGN = 32             # staged block bases: 32 floats = 128 bytes (TMA needs 16)
+
+
+def _rup(x: int, a: int) -> int:
+    return (int(x) + a - 1) // a * a
+
+
+def _tiles(tasks, segs, tile):
+    out, cost = [], []
+    for t, task in enumerate(tasks):
+        m, n = int(task["m"]), int(task["n"])
+        ktot = int(segs[int(task["seg_begin"]):int(task["seg_end"])]["k"].sum()) or 1
+        for m0 in range(0, m, tile):
+            for n0 in range(0, n, tile):
+                out.append((t, m0, n0, 0))
+                cost.append(ktot)
+    order = np.argsort(-np.asarray(cost, np.int64), kind="stable") if out else []
+    return (np.array([out[i] for i in order], dtype=GEMM_TILE) if out
+            else np.zeros(0, GEMM_TILE))
+
+
+def _cvt_items(tasks):
+    from ._lib import CVT_ITEM
+    items = []
+    for t, (src_off, dst_off, rows, cols, *_r) in enumerate(tasks):
+        for r0 in range(0, rows, 32):
+            for c0 in range(0, cols, 32):
+                items.append((t, r0, c0, 0))
+    return np.array(items, dtype=CVT_ITEM) if items else np.zeros(0, CVT_ITEM)
+
+
+class HostPlanTC:
+    """The two-site plan re-laid out for the tensor cores: every GEMM operand a K-major FP32
+    block at a 128-byte-aligned offset of one staging buffer with a 16-byte-multiple row stride
+    (theta stored transposed so that it, too, is K-major), tensor-map descriptors of those
+    blocks, and the FP64 -> FP32 staging tasks of L, R (once per local problem) and theta (every
+    matvec). Derived from the FP64 plan `hp`, whose block structure it keeps."""
+
+    def __init__(self, hp: HostPlan3, theta: Layout, L: Layout, R: Layout):
+        from ._lib import CVT_TASK, TC_SEG
+        (t1, s1, _), (t2, c2, i2), (t3, s3, _) = hp.g1, hp.c2, hp.g3
+        self.cursor = 0
+        self.maps: List[tuple] = []
+        map_of: Dict[tuple, int] = {}
+        cvt = {"L": [], "R": [], "T": []}
+
+        def alloc(n):
+            o = self.cursor
+            self.cursor += _rup(n, TC_ALIGN)
+            return o
+
+        def staged(kind, src_off, rows, cols, transpose=False):
+            """Map index of the staged block (source rows x cols at src_off, row-major)."""
+            key = (kind, int(src_off))
+            if key not in map_of:
+                r, c = (cols, rows) if transpose else (rows, cols)
+                ld = _rup(c, 4)
+                off = alloc(r * ld)
+                if kind in cvt:
+                    cvt[kind].append((int(src_off), off, rows, cols, cols, ld,
+                                      1 if transpose else 0, 0))
+                map_of[key] = len(self.maps)
+                self.maps.append((off, r, c, ld))
+            return map_of[key]
+
+        # stage 1: Y = L theta; A = L block (m x k), B = theta block (k x n) staged as (n x k)
+        T1, S1 = [], []
+        for t in t1:
+            sb, se = int(t["seg_begin"]), int(t["seg_end"])
+            segs = []
+            for s in s1[sb:se]:
+                k = int(s["k"])
+                am = staged("L", s["a_off"], int(t["m"]), k)
+                bm = staged("T", s["b_off"], k, int(t["n"]), transpose=True)
+                segs.append((am, bm, k, 0))
+            T1.append((int(t["c_off"]), int(t["ldc"]), int(t["m"]), int(t["n"]), len(S1),
+                       len(S1) + len(segs), 0))
+            S1.extend(segs)
+        # Z blocks (stage-3 A operands) in the staging buffer
+        zinfo: Dict[int, tuple] = {}
+        for t in t3:
+            for s in s3[int(t["seg_begin"]):int(t["seg_end"])]:
+                zo = int(s["a_off"])
+                if zo not in zinfo:
+                    K, M = int(s["k"]), int(t["m"])
+                    mi = staged("Z", zo, M, K)
+                    zinfo[zo] = (K, M, mi)
+        zkeys = np.array(sorted(zinfo), dtype=np.int64)
+        # stage 2: remap destinations into the padded Z blocks (sources: Y32 = Y's layout)
+        T2 = []
+        for t in t2:
+            d = int(t["dst_off"])
+            j = int(np.searchsorted(zkeys, d, side="right")) - 1
+            zo = int(zkeys[j])
+            K, M, mi = zinfo[zo]
+            off, rows, cols, ld = self.maps[mi]
+            rel = d - zo
+            row, col = divmod(rel, K)
+            if int(t["dst_ld"]) % K:
+                raise AssertionError("stage-2 destination stride is not a whole number of rows")
+            T2.append((off + row * ld + col, int(t["rows"]), int(t["cols"]),
+                       int(t["dst_ld"]) // K * ld, int(t["dst_cs"]), int(t["term_begin"]),
+                       int(t["term_end"])))
+        # stage 3: out = Z R^T, A = Z block (m x K), B = R block (n x K), FP64 output
+        T3, S3 = [], []
+        for t in t3:
+            segs = []
+            for s in s3[int(t["seg_begin"]):int(t["seg_end"])]:
+                K = int(s["k"])
+                am = zinfo[int(s["a_off"])][2]
+                bm = staged("R", s["b_off"], int(t["n"]), K)
+                segs.append((am, bm, K, 0))
+            T3.append((int(t["c_off"]), int(t["ldc"]), int(t["m"]), int(t["n"]), len(S3),
+                       len(S3) + len(segs), 2))
+            S3.extend(segs)
+        mk = lambda rows, dt: np.array(rows, dtype=dt) if rows else np.zeros(0, dt)
+        self.t1, self.s1 = mk(T1, GEMM_TASK), mk(S1, TC_SEG)
+        self.t3, self.s3 = mk(T3, GEMM_TASK), mk(S3, TC_SEG)
+        self.tiles1 = _tiles(self.t1, self.s1, TC_TILE)
+        self.tiles3 = _tiles(self.t3, self.s3, TC_TILE)
+        self.t2 = mk(T2, COMB_TASK)
+        self.c2, self.items2 = c2, i2
+        self.cvt = {k: mk(v, CVT_TASK) for k, v in cvt.items()}
+        self.cvt_items = {k: _cvt_items(v) for k, v in cvt.items()}
+        self.stage_elems = _rup(self.cursor, TC_ALIGN)    # hi region; lo at +stage_elems
+        self.y32_elems = hp.ws1
+        self.out_layout = hp.out_layout
+        self.macs = hp.macs
+
+    def map_desc(self) -> np.ndarray:
+        """(offset, rows, cols, ld) of every tensor map, hi and lo interleaved."""
+        d = np.zeros((2 * len(self.maps), 4), np.int64)
+        for i, (off, r, c, ld) in enumerate(self.maps):
+            d[2 * i] = (off, r, c, ld)
+            d[2 * i + 1] = (off + self.stage_elems, r, c, ld)
+        return d
