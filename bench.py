@@ -161,6 +161,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--sweep", action="store_true",
+                    help="also run the whole chi=1024 DMRG (6 sweeps, FP64 and mixed): minutes")
+    ap.add_argument("--sweep-chi", type=int, default=1024)
+    ap.add_argument("--sweep-n", type=int, default=64)
+    ap.add_argument("--sweeps", type=int, default=6)
+    ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()
@@ -320,6 +326,11 @@ def main():
                     "d2h_bytes_per_step": x.numel() * 8, "max_rel_err_vs_device": err_e2e},
             "gpu_launches": 3 * args.steps,
             "clocks": clocks}
+    line["mixed"] = mixed_leg(torch, dev, th, L, W1, W2, R, y, flush, flops_ref, parts,
+                              args.steps, ms)
+    line["gpu_launches"] += 4 * args.steps
+    if args.sweep:
+        line["sweep"] = sweep_leg(torch, args)
     if not args.no_cpu:
         dt, reps = cpu_matvec_baseline(th, L, W1, W2, R)
         line["cpu_baseline"] = {"value": flops_ref / dt / 1e9, "unit": "GFLOP/s",
@@ -329,6 +340,107 @@ def main():
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
+
+
+def _peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps, ms64):
+    """The same matvec on the tensor cores (tcgen05, split TF32, FP32 accumulation)."""
+    import ctypes as C
+    from tnkit_gb300 import _lib
+    from tnkit_gb300.mixed import TwoSiteOperatorTC
+    op = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=3)
+    x = th.data
+    y = torch.empty_like(x)
+    for _ in range(3):
+        op(x, y)
+    torch.cuda.synchronize()
+    err = float((y - y64).abs().max() / y64.abs().max())
+    stream = torch.cuda.current_stream()
+    t = 0.0
+    for i in range(steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        op(x, y)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t += a.elapsed_time(b) / 1e3
+    # the two tcgen05 GEMM stages alone, same stream, CUDA events around each launch
+    lib = _lib.lib()
+    c = op.c
+    sp = _lib.stream_ptr()
+    tg = 0.0
+    nrep = max(5, steps // 2)
+    for i in range(nrep):
+        flush.fill_(float(i))
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_tc(c.t1, c.s1, c.tiles1, c.n_tiles1, c.maps, c.y32,
+                                           c.err, 3, sp), "tc1")
+        e[1].record(stream)
+        _lib.check(lib.tnk_combine_f32(c.t2, c.c2, c.items2, c.n_items2, c.y32, c.stage,
+                                       c.lo_off, 1, sp), "comb32")
+        e[2].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_tc(c.t3, c.s3, c.tiles3, c.n_tiles3, c.maps,
+                                           y.data_ptr(), c.err, 3, sp), "tc3")
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        tg += (e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])) / 1e3
+    tg /= nrep
+    op.check_device_error()
+    bf16, src = _peaks()
+    tf32_peak = bf16 / 2.0
+    alg = 2 * (parts[0] + parts[3]) / tg / 1e12
+    mms = t / steps * 1e3
+    return {"value": flops_ref * steps / t / 1e9, "unit": "GFLOP/s", "ms_per_step": mms,
+            "speedup_vs_fp64": ms64 / mms, "max_rel_err_vs_fp64": err, "dtype": "tf32x3/f32",
+            "roofline": {"bound": "tensor", "kernel": "gemm_tc_kernel (tcgen05 kind::tf32, "
+                                                      "stages 1+3)",
+                         "achieved": alg, "mma_issued": 3 * alg, "peak": tf32_peak,
+                         "unit": "TFLOP/s", "frac": alg / tf32_peak,
+                         "peak_source": f"dense TF32 = bf16 ({src}, {bf16:.0f} TFLOP/s) / 2",
+                         "traffic": None, "gemm_ms": tg * 1e3}}
+
+
+def sweep_leg(torch, args):
+    """The whole U(1) XXZ DMRG at chi (6 sweeps, seed 1, expand 0) in FP64 and mixed precision,
+    with the reference's own FP64 result (tests/golden/c2_xxz_n64_chi1024.json) as the oracle."""
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.dmrg import dmrg
+    from tnkit_gb300.mpo import to_block_mpo
+    N, chi = args.sweep_n, args.sweep_chi
+    out = {"workload": f"U(1) XXZ N={N} chi={chi}, {args.sweeps} sweeps, seed 1, expand 0, "
+                       f"truncation '{args.svd_method}'"}
+    ref = None
+    gp = os.path.join(HERE, "tests", "golden", "c2_xxz_n64_chi1024.json")
+    if N == 64 and chi == 1024 and os.path.exists(gp):
+        ref = json.load(open(gp))
+        out["reference_E"] = ref["E"]
+        out["reference_sweep_s"] = ref["sweep_s"]
+    for prec in ("f64", "mixed"):
+        Wb = to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, M, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=args.sweeps, tol=0, rtol=0,
+                          expand=0, precision=prec, svd_method=args.svd_method)
+        torch.cuda.synchronize()
+        rec = {"E": E, "energies": info["energies"], "sweep_s": info["sweep_s"],
+               "total_s": time.perf_counter() - t0, "phase_time": info["phase_time"],
+               "matvecs": info["mixed_counts"], "discarded_weight": info["discarded_weight"]}
+        if ref is not None:
+            rec["abs_dE_vs_reference"] = abs(E - ref["E"])
+        out[prec] = rec
+    out["abs_dE_mixed_vs_f64"] = abs(out["mixed"]["E"] - out["f64"]["E"])
+    out["speedup_total"] = out["f64"]["total_s"] / out["mixed"]["total_s"]
+    return out
 
 
 if __name__ == "__main__":

@@ -54,6 +54,7 @@ class DMRGOptions:
     polish: int = 2                  # FP64 polish restarts allowed after the mixed stage
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
+    svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
 
 
 def _resolve(options, kw) -> DMRGOptions:
@@ -190,7 +191,7 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         t0 = time.perf_counter()
         mat, info = LA.fuse_matrix(x, 2)
         U, S, Vh, disc = LA.truncated_svd(mat, chi, scale="right" if right else "left",
-                                          driver=o.svd_driver)
+                                          driver=o.svd_driver, method=o.svd_method)
         M[i] = LA.split_rows(U, info)
         M[i + 1] = LA.split_cols(Vh, info)
         total_disc += disc

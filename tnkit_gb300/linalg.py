@@ -13,6 +13,8 @@ kept in FP64 on the GPU; only the singular values cross to the host, once per bo
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
+import threading
 from typing import Tuple
 
 import numpy as np
@@ -74,7 +76,77 @@ def _row_label(leg: Leg, r: int):
     return tuple(-x for x in q) if isinstance(q, tuple) else -q
 
 
-def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None):
+class _Concurrent:
+    """Per-sector factorisations issued from a thread pool, one CUDA stream per sector: the
+    cuSOLVER calls of one bond (a dozen sectors of a few hundred rows at chi = 1024) are
+    latency-bound one by one and overlap well."""
+
+    def __init__(self, workers: int = 16):
+        self.pool = cf.ThreadPoolExecutor(workers, thread_name_prefix="tnk-svd")
+        self.streams = {}
+        self.lock = threading.Lock()
+
+    def stream(self, device, i):
+        with self.lock:
+            key = (str(device), i)
+            if key not in self.streams:
+                self.streams[key] = torch.cuda.Stream(device=device)
+            return self.streams[key]
+
+    def map(self, fn, mats, device):
+        main = torch.cuda.current_stream(device)
+        streams = [self.stream(device, i) for i in range(len(mats))]
+        for s in streams:
+            s.wait_stream(main)
+
+        def run(i):
+            with torch.cuda.stream(streams[i]):
+                out = fn(mats[i])
+                for t in out:
+                    t.record_stream(main)
+                return out
+        res = list(self.pool.map(run, range(len(mats))))
+        for s in streams:
+            main.wait_stream(s)
+        return res
+
+
+_CONC = None
+
+
+def _concurrent() -> _Concurrent:
+    global _CONC
+    if _CONC is None:
+        _CONC = _Concurrent()
+    return _CONC
+
+
+def _svd_gram(M: torch.Tensor):
+    """U, S (descending), Vh of one block through the smaller Gram matrix: Hermitian eigh, then
+    a QR that re-orthonormalises the computed singular vectors (the reference's method='gram',
+    tnkit/blocks.py:1345-1377). Singular values below ~1e-8 of the largest are not resolved."""
+    R, C = M.shape
+    if R >= C:
+        w, V = torch.linalg.eigh(M.transpose(0, 1) @ M)
+        V = torch.flip(V, (-1,))
+        Q, Rr = torch.linalg.qr(M @ V)
+    else:
+        w, U = torch.linalg.eigh(M @ M.transpose(0, 1))
+        U = torch.flip(U, (-1,))
+        Q, Rr = torch.linalg.qr(M.transpose(0, 1) @ U)
+    d = torch.diagonal(Rr)
+    S = d.abs()
+    Q = Q * torch.where(S > 0, d / torch.where(S > 0, S, torch.ones_like(S)),
+                        torch.ones_like(S))
+    o = torch.argsort(S, descending=True, stable=True)
+    S, Q = S[o], Q[:, o]
+    if R >= C:
+        return Q.contiguous(), S, V[:, o].transpose(0, 1).contiguous()
+    return U[:, o].contiguous(), S, Q.transpose(0, 1).contiguous()
+
+
+def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
+                  method: str = "svd"):
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
@@ -82,10 +154,19 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None):
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
     lr, lc = m.layout.legs
-    parts = []
-    for r, c, M in _blocks(m):
-        U, S, Vh = torch.linalg.svd(M, full_matrices=False, driver=driver)
-        parts.append((r, c, U, S, Vh))
+    blocks = list(_blocks(m))
+    if method == "gram":
+        fn = _svd_gram
+    elif method == "svd":
+        fn = lambda M: torch.linalg.svd(M, full_matrices=False, driver=driver)
+    else:
+        raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
+    mats = [M for _, _, M in blocks]
+    if len(mats) > 1 and m.data.is_cuda:
+        facs = _concurrent().map(fn, mats, m.data.device)
+    else:
+        facs = [fn(M) for M in mats]
+    parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh) in zip(blocks, facs)]
     if not parts:
         raise ValueError("the matrix has no allowed blocks")
     s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
