@@ -136,6 +136,16 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def reduce_max(values, device="cpu"):
+    """Elementwise max of per-rank values over the process group (identity without one)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def measure_dgemm_peak(torch, dev):
     n = 8192
     a = torch.randn(n, n, dtype=torch.float64, device=dev)
@@ -285,10 +295,7 @@ def main():
     err_e2e = float((h_out.to(dev) - y).abs().max() / y.abs().max())
 
     # max over ranks
-    tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    t_dev, t_e2e = float(tt[0]), float(tt[1])
+    t_dev, t_e2e = reduce_max([t_dev, t_e2e], dev)
     if rank != 0:
         dist.barrier()
         return
