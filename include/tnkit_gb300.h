@@ -39,7 +39,9 @@ extern "C" {
 
 /* One output matrix of a grouped GEMM: C(i, j) at c_off + i*ldc + j, i < m, j < n.
  * C = sum over segments [seg_begin, seg_end) of coef * A_seg * B_seg; with no segment the
- * output is zero-filled. flags bit 0: accumulate into C instead of overwriting it. */
+ * output is zero-filled. flags bit 0: accumulate into C instead of overwriting it; bit 1: FP64
+ * output of a tensor-core stage; bit 2: output column stride 2 (one half of interleaved
+ * complex128 data, C(i, j) at c_off + i*ldc + 2*j). */
 typedef struct {
     int64_t c_off;
     int32_t ldc, m, n;
@@ -256,6 +258,26 @@ int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, doubl
 /* y = x * (f / s[0]) (normalisation by a device scalar). */
 int tnk_scale_div_f64(const double* x, double* y, int64_t n, const double* s, double f,
                       void* stream);
+
+/* ----------------------------------------------------------------------------------------
+ * Complex128 Lanczos kernels (interleaved re/im doubles; n counts complex entries). They serve
+ * the Krylov exponential of two-site TDVP (tnkit/eigensolver.py:282-349, block twin
+ * tnkit/block_lanczos.py:76-121): vdot conjugates its first argument, as the reference's does.
+ * Complex matvecs and environment updates use the FP64 entry points above on plans whose
+ * segments and outputs address the real and imaginary halves separately (flags bit 2).
+ * ---------------------------------------------------------------------------------------- */
+/* out[0] + i out[1] = sum_k conj(x[k]) y[k]. */
+int tnk_zdot_f64(const double* x, const double* y, int64_t n, double* out, double* red,
+                 void* stream);
+/* c[i] = sum_k conj(V[i*ldv + k]) w[k], i < nv <= 64 (c: 2*nv doubles). */
+int tnk_zmultidot_f64(const double* V, int64_t ldv, int32_t nv, const double* w, int64_t n,
+                      double* c, double* red, void* stream);
+/* w[k] -= sum_i c[i] V[i*ldv + k], complex c on the device. */
+int tnk_zgemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c, double* w,
+                      int64_t n, void* stream);
+/* y = a x + b y, a = sa[0]*fa, b = sb[0]*fb with complex sa, sb on the device (1 when null). */
+int tnk_zaxpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,
+                   const double* sb, double fb, void* stream);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,9 @@ Modes:
          chi=32 dense; XXZ N=12 U(1); XXZ N=64 U(1) at chi=64/128).  -> dmrg_small.json
   c2     The XXZ N=64 U(1) chi=1024 six-sweep run: energies, sweep times, matvec counts and every
          bond's sector dims.  -> c2_xxz_n64_chi1024.json
+  tdvp   Two-site TDVP of the XXZ N=10 chain on complex U(1) blocks from a seeded random state:
+         the initial tensors, the reference's Krylov exponential on a fixed vector, and the
+         state vector after 4 steps of dt=0.05.  -> tdvp_xxz10.npz, tdvp_xxz10.json
 """
 from __future__ import annotations
 
@@ -252,10 +255,58 @@ def mode_c2(ref):
     print("E", E)
 
 
+def _dense_vector(mps):
+    """The state vector of a block MPS with every leg in sector order (its flat amplitudes)."""
+    v = np.ones((1,), complex)
+    for t in mps:
+        d = t.to_dense()
+        v = np.tensordot(v.reshape(-1, d.shape[0]), d, (1, 0)).reshape(-1, d.shape[-1])
+    return v.reshape(-1)
+
+
+def mode_tdvp(ref):
+    from tnkit import get_backend, U1, to_block_mpo, tdvp2_evolve
+    from tnkit.block_backend import BlockBackend, random_block_mps
+    from tnkit.eigensolver import lanczos_expm
+    from tnkit._dmrg import apply_two_site
+    arrays, meta = {}, {}
+    N, chi, dt, steps = 10, 32, 0.05, 4
+    be = get_backend("numpy")
+    bb = BlockBackend(be)
+    W = open_chain(xxz_bulk(1.0), N)
+    Wb, _ = to_block_mpo(W, [[1, -1]] * N, be, sym=U1())
+    mps = random_block_mps(Wb, 8, be, 0, np.random.default_rng(5))
+    mps = [m.canonical() for m in mps]
+    for i, m in enumerate(mps):
+        arrays[f"init_{i}"] = np.asarray(m.data)
+        meta[f"init_{i}"] = {"legs": _legs_json(m.struct), "charge": int(m.struct.charge)}
+    out, rec = tdvp2_evolve(list(mps), Wb, chi, dt, steps, backend=bb)
+    arrays["final_vector"] = _dense_vector(out)
+    arrays["init_vector"] = _dense_vector(mps)
+    meta["params"] = {"N": N, "chi": chi, "dt": dt, "n_steps": steps, "seed": 5, "chi0": 8}
+    meta["final_bonds"] = [{"charges": [int(c) for c in m.legs[2].charges],
+                            "dims": [int(d) for d in m.legs[2].dims]} for m in out]
+    # the Krylov exponential alone: exp(-i dt/2 H) on a fixed vector of a 300x300 Hermitian H
+    rng = np.random.default_rng(4)
+    n = 300
+    Q = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    H = 0.5 * (Q + Q.conj().T)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    info = {}
+    y = lanczos_expm(lambda x: H @ x, v, -0.5j * 0.1, be, m=30, info=info)
+    arrays["expm_H"], arrays["expm_v"], arrays["expm_y"] = H, v, np.asarray(y)
+    meta["expm"] = {"tau_imag": -0.05, "m": 30, "krylov_dim": int(info["krylov_dim"]),
+                    "err_est": float(info["err_est"])}
+    np.savez_compressed(os.path.join(HERE, "tdvp_xxz10.npz"), **arrays)
+    with open(os.path.join(HERE, "tdvp_xxz10.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print("wrote tdvp_xxz10.{npz,json}; krylov dim", info["krylov_dim"])
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["small", "dmrg", "c2"])
+    ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp"])
     ap.add_argument("--ref", default="/root/reference")
     a = ap.parse_args()
     ref = _import_ref(a.ref)
-    {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2}[a.mode](ref)
+    {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2, "tdvp": mode_tdvp}[a.mode](ref)

@@ -27,7 +27,9 @@ def run_gemm(tables, slots, C):
             A = _view(slots[int(s["a_buf"])], s["a_off"], (m, k), (s["a_rs"], s["a_cs"]))
             B = _view(slots[int(s["b_buf"])], s["b_off"], (k, n), (s["b_rs"], s["b_cs"]))
             acc += float(s["coef"]) * (A @ B)
-        idx = int(t["c_off"]) + np.arange(m)[:, None] * int(t["ldc"]) + np.arange(n)[None, :]
+        ccs = 2 if int(t["flags"]) & 4 else 1
+        idx = (int(t["c_off"]) + np.arange(m)[:, None] * int(t["ldc"])
+               + np.arange(n)[None, :] * ccs)
         if int(t["flags"]) & 1:
             C[idx] += acc
         else:
@@ -58,7 +60,8 @@ def run_comb(tables, src, dst):
 
 def run_plan3(plan, x0, x1, x2):
     ws = np.zeros(plan.ws1 + plan.ws2)
-    out = np.zeros(plan.out_layout.size)
+    scale = 2 if getattr(plan, "kind", "").endswith("c128") else 1
+    out = np.zeros(plan.out_layout.size * scale)
     slots = [x0, x1, x2, ws]
     run_gemm(plan.g1, slots, ws)
     run_comb(plan.c2, ws.copy(), ws)

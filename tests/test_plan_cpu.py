@@ -124,3 +124,40 @@ def test_tensor_core_plan_relayout(passes, tol):
     for off, r, c, ld in tc.maps:
         assert off % P.TC_ALIGN == 0 and (ld * 4) % 16 == 0 and ld >= c
     assert tc.stage_elems % P.TC_ALIGN == 0
+
+
+def _cplx(rng, n):
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
+def test_complex_plans_match_oracle(golden):
+    """Complex128 operands through the interleaved re/im expansion of the real plans, against
+    the oracle's complex contractions (the conjugated site tensor of the environment updates
+    included)."""
+    from oracle.blocks_np import BT, Leg as OL
+    meta, A = golden
+    tag = "xxz12_b5"
+    g = lambda k: lay(meta[f"{tag}_{k}"])
+    Ll, Rl, W1l, W2l, Tl, Al, Bl, R1l = (g(k) for k in ("L", "R", "W1", "W2", "theta", "A", "B",
+                                                          "R1"))
+    W1d, W2d = A[f"{tag}_W1"], A[f"{tag}_W2"]
+    rng = np.random.default_rng(9)
+    L, R, th, Am, Bm, R1 = (_cplx(rng, x.size) for x in (Ll, Rl, Tl, Al, Bl, R1l))
+    iv = lambda z: np.stack([z.real, z.imag], -1).reshape(-1)      # interleaved view
+    cv = lambda d: d[0::2] + 1j * d[1::2]
+    ob = lambda l, d: BT.from_flat([OL(tuple(x.charges), tuple(x.dims), x.sign) for x in l.legs],
+                                   l.charge, d)
+    W1, W2 = ob(W1l, W1d), ob(W2l, W2d)
+    hp = P.plan_apply(Tl, Ll, [(W1l, W1d), (W2l, W2d)], Rl)
+    got = cv(run_plan3(P.ComplexPlan3(hp), iv(L), iv(th), iv(R)))
+    ref = O.apply_two_site(ob(Tl, th), ob(Ll, L), W1, W2, ob(Rl, R)).flat()
+    assert _rel(got, ref) <= 1e-13
+    p1 = P.plan_apply(Al, Ll, [(W1l, W1d)], R1l)
+    got = cv(run_plan3(P.ComplexPlan3(p1), iv(L), iv(Am), iv(R1)))
+    assert _rel(got, O.apply_one_site(ob(Al, Am), ob(Ll, L), W1, ob(R1l, R1)).flat()) <= 1e-13
+    pl = P.plan_left_env(Ll, Al, (W1l, W1d))
+    got = cv(run_plan3(P.ComplexPlan3(pl), iv(Am), iv(L), iv(Am)))
+    assert _rel(got, O.update_left_env(ob(Ll, L), ob(Al, Am), W1).flat()) <= 1e-13
+    pr = P.plan_right_env(Rl, Bl, (W2l, W2d))
+    got = cv(run_plan3(P.ComplexPlan3(pr), iv(Bm), iv(R), iv(Bm)))
+    assert _rel(got, O.update_right_env(ob(Rl, R), ob(Bl, Bm), W2).flat()) <= 1e-13

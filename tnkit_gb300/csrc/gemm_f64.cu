@@ -135,6 +135,8 @@ gemm_f64_kernel(const tnk_gemm_task* __restrict__ tasks, const tnk_gemm_seg* __r
     }
 
     const bool accumulate = (task.flags & 1) != 0;
+    // flags bit 2: output column stride 2 (the real or imaginary half of interleaved complex)
+    const int64_t ccs = (task.flags & 4) ? 2 : 1;
     double* c = C + task.c_off;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -144,7 +146,7 @@ gemm_f64_kernel(const tnk_gemm_task* __restrict__ tasks, const tnk_gemm_seg* __r
         for (int j = 0; j < 4; ++j) {
             const int n = n0 + tx + 16 * j;
             if (n >= N) continue;
-            double* p = c + (int64_t)m * task.ldc + n;
+            double* p = c + (int64_t)m * task.ldc + (int64_t)n * ccs;
             *p = accumulate ? *p + acc[i][j] : acc[i][j];
         }
     }

@@ -31,31 +31,41 @@ def _fuse_info(layout: Layout, nrow: int) -> P.FuseInfo:
     return _PLANS.get_or(("fuseinfo", layout, nrow), lambda: P.FuseInfo(layout, nrow))
 
 
+def _comb_plan(key, build, data):
+    """Device combination plan for `data`'s dtype (complex128: re/im halves separately)."""
+    cplx = data.is_complex()
+
+    def make():
+        hp = build()
+        if cplx:
+            c = P.HostCombPlan.__new__(P.HostCombPlan)
+            c.c, c.out_layout, c.extra = P.complexify_comb(hp.c), hp.out_layout, hp.extra
+            hp = c
+        return DeviceCombPlan(hp, data.device)
+    return _PLANS.get_or(key + (str(data.device), cplx), make)
+
+
 def fuse_matrix(t: BlockTensor, nrow: int) -> Tuple[BlockTensor, P.FuseInfo]:
     """Fuse legs [0, nrow) and [nrow, n) of `t` into a two-leg block matrix."""
     info = _fuse_info(t.layout, nrow)
-    dev = t.data.device
-    p = _PLANS.get_or(("fuse", t.layout, nrow, str(dev)),
-                      lambda: DeviceCombPlan(P.plan_fuse(info), dev))
-    out = torch.empty(info.matrix.size, dtype=torch.float64, device=dev)
+    p = _comb_plan(("fuse", t.layout, nrow), lambda: P.plan_fuse(info), t.data)
+    out = torch.empty(info.matrix.size, dtype=t.data.dtype, device=t.data.device)
     p.run(t.data, out)
     return BlockTensor(info.matrix, out), info
 
 
 def split_rows(m: BlockTensor, info: P.FuseInfo) -> BlockTensor:
-    dev = m.data.device
-    p = _PLANS.get_or(("split_r", info.layout, info.nrow, m.layout, str(dev)),
-                      lambda: DeviceCombPlan(P.plan_split_rows(info, m.layout), dev))
-    out = torch.empty(p.out_layout.size, dtype=torch.float64, device=dev)
+    p = _comb_plan(("split_r", info.layout, info.nrow, m.layout),
+                   lambda: P.plan_split_rows(info, m.layout), m.data)
+    out = torch.empty(p.out_layout.size, dtype=m.data.dtype, device=m.data.device)
     p.run(m.data, out)
     return BlockTensor(p.out_layout, out)
 
 
 def split_cols(m: BlockTensor, info: P.FuseInfo) -> BlockTensor:
-    dev = m.data.device
-    p = _PLANS.get_or(("split_c", info.layout, info.nrow, m.layout, str(dev)),
-                      lambda: DeviceCombPlan(P.plan_split_cols(info, m.layout), dev))
-    out = torch.empty(p.out_layout.size, dtype=torch.float64, device=dev)
+    p = _comb_plan(("split_c", info.layout, info.nrow, m.layout),
+                   lambda: P.plan_split_cols(info, m.layout), m.data)
+    out = torch.empty(p.out_layout.size, dtype=m.data.dtype, device=m.data.device)
     p.run(m.data, out)
     return BlockTensor(p.out_layout, out)
 
@@ -127,13 +137,13 @@ def _svd_gram(M: torch.Tensor):
     tnkit/blocks.py:1345-1377). Singular values below ~1e-8 of the largest are not resolved."""
     R, C = M.shape
     if R >= C:
-        w, V = torch.linalg.eigh(M.transpose(0, 1) @ M)
+        w, V = torch.linalg.eigh(M.mH @ M)
         V = torch.flip(V, (-1,))
         Q, Rr = torch.linalg.qr(M @ V)
     else:
-        w, U = torch.linalg.eigh(M @ M.transpose(0, 1))
+        w, U = torch.linalg.eigh(M @ M.mH)
         U = torch.flip(U, (-1,))
-        Q, Rr = torch.linalg.qr(M.transpose(0, 1) @ U)
+        Q, Rr = torch.linalg.qr(M.mH @ U)
     d = torch.diagonal(Rr)
     S = d.abs()
     Q = Q * torch.where(S > 0, d / torch.where(S > 0, S, torch.ones_like(S)),
@@ -141,12 +151,12 @@ def _svd_gram(M: torch.Tensor):
     o = torch.argsort(S, descending=True, stable=True)
     S, Q = S[o], Q[:, o]
     if R >= C:
-        return Q.contiguous(), S, V[:, o].transpose(0, 1).contiguous()
-    return U[:, o].contiguous(), S, Q.transpose(0, 1).contiguous()
+        return Q.contiguous(), S, V[:, o].mH.contiguous()
+    return U[:, o].contiguous(), S, Q.mH.contiguous()
 
 
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
-                  method: str = "svd"):
+                  method: str = "svd", normalize: bool = True):
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
@@ -180,7 +190,7 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
            for (r, c, U, S, Vh), n in zip(parts, kept.tolist()) if n]
     new.sort(key=lambda x: (x[0], x[1]))
     bond = Leg(tuple(x[0] for x in new), tuple(int(x[4].shape[0]) for x in new), 1)
-    if scale != "none":
+    if scale != "none" and normalize:
         new = [(q, r, c, U, S / norm, Vh) for (q, r, c, U, S, Vh) in new]
     Ub, Vb = [], []
     for q, r, c, U, S, Vh in sorted(new, key=lambda x: x[1]):
@@ -203,9 +213,8 @@ def lq(m: BlockTensor):
     lr, lc = m.layout.legs
     new = []
     for r, c, M in _blocks(m):
-        q, t = torch.linalg.qr(M.transpose(0, 1))
-        new.append((_row_label(lr, r), r, c, t.transpose(0, 1).contiguous(),
-                    q.transpose(0, 1).contiguous()))
+        q, t = torch.linalg.qr(M.mH)
+        new.append((_row_label(lr, r), r, c, t.mH.contiguous(), q.mH.contiguous()))
     new.sort(key=lambda x: x[0])
     bond = Leg(tuple(x[0] for x in new), tuple(int(x[3].shape[1]) for x in new), 1)
     A = torch.cat([a.reshape(-1) for _, _, _, a, _ in sorted(new, key=lambda x: x[1])])
@@ -224,14 +233,16 @@ class Scalars:
 
     def normalize_(self, x: torch.Tensor) -> torch.Tensor:
         sp = _lib.stream_ptr()
-        _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.sc.data_ptr(),
+        r = torch.view_as_real(x).reshape(-1) if x.is_complex() else x
+        _lib.check(self.lib.tnk_nrm2_f64(r.data_ptr(), r.numel(), self.sc.data_ptr(),
                                          self.red.data_ptr(), sp), "nrm2")
-        _lib.check(self.lib.tnk_scale_div_f64(x.data_ptr(), x.data_ptr(), x.numel(),
+        _lib.check(self.lib.tnk_scale_div_f64(r.data_ptr(), r.data_ptr(), r.numel(),
                                               self.sc.data_ptr(), 1.0, sp), "scale_div")
         return x
 
     def norm(self, x: torch.Tensor) -> float:
         sp = _lib.stream_ptr()
+        x = torch.view_as_real(x).reshape(-1) if x.is_complex() else x
         _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.sc.data_ptr(),
                                          self.red.data_ptr(), sp), "nrm2")
         return float(self.sc[0].item())

@@ -24,10 +24,22 @@ _ALIGN = 64
 
 
 def _require_cuda(*ts):
+    """All operands contiguous CUDA float64, or all complex128; returns True when complex."""
+    kinds = set()
     for t in ts:
-        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64
-                and t.is_contiguous()):
-            raise TypeError("tnkit_gb300 kernels need contiguous float64 CUDA tensors")
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous()
+                and t.dtype in (torch.float64, torch.complex128)):
+            raise TypeError("tnkit_gb300 kernels need contiguous float64 or complex128 CUDA "
+                            "tensors")
+        kinds.add(t.dtype)
+    if len(kinds) > 1:
+        raise TypeError("tnkit_gb300 kernels need operands of one dtype (float64 or "
+                        "complex128); cast the state with .to(torch.complex128) first")
+    return torch.complex128 in kinds
+
+
+def _cplx(hp):
+    return P.ComplexPlan3(hp)
 
 
 def _pack(arrays, device):
@@ -161,86 +173,109 @@ def _host_of(W: BlockTensor) -> np.ndarray:
     return W.host
 
 
-def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
-                  R: BlockTensor, device) -> DevicePlan3:
-    key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout, str(device))
+def _real_plan(key, build):
+    return _PLANS.get_or(("host",) + key, build)
 
-    def build():
+
+def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                  R: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+    key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout)
+
+    def host():
         hp = P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
                           R.layout)
         hp.ref_macs = P.two_site_ref_macs(theta, L.layout, W1.layout, W2.layout, R.layout)
-        return DevicePlan3(hp, device)
-    return _PLANS.get_or(key, build)
+        return hp
+
+    def build():
+        hp = _real_plan(key, host)
+        return DevicePlan3(_cplx(hp) if cplx else hp, device)
+    return _PLANS.get_or(key + (str(device), cplx), build)
 
 
 def plan_one_site(M: Layout, L: BlockTensor, W: BlockTensor, R: BlockTensor,
-                  device) -> DevicePlan3:
-    key = ("apply1", M, L.layout, _mpo_key(W), R.layout, str(device))
-    return _PLANS.get_or(key, lambda: DevicePlan3(
-        P.plan_apply(M, L.layout, [(W.layout, _host_of(W))], R.layout), device))
+                  device, cplx: bool = False) -> DevicePlan3:
+    key = ("apply1", M, L.layout, _mpo_key(W), R.layout)
+    host = lambda: P.plan_apply(M, L.layout, [(W.layout, _host_of(W))], R.layout)
+    return _PLANS.get_or(key + (str(device), cplx), lambda: DevicePlan3(
+        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
 
 
-def plan_left(L: Layout, A: Layout, W: BlockTensor, device) -> DevicePlan3:
-    key = ("left", L, A, _mpo_key(W), str(device))
-    return _PLANS.get_or(key, lambda: DevicePlan3(
-        P.plan_left_env(L, A, (W.layout, _host_of(W))), device))
+def plan_left(L: Layout, A: Layout, W: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+    key = ("left", L, A, _mpo_key(W))
+    host = lambda: P.plan_left_env(L, A, (W.layout, _host_of(W)))
+    return _PLANS.get_or(key + (str(device), cplx), lambda: DevicePlan3(
+        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
 
 
-def plan_right(R: Layout, B: Layout, W: BlockTensor, device) -> DevicePlan3:
-    key = ("right", R, B, _mpo_key(W), str(device))
-    return _PLANS.get_or(key, lambda: DevicePlan3(
-        P.plan_right_env(R, B, (W.layout, _host_of(W))), device))
+def plan_right(R: Layout, B: Layout, W: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+    key = ("right", R, B, _mpo_key(W))
+    host = lambda: P.plan_right_env(R, B, (W.layout, _host_of(W)))
+    return _PLANS.get_or(key + (str(device), cplx), lambda: DevicePlan3(
+        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
 
 
-def plan_tdot(a: Layout, b: Layout, nc: int, device) -> DeviceGemmPlan:
-    key = ("tdot", a, b, nc, str(device))
-    return _PLANS.get_or(key, lambda: DeviceGemmPlan(P.plan_tensordot(a, b, nc), device))
+def plan_tdot(a: Layout, b: Layout, nc: int, device, cplx: bool = False) -> DeviceGemmPlan:
+    key = ("tdot", a, b, nc)
+
+    def build():
+        hp = _real_plan(key, lambda: P.plan_tensordot(a, b, nc))
+        if cplx:
+            c = P.HostGemmPlan.__new__(P.HostGemmPlan)
+            c.g, c.macs, c.out_layout = P.complexify_gemm(hp.g), 4 * hp.macs, hp.out_layout
+            hp = c
+        return DeviceGemmPlan(hp, device)
+    return _PLANS.get_or(key + (str(device), cplx), build)
 
 
 # --------------------------------------------------------------------------- #
 # the reference's hot-path functions on block tensors (tnkit/_dmrg.py:162-231)
 # --------------------------------------------------------------------------- #
+def _out(p, like, out=None):
+    if out is not None:
+        return out
+    return torch.empty(p.out_layout.size, dtype=like.dtype, device=like.device)
+
+
 def apply_two_site(theta: BlockTensor, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
                    R: BlockTensor, out: Optional[torch.Tensor] = None) -> BlockTensor:
-    _require_cuda(theta.data, L.data, R.data)
-    p = plan_two_site(theta.layout, L, W1, W2, R, theta.data.device)
-    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=theta.data.device) \
-        if out is None else out
+    c = _require_cuda(theta.data, L.data, R.data)
+    p = plan_two_site(theta.layout, L, W1, W2, R, theta.data.device, c)
+    y = _out(p, theta.data, out)
     p.run("tnk_apply_two_site_f64", L.data, theta.data, R.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
 def apply_one_site(M: BlockTensor, L: BlockTensor, W: BlockTensor, R: BlockTensor,
                    out: Optional[torch.Tensor] = None) -> BlockTensor:
-    _require_cuda(M.data, L.data, R.data)
-    p = plan_one_site(M.layout, L, W, R, M.data.device)
-    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=M.data.device) \
-        if out is None else out
+    c = _require_cuda(M.data, L.data, R.data)
+    p = plan_one_site(M.layout, L, W, R, M.data.device, c)
+    y = _out(p, M.data, out)
     p.run("tnk_apply_one_site_f64", L.data, M.data, R.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
 def update_left_env(L: BlockTensor, A: BlockTensor, W: BlockTensor) -> BlockTensor:
-    _require_cuda(L.data, A.data)
-    p = plan_left(L.layout, A.layout, W, A.data.device)
-    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=A.data.device)
+    c = _require_cuda(L.data, A.data)
+    p = plan_left(L.layout, A.layout, W, A.data.device, c)
+    y = _out(p, A.data)
     p.run("tnk_update_left_env_f64", A.data, L.data, A.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
 def update_right_env(R: BlockTensor, B: BlockTensor, W: BlockTensor) -> BlockTensor:
-    _require_cuda(R.data, B.data)
-    p = plan_right(R.layout, B.layout, W, B.data.device)
-    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=B.data.device)
+    c = _require_cuda(R.data, B.data)
+    p = plan_right(R.layout, B.layout, W, B.data.device, c)
+    y = _out(p, B.data)
     p.run("tnk_update_right_env_f64", B.data, R.data, B.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
 def tensordot(a: BlockTensor, b: BlockTensor, nc: int = 1) -> BlockTensor:
     """Contract the last `nc` legs of a with the first `nc` legs of b (e.g. "asc,ctb->astb")."""
-    _require_cuda(a.data, b.data)
-    p = plan_tdot(a.layout, b.layout, nc, a.data.device)
-    y = torch.empty(p.out_layout.size, dtype=torch.float64, device=a.data.device)
+    c = _require_cuda(a.data, b.data)
+    p = plan_tdot(a.layout, b.layout, nc, a.data.device, c)
+    y = _out(p, a.data)
     p.run(a.data, b.data, y)
     return BlockTensor(p.out_layout, y)
 
@@ -251,10 +286,10 @@ class TwoSiteOperator:
 
     def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
                  R: BlockTensor):
-        _require_cuda(L.data, R.data)
+        self.cplx = _require_cuda(L.data, R.data)
         self.L, self.R = L, R
         self.device = L.data.device
-        self.plan = plan_two_site(theta_layout, L, W1, W2, R, self.device)
+        self.plan = plan_two_site(theta_layout, L, W1, W2, R, self.device, self.cplx)
         self.n = theta_layout.size
         self.ws = workspace(self.plan.ws_elems, self.device)
         self.calls = 0
@@ -266,5 +301,24 @@ class TwoSiteOperator:
     def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         y = torch.empty_like(x) if out is None else out
         self.plan.run("tnk_apply_two_site_f64", self.L.data, x, self.R.data, y, self.ws)
+        self.calls += 1
+        return y
+
+
+class OneSiteOperator:
+    """H_eff of one site (tnkit/_dmrg.py:192-199) as `op(x, out)` on flat canonical buffers:
+    the back-evolution operator of two-site TDVP."""
+
+    def __init__(self, m_layout: Layout, L: BlockTensor, W: BlockTensor, R: BlockTensor):
+        self.cplx = _require_cuda(L.data, R.data)
+        self.L, self.R = L, R
+        self.device = L.data.device
+        self.plan = plan_one_site(m_layout, L, W, R, self.device, self.cplx)
+        self.ws = workspace(self.plan.ws_elems, self.device)
+        self.calls = 0
+
+    def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        y = torch.empty_like(x) if out is None else out
+        self.plan.run("tnk_apply_one_site_f64", self.L.data, x, self.R.data, y, self.ws)
         self.calls += 1
         return y

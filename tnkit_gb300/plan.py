@@ -802,3 +802,74 @@ class HostPlanTC:
             d[2 * i] = (off, r, c, ld)
             d[2 * i + 1] = (off + self.stage_elems, r, c, ld)
         return d
+
+
+# --------------------------------------------------------------------------- #
+# complex128: the same plans over interleaved (re, im) storage
+# --------------------------------------------------------------------------- #
+def complexify_gemm(g, tile=TILE_M):
+    """A real grouped-GEMM table on complex operands stored as interleaved doubles: each output
+    becomes a real-part and an imaginary-part task (output column stride 2, flags bit 2), each
+    segment A B the four real products of (Ar + i Ai)(Br + i Bi), with the signs that a
+    conjugated operand (segment conj bits) flips."""
+    tasks, segs, _ = g
+    T, S = [], []
+    for t in tasks:
+        sb, se = int(t["seg_begin"]), int(t["seg_end"])
+        re_segs, im_segs = [], []
+        for s in segs[sb:se]:
+            ca = -1.0 if int(s["conj"]) & 1 else 1.0
+            cb = -1.0 if int(s["conj"]) & 2 else 1.0
+            c = float(s["coef"])
+            a0, b0 = 2 * int(s["a_off"]), 2 * int(s["b_off"])
+            ars, acs, brs, bcs = (2 * int(s["a_rs"]), 2 * int(s["a_cs"]), 2 * int(s["b_rs"]),
+                                  2 * int(s["b_cs"]))
+            k, abuf, bbuf = int(s["k"]), int(s["a_buf"]), int(s["b_buf"])
+            mk = lambda ao, bo, cf: (ao, bo, ars, acs, brs, bcs, k, abuf, bbuf, 0, 0, cf)
+            re_segs += [mk(a0, b0, c), mk(a0 + 1, b0 + 1, -c * ca * cb)]
+            im_segs += [mk(a0, b0 + 1, c * cb), mk(a0 + 1, b0, c * ca)]
+        fl = int(t["flags"]) | 4
+        for part, ss in ((0, re_segs), (1, im_segs)):
+            T.append((2 * int(t["c_off"]) + part, 2 * int(t["ldc"]), int(t["m"]), int(t["n"]),
+                      len(S), len(S) + len(ss), fl))
+            S.extend(ss)
+    ta = np.array(T, dtype=GEMM_TASK) if T else np.zeros(0, GEMM_TASK)
+    sa = np.array(S, dtype=GEMM_SEG) if S else np.zeros(0, GEMM_SEG)
+    return ta, sa, _tiles(ta, sa, tile)
+
+
+def complexify_comb(c):
+    """A real combination table (real coefficients) on interleaved complex data: the real and the
+    imaginary halves combine separately."""
+    tasks, terms, _ = c
+    T, U = [], []
+    for t in tasks:
+        tb, te = int(t["term_begin"]), int(t["term_end"])
+        for part in (0, 1):
+            b = len(U)
+            for u in terms[tb:te]:
+                U.append((2 * int(u["src_off"]) + part, 2 * int(u["src_ld"]),
+                          2 * int(u["src_cs"]), float(u["coef"])))
+            T.append((2 * int(t["dst_off"]) + part, int(t["rows"]), int(t["cols"]),
+                      2 * int(t["dst_ld"]), 2 * int(t["dst_cs"]), b, len(U)))
+    ct = CombTable()
+    ct.tasks, ct.terms = T, U
+    return ct.arrays()
+
+
+class ComplexPlan3:
+    """A HostPlan3 for complex128 operands (interleaved storage; workspace in doubles)."""
+
+    def __init__(self, hp: HostPlan3):
+        self.g1 = complexify_gemm(hp.g1)
+        self.c2 = complexify_comb(hp.c2)
+        self.g3 = complexify_gemm(hp.g3)
+        self.ws1, self.ws2 = 2 * hp.ws1, 2 * hp.ws2
+        self.out_layout = hp.out_layout
+        self.macs = 4 * hp.macs
+        self.ref_macs = None
+        self.kind = hp.kind + "-c128"
+
+    @property
+    def ws_elems(self):
+        return self.ws1 + self.ws2
