@@ -177,6 +177,7 @@ def main():
     ap.add_argument("--sweep-n", type=int, default=64)
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
+    ap.add_argument("--sweep-precisions", default="f64,ff,mixed,mixed-ff")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()
@@ -335,7 +336,9 @@ def main():
             "clocks": clocks}
     line["mixed"] = mixed_leg(torch, dev, th, L, W1, W2, R, y, flush, flops_ref, parts,
                               args.steps, ms)
-    line["gpu_launches"] += 4 * args.steps
+    line["float_float"] = ff_leg(torch, th, L, W1, W2, R, y, flush, flops_ref, parts,
+                                 args.steps, ms, dgemm)
+    line["gpu_launches"] += 7 * args.steps
     if args.sweep:
         line["sweep"] = sweep_leg(torch, args)
     if not args.no_cpu:
@@ -417,6 +420,33 @@ def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps,
                          "traffic": None, "gemm_ms": tg * 1e3}}
 
 
+def ff_leg(torch, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps, ms64, dgemm):
+    """The same matvec with the float-float grouped GEMM (double-FP32 on the FP32 cores)."""
+    from tnkit_gb300 import ops
+    op = ops.TwoSiteOperator(th.layout, L, W1, W2, R, precision="ff")
+    x = th.data
+    y = torch.empty_like(x)
+    for _ in range(3):
+        op(x, y)
+    torch.cuda.synchronize()
+    err = float((y - y64).abs().max() / y64.abs().max())
+    stream = torch.cuda.current_stream()
+    t = 0.0
+    for i in range(steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        op(x, y)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t += a.elapsed_time(b) / 1e3
+    mms = t / steps * 1e3
+    gf = flops_ref * steps / t / 1e9
+    return {"value": gf, "unit": "GFLOP/s", "ms_per_step": mms, "speedup_vs_fp64": ms64 / mms,
+            "max_rel_err_vs_fp64": err, "dtype": "f32x2 (float-float, 48-bit)",
+            "vs_measured_dgemm_peak": gf / 1e3 / dgemm}
+
+
 def sweep_leg(torch, args):
     """The whole U(1) XXZ DMRG at chi (6 sweeps, seed 1, expand 0) in FP64 and mixed precision,
     with the reference's own FP64 result (tests/golden/c2_xxz_n64_chi1024.json) as the oracle."""
@@ -432,7 +462,8 @@ def sweep_leg(torch, args):
         ref = json.load(open(gp))
         out["reference_E"] = ref["E"]
         out["reference_sweep_s"] = ref["sweep_s"]
-    for prec in ("f64", "mixed"):
+    precs = [p for p in args.sweep_precisions.split(",") if p]
+    for prec in precs:
         Wb = to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -445,8 +476,11 @@ def sweep_leg(torch, args):
         if ref is not None:
             rec["abs_dE_vs_reference"] = abs(E - ref["E"])
         out[prec] = rec
-    out["abs_dE_mixed_vs_f64"] = abs(out["mixed"]["E"] - out["f64"]["E"])
-    out["speedup_total"] = out["f64"]["total_s"] / out["mixed"]["total_s"]
+    if "f64" in out:
+        for p in precs:
+            if p != "f64":
+                out[p]["abs_dE_vs_f64"] = abs(out[p]["E"] - out["f64"]["E"])
+                out[p]["speedup_total_vs_f64"] = out["f64"]["total_s"] / out[p]["total_s"]
     return out
 
 

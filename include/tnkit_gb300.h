@@ -41,7 +41,8 @@ extern "C" {
  * C = sum over segments [seg_begin, seg_end) of coef * A_seg * B_seg; with no segment the
  * output is zero-filled. flags bit 0: accumulate into C instead of overwriting it; bit 1: FP64
  * output of a tensor-core stage; bit 2: output column stride 2 (one half of interleaved
- * complex128 data, C(i, j) at c_off + i*ldc + 2*j). */
+ * complex128 data, C(i, j) at c_off + i*ldc + 2*j); bit 3: float-float output of a float-float
+ * stage (a (hi, lo) float pair in each 8-byte element). */
 typedef struct {
     int64_t c_off;
     int32_t ldc, m, n;
@@ -157,6 +158,26 @@ int tnk_apply_two_site_f64_noalloc(const tnk_plan3* plan, const double* L, const
                                    const double* R, double* out, void* stream);
 /* out[0] = TNK_NOALLOC_SCRATCH_ELEMS, as compiled into the library. */
 int tnk_noalloc_scratch_elems(int64_t* out);
+
+/* The same plans in float-float ("double-FP32") arithmetic on the FP32 CUDA cores: operands
+ * are (hi, lo) float pairs (48 significant bits) stored in buffers with the FP64 layout, products
+ * by error-free transformations; ~1e-13 relative on the H_eff contractions at several times the
+ * FP64 rate of GB300. Stage-1 tasks carry flags bit 3 (float-float intermediates), GEMM segment
+ * coefficients must be +1 or -1. Replaces the same reference functions as the FP64 entry points.
+ * tnk_ff_split: y[i] = (fl(x[i]), fl(x[i] - fl(x[i]))) for n doubles (y may not alias x). */
+int tnk_ff_split(const double* x, double* y, int64_t n, void* stream);
+/* x0..x2 already split (float-float buffers); out is float-float where a task says so. */
+int tnk_contract3_ff(const tnk_plan3* plan, const double* x0, const double* x1,
+                     const double* x2, double* out, double* ws, int64_t ws_elems, void* stream);
+/* L2, R2: float-float copies (tnk_ff_split) of L and R; theta, out: FP64. `ws` holds
+ * ws1_elems + ws2_elems + out_elems doubles (the split theta goes after the intermediates). */
+int tnk_apply_two_site_ff(const tnk_plan3* plan, const double* L2, const double* theta,
+                          const double* R2, double* out, double* ws, int64_t ws_elems,
+                          void* stream);
+int tnk_grouped_gemm_ff(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
+                        const tnk_gemm_tile* tiles, int64_t n_tiles, const double* b0,
+                        const double* b1, const double* b2, const double* b3, double* C,
+                        void* stream);
 
 /* One grouped GEMM stage on its own (a two-operand block contraction, e.g. theta = M_i M_i+1,
  * tnkit/blocks.py:1156-1192 tensordot). Slots 0..3 = b0..b3; C is the output base. */

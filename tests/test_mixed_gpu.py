@@ -78,3 +78,28 @@ def test_mixed_dmrg_matches_fp64_dmrg(N, chi, sweeps):
     assert abs(Em - E64) <= 1e-10, (Em, E64)
     assert np.allclose(im["energies"], i64["energies"], rtol=0, atol=1e-10)
     assert im["mixed_counts"]["lo"] > 0
+
+
+@pytest.mark.parametrize("scale", [4, 1])
+def test_float_float_matvec_matches_fp64(scale):
+    """The float-float grouped GEMM (double-FP32 on the FP32 cores) on the same plan: within
+    1e-12 of the FP64 matvec, relative to the largest entry."""
+    from tnkit_gb300 import ops, workloads
+    dims = [max(1, d // scale) for d in workloads.C2_MID_DIMS]
+    th, L, W1, W2, R = workloads.mid_bond_problem(dims=dims, seed=40 + scale)
+    ref = ops.TwoSiteOperator(th.layout, L, W1, W2, R)(th.data)
+    got = ops.TwoSiteOperator(th.layout, L, W1, W2, R, precision="ff")(th.data)
+    assert _rel(got, ref) <= 1e-12, _rel(got, ref)
+
+
+@pytest.mark.parametrize("prec", ["ff", "mixed-ff"])
+def test_ff_dmrg_matches_reference(prec):
+    """Whole sweeps on the float-float matvec (alone, or as the polish after tensor-core
+    Lanczos): the reference's energies to 1e-12 relative."""
+    import json, os
+    from conftest import GOLDEN
+    from tnkit_gb300.dmrg import dmrg
+    ref = json.load(open(os.path.join(GOLDEN, "dmrg_small.json")))["xxz_n64_chi64"]
+    E, M, info = dmrg(_xxz_blocks(64), 64, charge=0, seed=1, n_sweeps=len(ref["energies"]),
+                      tol=0, rtol=0, expand=0, precision=prec)
+    assert abs(E - ref["E"]) <= 1e-12 * abs(ref["E"]), (E, ref["E"])

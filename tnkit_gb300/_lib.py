@@ -96,6 +96,10 @@ _SIGS = {
     "tnk_tc_encode_tmaps": ([_P, _P, _I64, _P], C.c_int),
     "tnk_grouped_gemm_tc": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _P], C.c_int),
     "tnk_combine_f32": ([_P, _P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
+    "tnk_ff_split": ([_P, _P, _I64, _P], C.c_int),
+    "tnk_contract3_ff": ([_P, _P, _P, _P, _P, _P, _I64, _P], C.c_int),
+    "tnk_apply_two_site_ff": ([_P, _P, _P, _P, _P, _P, _I64, _P], C.c_int),
+    "tnk_grouped_gemm_ff": ([_P, _P, _P, _I64, _P, _P, _P, _P, _P, _P], C.c_int),
     "tnk_zdot_f64": ([_P, _P, _I64, _P, _P, _P], C.c_int),
     "tnk_zmultidot_f64": ([_P, _I64, _I32, _P, _I64, _P, _P, _P], C.c_int),
     "tnk_zgemv_sub_f64": ([_P, _I64, _I32, _P, _P, _I64, _P], C.c_int),

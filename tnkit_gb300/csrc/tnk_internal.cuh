@@ -28,6 +28,9 @@ struct Slots {
 int launch_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
                     const tnk_gemm_tile* tiles, int64_t n_tiles, Slots slots, double* C,
                     cudaStream_t stream);
+int launch_gemm_ff(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
+                   const tnk_gemm_tile* tiles, int64_t n_tiles, Slots slots, double* C,
+                   cudaStream_t stream);
 int launch_comb_f64(const tnk_comb_task* tasks, const tnk_comb_term* terms,
                     const tnk_comb_item* items, int64_t n_items, const double* src,
                     double* dst, cudaStream_t stream);

@@ -49,7 +49,8 @@ class DMRGOptions:
     sites: int = 2
     expand: Optional[int] = None
     rtol: float = 1e-10
-    precision: str = "f64"          # 'f64' (plain) or 'mixed' (see tnkit_gb300.mixed)
+    precision: str = "f64"          # 'f64', 'ff' (float-float), 'mixed' or 'mixed-ff'
+                                    # (tensor-core Lanczos, then an FP64 / float-float polish)
     mixed_tol_lo: float = 1e-4
     polish: int = 2                  # FP64 polish restarts allowed after the mixed stage
     device: Any = None
@@ -105,6 +106,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         if chi is None:
             raise TypeError("dmrg() missing required argument 'chi' (bond dimension)")
     o = _resolve(options, kw)
+    if o.precision not in ("f64", "ff", "mixed", "mixed-ff"):
+        raise ValueError("precision must be 'f64', 'ff', 'mixed' or 'mixed-ff'")
     if o.sites != 2:
         raise NotImplementedError("this backend runs two-site DMRG (sites=2)")
     if o.trunc != "svd":
@@ -159,7 +162,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
 
     def eigsolve(theta: BlockTensor, i: int):
         nonlocal mv_calls
-        op = ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1], R[i + 2])
+        hi = "ff" if o.precision in ("ff", "mixed-ff") else "f64"
+        op = ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1], R[i + 2], precision=hi)
         n = theta.layout.size
         mi = o.max_iter if o.max_iter is not None else min(n, max(200, 4 * chi))
         need = (o.restart_m + 1) * n
@@ -168,7 +172,7 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         Vb = basis["buf"][:need].view(o.restart_m + 1, n)
         v0 = theta.data if o.warm_start else torch.as_tensor(
             np.random.default_rng(o.seed + 1).standard_normal(n), device=device)
-        if o.precision == "mixed":
+        if o.precision in ("mixed", "mixed-ff"):
             from .mixed import mixed_ground
             e, x, info = mixed_ground(theta.layout, L[i], W[i], W[i + 1], R[i + 2], op, v0,
                                       tol=o.eig_tol, max_iter=mi, m=o.restart_m,

@@ -57,17 +57,26 @@ def _pack(arrays, device):
 
 
 class DevicePlan3:
-    """A three-stage plan resident on the GPU."""
+    """A three-stage plan resident on the GPU. With ff=True its stage-1 tasks write float-float
+    intermediates (flags bit 3), for the float-float entry points."""
 
-    def __init__(self, hp: P.HostPlan3, device):
+    def __init__(self, hp: P.HostPlan3, device, ff: bool = False):
         self.host = hp
         (t1, s1, l1), (t2, c2, i2), (t3, s3, l3) = hp.g1, hp.c2, hp.g3
+        if ff:
+            t1 = t1.copy()
+            t1["flags"] |= 8
+            for s in (s1, s3):
+                if len(s) and not np.all(np.abs(s["coef"]) == 1.0):
+                    raise ValueError("float-float plans need GEMM coefficients of +-1")
         arrays = [t1, s1, l1, t2, c2, i2, t3, s3, l3]
         self.buf, offs = _pack(arrays, device)
         base = self.buf.data_ptr()
         a = [base + o for o in offs]
+        out_elems = hp.out_layout.size * (2 if hp.kind.endswith("c128") else 1)
+        self.out_elems = out_elems
         self.c = _lib.Plan3(a[0], a[1], a[2], len(l1), a[3], a[4], a[5], len(i2),
-                            a[6], a[7], a[8], len(l3), hp.ws1, hp.ws2, hp.out_layout.size)
+                            a[6], a[7], a[8], len(l3), hp.ws1, hp.ws2, out_elems)
         self.out_layout = hp.out_layout
         self.ws_elems = hp.ws_elems
         self.macs = hp.macs
@@ -178,7 +187,7 @@ def _real_plan(key, build):
 
 
 def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
-                  R: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+                  R: BlockTensor, device, cplx: bool = False, ff: bool = False) -> DevicePlan3:
     key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout)
 
     def host():
@@ -189,8 +198,8 @@ def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTenso
 
     def build():
         hp = _real_plan(key, host)
-        return DevicePlan3(_cplx(hp) if cplx else hp, device)
-    return _PLANS.get_or(key + (str(device), cplx), build)
+        return DevicePlan3(_cplx(hp) if cplx else hp, device, ff=ff)
+    return _PLANS.get_or(key + (str(device), cplx, ff), build)
 
 
 def plan_one_site(M: Layout, L: BlockTensor, W: BlockTensor, R: BlockTensor,
@@ -280,18 +289,36 @@ def tensordot(a: BlockTensor, b: BlockTensor, nc: int = 1) -> BlockTensor:
     return BlockTensor(p.out_layout, y)
 
 
+_APPLY2 = {"f64": "tnk_apply_two_site_f64", "ff": "tnk_apply_two_site_ff"}
+
+
 class TwoSiteOperator:
     """H_eff of one bond as a matvec on flat canonical buffers, for the Krylov solvers: the plan
-    and operands are bound once per local problem (tnkit/_dmrg.py:633-675 `matvec`)."""
+    and operands are bound once per local problem (tnkit/_dmrg.py:633-675 `matvec`).
+    precision 'f64' runs the FP64 grouped GEMM, 'ff' the float-float one (same plan)."""
 
     def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
-                 R: BlockTensor):
+                 R: BlockTensor, precision: str = "f64"):
+        if precision not in _APPLY2:
+            raise ValueError(f"precision must be one of {sorted(_APPLY2)}")
+        self.fn = _APPLY2[precision]
+        self.precision = precision
         self.cplx = _require_cuda(L.data, R.data)
         self.L, self.R = L, R
         self.device = L.data.device
-        self.plan = plan_two_site(theta_layout, L, W1, W2, R, self.device, self.cplx)
+        ff = precision == "ff"
+        self.plan = plan_two_site(theta_layout, L, W1, W2, R, self.device, self.cplx, ff=ff)
         self.n = theta_layout.size
-        self.ws = workspace(self.plan.ws_elems, self.device)
+        need = self.plan.ws_elems + (self.plan.out_elems if ff else 0)
+        self.ws = workspace(need, self.device)
+        if ff:           # float-float copies of the environments, split once per local problem
+            lib, sp = _lib.lib(), _lib.stream_ptr()
+            self.Lx, self.Rx = torch.empty_like(L.data), torch.empty_like(R.data)
+            for src, dst in ((L.data, self.Lx), (R.data, self.Rx)):
+                n = src.numel() * (2 if src.is_complex() else 1)
+                _lib.check(lib.tnk_ff_split(src.data_ptr(), dst.data_ptr(), n, sp), "ff split")
+        else:
+            self.Lx, self.Rx = L.data, R.data
         self.calls = 0
 
     @property
@@ -300,7 +327,7 @@ class TwoSiteOperator:
 
     def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         y = torch.empty_like(x) if out is None else out
-        self.plan.run("tnk_apply_two_site_f64", self.L.data, x, self.R.data, y, self.ws)
+        self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
         self.calls += 1
         return y
 
