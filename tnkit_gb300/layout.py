@@ -106,6 +106,10 @@ class Layout:
         self.offsets = np.cumsum(sizes) - sizes
         self.size = int(sizes.sum())
         self._index = None
+        # plain-Python views for the planners' inner loops
+        self.keys = [tuple(b) for b in self.blocks.tolist()]
+        self.shapes_t = [tuple(b) for b in self.shapes.tolist()]
+        self.offsets_l = self.offsets.tolist()
 
     @property
     def nblocks(self) -> int:
@@ -114,14 +118,14 @@ class Layout:
     @property
     def index(self) -> Dict[Tuple[int, ...], int]:
         if self._index is None:
-            self._index = {tuple(int(s) for s in b): k for k, b in enumerate(self.blocks)}
+            self._index = {b: k for k, b in enumerate(self.keys)}
         return self._index
 
     def key(self, k: int) -> Tuple[int, ...]:
-        return tuple(int(s) for s in self.blocks[k])
+        return self.keys[k]
 
     def shape(self, k: int) -> Tuple[int, ...]:
-        return tuple(int(s) for s in self.shapes[k])
+        return self.shapes_t[k]
 
     def __repr__(self):
         return (f"Layout(dims={[l.size for l in self.legs]}, charge={self.charge}, "

@@ -191,10 +191,8 @@ def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTenso
     key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout)
 
     def host():
-        hp = P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
-                          R.layout)
-        hp.ref_macs = P.two_site_ref_macs(theta, L.layout, W1.layout, W2.layout, R.layout)
-        return hp
+        return P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)),
+                                              (W2.layout, _host_of(W2))], R.layout)
 
     def build():
         hp = _real_plan(key, host)

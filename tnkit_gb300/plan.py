@@ -21,6 +21,8 @@ tnkit/blocks.py:_sym_plan does, from the same canonical layouts.
 """
 from __future__ import annotations
 
+import itertools
+import math
 from collections import defaultdict
 from typing import Dict, List, Sequence, Tuple
 
@@ -54,16 +56,29 @@ class GemmTable:
     def arrays(self):
         tasks = np.array(self.tasks, dtype=GEMM_TASK) if self.tasks else np.zeros(0, GEMM_TASK)
         segs = np.array(self.segs, dtype=GEMM_SEG) if self.segs else np.zeros(0, GEMM_SEG)
-        tiles, cost = [], []
-        for t, (c_off, ldc, m, n, sb, se, fl) in enumerate(self.tasks):
-            ktot = sum(int(s[6]) for s in self.segs[sb:se]) or 1
-            for m0 in range(0, m, TILE_M):
-                for n0 in range(0, n, TILE_N):
-                    tiles.append((t, m0, n0, 0))
-                    cost.append(ktot * min(TILE_M, m - m0) * min(TILE_N, n - n0))
-        order = np.argsort(-np.asarray(cost, np.int64), kind="stable") if tiles else []
-        tl = np.array([tiles[i] for i in order], dtype=GEMM_TILE) if tiles else np.zeros(0, GEMM_TILE)
-        return tasks, segs, tl
+        return tasks, segs, _tiles_cost(tasks, segs, TILE_M)
+
+
+def _tiles_cost(tasks, segs, tile):
+    """Every (task, m0, n0) tile, ordered by decreasing work (K x tile area), vectorised."""
+    if len(tasks) == 0:
+        return np.zeros(0, GEMM_TILE)
+    m = tasks["m"].astype(np.int64)
+    n = tasks["n"].astype(np.int64)
+    kcum = np.concatenate([[0], np.cumsum(segs["k"].astype(np.int64))]) if len(segs) else \
+        np.zeros(1, np.int64)
+    ktot = np.maximum(kcum[tasks["seg_end"]] - kcum[tasks["seg_begin"]], 1)
+    tm, tn = -(-m // tile), -(-n // tile)
+    cnt = tm * tn
+    tid = np.repeat(np.arange(len(tasks)), cnt)
+    local = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+    m0 = (local // tn[tid]) * tile
+    n0 = (local % tn[tid]) * tile
+    cost = ktot[tid] * np.minimum(tile, m[tid] - m0) * np.minimum(tile, n[tid] - n0)
+    order = np.argsort(-cost, kind="stable")
+    tl = np.zeros(len(tid), GEMM_TILE)
+    tl["task"], tl["m0"], tl["n0"] = tid[order], m0[order], n0[order]
+    return tl
 
 
 def seg(a_off, a_rs, a_cs, a_buf, b_off, b_rs, b_cs, b_buf, k, coef=1.0, conj=0):
@@ -190,7 +205,7 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
             kl, kt = ycand[yk]
             P, Wd_, Q = L.shape(kl)
             tsh = theta.shape(kt)
-            ncols = int(np.prod(tsh[1:]))
+            ncols = math.prod(tsh[1:])
             y_off[yk] = ws1
             ws1 += P * Wd_ * ncols
             g1.add(y_off[yk], ncols, P * Wd_, ncols,
@@ -204,7 +219,7 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
         p, phys_o, d = ok[0], ok[1:1 + n], ok[-1]
         oshape = out.shape(ko)
         P = oshape[0]
-        PO = int(np.prod(oshape[1:1 + n]))
+        PO = math.prod(oshape[1:1 + n])
         segs3 = []
         for kr in R_by_d.get(d, ()):
             _, r, b = R.key(kr)
@@ -219,7 +234,7 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
                               + [slice(ost[a][phys_o[a]], ost[a][phys_o[a]] + outs[a].dims[phys_o[a]])
                                  for a in range(n)]
                               + [slice(rst[r], rst[r] + Rd)])]
-                if np.any(sub):
+                if sub.any():
                     slices.append((yk, sub))
             if not slices:
                 continue
@@ -239,30 +254,32 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
         ws2 += P * PO * Rd * B
         ld = PO * Rd * B
         po_dims = [outs[a].dims[zk[1 + a]] for a in range(n)]
+        # per Y block: its nonzero coefficients, flattened as (ww, pi, po, rr) -> value
+        prepared = []
+        for yk, sub in slices:
+            kl, kt = ycand[yk]
+            Wd_ = L.shape(kl)[1]
+            tsh = theta.shape(kt)
+            ncols = math.prod(tsh[1:])
+            pi_n = math.prod(tsh[1:1 + n])
+            po_n = math.prod(po_dims)
+            flat = np.asarray(sub).reshape(Wd_, pi_n, po_n, Rd)
+            prepared.append((y_off[yk], Wd_ * ncols, ncols, flat, Wd_, pi_n))
         # one combination task per (phys_o', r') slice of this Z block
-        for po in np.ndindex(*po_dims):
-            po_flat = int(np.ravel_multi_index(po, po_dims))
+        for po_flat in range(math.prod(po_dims)):
             for rr in range(Rd):
                 dst = base + (po_flat * Rd + rr) * B
                 terms = []
-                for yk, sub in slices:
-                    kl, kt = ycand[yk]
-                    Wd_ = L.shape(kl)[1]
-                    pi_dims = list(theta.shape(kt)[1:1 + n])
-                    ncols = int(np.prod(theta.shape(kt)[1:]))
-                    for ww in range(Wd_):
-                        for pi in np.ndindex(*pi_dims):
-                            c = sub[(ww,) + pi + po + (rr,)]
-                            if c == 0.0:
-                                continue
-                            pi_flat = int(np.ravel_multi_index(pi, pi_dims))
-                            src = y_off[yk] + ww * ncols + pi_flat * B
-                            terms.append(term(src, Wd_ * ncols, 1, c))
+                for yo, src_ld, ncols, flat, Wd_, pi_n in prepared:
+                    sub2 = flat[:, :, po_flat, rr]
+                    ww_idx, pi_idx = np.nonzero(sub2)
+                    for ww, pi in zip(ww_idx.tolist(), pi_idx.tolist()):
+                        terms.append((yo + ww * ncols + pi * B, src_ld, 1, float(sub2[ww, pi])))
                 c2.add(dst, P, B, ld, 1, terms)
     for ko, segs3 in tasks3:
         oshape = out.shape(ko)
         P, D = oshape[0], oshape[-1]
-        PO = int(np.prod(oshape[1:1 + n]))
+        PO = math.prod(oshape[1:1 + n])
         segs = []
         for zi in segs3:
             _, _, _, Rd, B, _, kr = zdefs[zi]
