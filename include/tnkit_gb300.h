@@ -42,7 +42,8 @@ extern "C" {
  * output is zero-filled. flags bit 0: accumulate into C instead of overwriting it; bit 1: FP64
  * output of a tensor-core stage; bit 2: output column stride 2 (one half of interleaved
  * complex128 data, C(i, j) at c_off + i*ldc + 2*j); bit 3: float-float output of a float-float
- * stage (a (hi, lo) float pair in each 8-byte element). */
+ * stage (a (hi, lo) float pair in each 8-byte element); bit 4: the task writes to the workspace
+ * (operand slot 3) instead of C -- a split-K partial product summed by a plan's stage 4. */
 typedef struct {
     int64_t c_off;
     int32_t ldc, m, n;
@@ -96,8 +97,12 @@ typedef struct {
     const tnk_comb_task* t2; const tnk_comb_term* c2; const tnk_comb_item* items2; int64_t n_items2;
     const tnk_gemm_task* t3; const tnk_gemm_seg* s3; const tnk_gemm_tile* tiles3; int64_t n_tiles3;
     int64_t ws1_elems;               /* stage-1 output: workspace elements [0, ws1_elems) */
-    int64_t ws2_elems;               /* stage-2 output: [ws1_elems, ws1_elems + ws2_elems) */
+    int64_t ws2_elems;               /* stage-2 output and split-K partials:
+                                        [ws1_elems, ws1_elems + ws2_elems) */
     int64_t out_elems;               /* elements of the output buffer */
+    /* optional stage 4: the stage-3 tasks split along K (flags bit 4) write partial products to
+     * the workspace; this combination sums them, in a fixed order, into the output */
+    const tnk_comb_task* t4; const tnk_comb_term* c4; const tnk_comb_item* items4; int64_t n_items4;
 } tnk_plan3;
 
 /* ----------------------------------------------------------------------------------------

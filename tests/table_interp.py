@@ -30,10 +30,11 @@ def run_gemm(tables, slots, C):
         ccs = 2 if int(t["flags"]) & 4 else 1
         idx = (int(t["c_off"]) + np.arange(m)[:, None] * int(t["ldc"])
                + np.arange(n)[None, :] * ccs)
+        dst = slots[3] if int(t["flags"]) & 16 else C
         if int(t["flags"]) & 1:
-            C[idx] += acc
+            dst[idx] += acc
         else:
-            C[idx] = acc
+            dst[idx] = acc
 
 
 def run_comb(tables, src, dst):
@@ -66,6 +67,9 @@ def run_plan3(plan, x0, x1, x2):
     run_gemm(plan.g1, slots, ws)
     run_comb(plan.c2, ws.copy(), ws)
     run_gemm(plan.g3, slots, out)
+    c4 = getattr(plan, "c4", None)
+    if c4 is not None and len(c4[0]):
+        run_comb(c4, ws, out)
     return out
 
 

@@ -34,7 +34,7 @@ def test_struct_layouts_match_planner_dtypes():
     assert list(sizes) == [32, 56, 16, 32, 24, 16]
     assert [d.itemsize for d in (_lib.GEMM_TASK, _lib.GEMM_SEG, _lib.GEMM_TILE, _lib.COMB_TASK,
                                  _lib.COMB_TERM, _lib.COMB_ITEM)] == list(sizes)
-    assert C.sizeof(_lib.Plan3) == 15 * 8
+    assert C.sizeof(_lib.Plan3) == 19 * 8
 
 
 def test_null_plan_is_an_error_not_a_crash():

@@ -161,3 +161,23 @@ def test_complex_plans_match_oracle(golden):
     pr = P.plan_right_env(Rl, Bl, (W2l, W2d))
     got = cv(run_plan3(P.ComplexPlan3(pr), iv(Bm), iv(R), iv(Bm)))
     assert _rel(got, O.update_right_env(ob(Rl, R), ob(Bl, Bm), W2).flat()) <= 1e-13
+
+
+def test_split_k_stage_balances_and_matches():
+    """The split of long stage-3 tiles along K (partials in the workspace, stage 4 sums them):
+    the same result, and no tile longer than a few times the average work per resident CTA."""
+    from tnkit_gb300 import workloads
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=6, device="cpu")
+    hp = P.plan_apply(th.layout, L.layout, [(W1.layout, W1.host), (W2.layout, W2.host)], R.layout)
+    assert len(hp.c4[0]) > 0 and hp.ws2 > hp.ws2_unsplit
+    import copy
+    un = copy.copy(hp)
+    un.g3, un.c4, un.ws2 = hp.g3_unsplit, P._empty_comb(), hp.ws2_unsplit
+    a = run_plan3(hp, L.host, th.host, R.host)
+    b = run_plan3(un, L.host, th.host, R.host)
+    assert _rel(a, b) <= 1e-13
+    t, sgs, _ = hp.g3
+    kc = np.concatenate([[0], np.cumsum(sgs["k"].astype(np.int64))])
+    work = (kc[t["seg_end"]] - kc[t["seg_begin"]]) * np.minimum(64, t["m"]) * np.minimum(64, t["n"])
+    tot = float((work * (-(-t["m"] // 64)) * (-(-t["n"] // 64))).sum())
+    assert work.max() <= 2.0 * tot / P.SLOTS

@@ -55,7 +55,9 @@ class Plan3(C.Structure):
                 ("n_items2", C.c_int64),
                 ("t3", C.c_void_p), ("s3", C.c_void_p), ("tiles3", C.c_void_p),
                 ("n_tiles3", C.c_int64),
-                ("ws1_elems", C.c_int64), ("ws2_elems", C.c_int64), ("out_elems", C.c_int64)]
+                ("ws1_elems", C.c_int64), ("ws2_elems", C.c_int64), ("out_elems", C.c_int64),
+                ("t4", C.c_void_p), ("c4", C.c_void_p), ("items4", C.c_void_p),
+                ("n_items4", C.c_int64)]
 
 
 class TcPlan(C.Structure):

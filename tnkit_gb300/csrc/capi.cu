@@ -44,7 +44,9 @@ static int run_plan3(const tnk_plan3* p, const double* x0, const double* x1, con
     if (rc) return rc;
     rc = launch_comb_f64(p->t2, p->c2, p->items2, p->n_items2, ws, ws, st);
     if (rc) return rc;
-    return launch_gemm_f64(p->t3, p->s3, p->tiles3, p->n_tiles3, s, out, st);
+    rc = launch_gemm_f64(p->t3, p->s3, p->tiles3, p->n_tiles3, s, out, st);
+    if (rc) return rc;
+    return launch_comb_f64(p->t4, p->c4, p->items4, p->n_items4, ws, out, st);
 }
 
 }  // namespace tnk

@@ -17,8 +17,8 @@
 // on the GPU (different streams, or threads, without ordering between them) race on it. Nothing
 // in the scratch needs to start at zero: every element a call reads is first written by that
 // call (stage 1 writes each intermediate block stage 2 reads, stage 2 writes every slice of each
-// block stage 3 reads). The entry point allocates nothing: no cudaMalloc, no cudaFree, no
-// allocating library routine.
+// block stage 3 reads, stage 3 writes every split-K partial stage 4 sums). The entry point
+// allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine.
 #include <mutex>
 
 #include "tnk_internal.cuh"
@@ -95,5 +95,7 @@ extern "C" int tnk_apply_two_site_f64_noalloc(const tnk_plan3* plan, const doubl
     if (rc) return rc;
     rc = tnk::launch_comb_f64(plan->t2, plan->c2, plan->items2, plan->n_items2, ws, ws, st);
     if (rc) return rc;
-    return tnk::launch_gemm_f64(plan->t3, plan->s3, plan->tiles3, plan->n_tiles3, s, out, st);
+    rc = tnk::launch_gemm_f64(plan->t3, plan->s3, plan->tiles3, plan->n_tiles3, s, out, st);
+    if (rc) return rc;
+    return tnk::launch_comb_f64(plan->t4, plan->c4, plan->items4, plan->n_items4, ws, out, st);
 }

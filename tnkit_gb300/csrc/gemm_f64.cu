@@ -135,9 +135,10 @@ gemm_f64_kernel(const tnk_gemm_task* __restrict__ tasks, const tnk_gemm_seg* __r
     }
 
     const bool accumulate = (task.flags & 1) != 0;
-    // flags bit 2: output column stride 2 (the real or imaginary half of interleaved complex)
+    // flags bit 2: output column stride 2 (the real or imaginary half of interleaved complex);
+    // bit 4: a split-K partial product, written to the workspace (slot 3) instead of C
     const int64_t ccs = (task.flags & 4) ? 2 : 1;
-    double* c = C + task.c_off;
+    double* c = ((task.flags & 16) ? const_cast<double*>(slots.p[3]) : C) + task.c_off;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int m = m0 + ty + 16 * i;

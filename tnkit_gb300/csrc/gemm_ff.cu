@@ -170,9 +170,11 @@ gemm_ff_kernel(const tnk_gemm_task* __restrict__ tasks, const tnk_gemm_seg* __re
         }
     }
 
-    // flags bit 2: output column stride 2; bit 3: float-float output (a float2 per element)
+    // flags bit 2: output column stride 2; bit 3: float-float output (a float2 per element);
+    // bit 4: a split-K partial product (FP64), written to the workspace (slot 3) instead of C
     const int64_t ccs = (task.flags & 4) ? 2 : 1;
     const bool ffout = (task.flags & 8) != 0;
+    if (task.flags & 16) C = const_cast<double*>(slots.p[3]);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int m = m0 + ty + 16 * i;
@@ -333,7 +335,9 @@ int tnk_contract3_ff(const tnk_plan3* p, const double* x0, const double* x1, con
     if (rc) return rc;
     rc = tnk::launch_comb_ff(p->t2, p->c2, p->items2, p->n_items2, ws, ws, st);
     if (rc) return rc;
-    return tnk::launch_gemm_ff(p->t3, p->s3, p->tiles3, p->n_tiles3, s, out, st);
+    rc = tnk::launch_gemm_ff(p->t3, p->s3, p->tiles3, p->n_tiles3, s, out, st);
+    if (rc) return rc;
+    return tnk::launch_comb_f64(p->t4, p->c4, p->items4, p->n_items4, ws, out, st);
 }
 
 int tnk_apply_two_site_ff(const tnk_plan3* plan, const double* L2, const double* theta,

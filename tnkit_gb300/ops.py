@@ -63,20 +63,22 @@ class DevicePlan3:
     def __init__(self, hp: P.HostPlan3, device, ff: bool = False):
         self.host = hp
         (t1, s1, l1), (t2, c2, i2), (t3, s3, l3) = hp.g1, hp.c2, hp.g3
+        t4, c4, i4 = hp.c4
         if ff:
             t1 = t1.copy()
             t1["flags"] |= 8
             for s in (s1, s3):
                 if len(s) and not np.all(np.abs(s["coef"]) == 1.0):
                     raise ValueError("float-float plans need GEMM coefficients of +-1")
-        arrays = [t1, s1, l1, t2, c2, i2, t3, s3, l3]
+        arrays = [t1, s1, l1, t2, c2, i2, t3, s3, l3, t4, c4, i4]
         self.buf, offs = _pack(arrays, device)
         base = self.buf.data_ptr()
         a = [base + o for o in offs]
         out_elems = hp.out_layout.size * (2 if hp.kind.endswith("c128") else 1)
         self.out_elems = out_elems
         self.c = _lib.Plan3(a[0], a[1], a[2], len(l1), a[3], a[4], a[5], len(i2),
-                            a[6], a[7], a[8], len(l3), hp.ws1, hp.ws2, out_elems)
+                            a[6], a[7], a[8], len(l3), hp.ws1, hp.ws2, out_elems,
+                            a[9], a[10], a[11], len(i4))
         self.out_layout = hp.out_layout
         self.ws_elems = hp.ws_elems
         self.macs = hp.macs

@@ -114,13 +114,88 @@ def term(src_off, src_ld, src_cs, coef):
     return (int(src_off), int(src_ld), int(src_cs), float(coef))
 
 
+EMPTY_COMB = None
+
+
+def _empty_comb():
+    return (np.zeros(0, COMB_TASK), np.zeros(0, COMB_TERM), np.zeros(0, COMB_ITEM))
+
+
+SLOTS = 152 * 2            # resident 64x64-tile CTAs of the FP64 / float-float GEMMs
+
+
+def split_long_tiles(g3, ws_base: int, slots: int = SLOTS, max_chunks: int = 8):
+    """Split along K the stage-3 tasks whose tiles are much longer than the average work per
+    resident CTA, so one wave of tiles finishes together. Each chunk becomes a task that writes
+    its partial product to the workspace (flags bit 4, compact rows at ws_base + ...); stage 4
+    sums a split task's partials into its output block in a fixed order. Returns (tables,
+    stage-4 tables, workspace elements added)."""
+    tasks, segs, tiles = g3
+    if len(tasks) == 0:
+        return g3, _empty_comb(), 0
+    kcum = np.concatenate([[0], np.cumsum(segs["k"].astype(np.int64))])
+    ktot = kcum[tasks["seg_end"]] - kcum[tasks["seg_begin"]]
+    tile_work = ktot * np.minimum(TILE_M, tasks["m"]) * np.minimum(TILE_N, tasks["n"])
+    tm = -(-tasks["m"].astype(np.int64) // TILE_M)
+    tn = -(-tasks["n"].astype(np.int64) // TILE_N)
+    total = float((tile_work * tm * tn).sum())
+    target = max(total / slots, 1.0)
+    chunks = np.minimum(np.ceil(tile_work / target).astype(np.int64), max_chunks)
+    if (chunks <= 1).all():
+        return g3, _empty_comb(), 0
+    T, S, red = [], [], CombTable()
+    extra = 0
+    for ti, t in enumerate(tasks):
+        sb, se = int(t["seg_begin"]), int(t["seg_end"])
+        c = int(chunks[ti])
+        if c <= 1:
+            T.append(tuple(t.tolist()[:4]) + (len(S), len(S) + se - sb, int(t["flags"])))
+            S.extend(tuple(x.tolist()) for x in segs[sb:se])
+            continue
+        m, n, K = int(t["m"]), int(t["n"]), int(ktot[ti])
+        bounds = [K * j // c for j in range(c + 1)]
+        terms = []
+        for j in range(c):
+            lo, hi = bounds[j], bounds[j + 1]
+            part = []
+            k0 = 0
+            for sg in segs[sb:se]:
+                k = int(sg["k"])
+                a, b = max(lo, k0), min(hi, k0 + k)
+                if a < b:
+                    d = a - k0
+                    x = list(sg.tolist())
+                    x[0] = int(sg["a_off"]) + d * int(sg["a_cs"])
+                    x[1] = int(sg["b_off"]) + d * int(sg["b_rs"])
+                    x[6] = b - a
+                    part.append(tuple(x))
+                k0 += k
+            off = ws_base + extra
+            extra += m * n
+            T.append((off, n, m, n, len(S), len(S) + len(part), (int(t["flags"]) & ~1) | 16))
+            S.extend(part)
+            terms.append(term(off, n, 1, 1.0))
+        red.add(int(t["c_off"]), m, n, int(t["ldc"]), 1, terms)
+    ta = np.array(T, dtype=GEMM_TASK)
+    sa = np.array(S, dtype=GEMM_SEG) if S else np.zeros(0, GEMM_SEG)
+    return (ta, sa, _tiles_cost(ta, sa, TILE_M)), red.arrays(), extra
+
+
 class HostPlan3:
-    """A three-stage plan on the host: numpy tables plus sizes and MAC counts."""
+    """A three-stage plan on the host: numpy tables plus sizes and MAC counts (and an optional
+    fourth stage summing the split-K partials of stage 3)."""
 
     def __init__(self, g1: GemmTable, c2: CombTable, g3: GemmTable, ws1, ws2, out_layout,
-                 ref_macs=None, kind=""):
-        self.g1, self.c2, self.g3 = g1.arrays(), c2.arrays(), g3.arrays()
+                 ref_macs=None, kind="", split: bool = True):
+        self.g1, self.c2 = g1.arrays(), c2.arrays()
+        self.g3_unsplit = g3.arrays()
         self.ws1, self.ws2 = int(ws1), int(ws2)
+        self.ws2_unsplit = self.ws2
+        if split:
+            self.g3, self.c4, extra = split_long_tiles(self.g3_unsplit, self.ws1 + self.ws2)
+            self.ws2 += extra
+        else:
+            self.g3, self.c4 = self.g3_unsplit, _empty_comb()
         self.out_layout = out_layout
         self.macs = g1.macs + g3.macs
         self.comb_terms = len(c2.terms)
@@ -723,7 +798,7 @@ class HostPlanTC:
 
     def __init__(self, hp: HostPlan3, theta: Layout, L: Layout, R: Layout):
         from ._lib import CVT_TASK, TC_SEG
-        (t1, s1, _), (t2, c2, i2), (t3, s3, _) = hp.g1, hp.c2, hp.g3
+        (t1, s1, _), (t2, c2, i2), (t3, s3, _) = hp.g1, hp.c2, hp.g3_unsplit
         self.cursor = 0
         self.maps: List[tuple] = []
         map_of: Dict[tuple, int] = {}
@@ -881,6 +956,8 @@ class ComplexPlan3:
         self.g1 = complexify_gemm(hp.g1)
         self.c2 = complexify_comb(hp.c2)
         self.g3 = complexify_gemm(hp.g3)
+        self.c4 = complexify_comb(hp.c4)
+        self.g3_unsplit = complexify_gemm(hp.g3_unsplit)
         self.ws1, self.ws2 = 2 * hp.ws1, 2 * hp.ws2
         self.out_layout = hp.out_layout
         self.macs = 4 * hp.macs
