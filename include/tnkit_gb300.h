@@ -261,7 +261,8 @@ int tnk_combine_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
 /* ----------------------------------------------------------------------------------------
  * Lanczos vector kernels (FP64). Replace the reductions and CGS2 reorthogonalisation of
  * tnkit/eigensolver.py:560-604 (vdot, norm, two classical Gram-Schmidt passes).
- * `red` is a caller workspace of at least TNK_RED_ELEMS doubles for the two-phase reductions;
+ * `red` is a caller workspace of at least TNK_RED_ELEMS doubles (16-byte aligned) for the
+ * reductions;
  * results are written to device memory, so no call synchronises.
  * ---------------------------------------------------------------------------------------- */
 #define TNK_RED_ELEMS 65536
@@ -277,6 +278,23 @@ int tnk_multidot_f64(const double* V, int64_t ldv, int32_t nv, const double* w, 
 /* w[k] = w[k] - sum_i c[i] V[i*ldv + k], with c on the device (nv <= 64). */
 int tnk_gemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c, double* w,
                      int64_t n, void* stream);
+/* One fused pass of classical Gram-Schmidt against the rows V[0..nv) (nv <= 64), over a single
+ * read of the basis; `mode` is a sum of
+ *   TNK_CGS_SUB  w[k] -= sum_i cin[i] V[i*ldv + k]      (cin on the device; i ascending)
+ *   TNK_CGS_DOT  out[i] = sum_k V[i*ldv + k] w[k], i < nv (w after the subtraction)
+ *   TNK_CGS_NRM  out[0] = ||w||_2                        (w after the subtraction)
+ * (DOT and NRM exclude each other). Two passes, SUB|DOT then SUB|NRM after a DOT, are CGS2 with
+ * the Lanczos coefficients alpha = c1[j] + c2[j] and beta = ||w|| (the reference computes the
+ * same numbers with a three-term step, tnkit/eigensolver.py:567-599). The reduction finishes
+ * inside the launch: `counter` is a zero-initialised uint32 in device memory, used by one
+ * stream at a time, and left zero on return; `red` holds TNK_RED_ELEMS doubles, 16-byte
+ * aligned. */
+#define TNK_CGS_SUB 1
+#define TNK_CGS_DOT 2
+#define TNK_CGS_NRM 4
+int tnk_cgs_pass_f64(const double* V, int64_t ldv, int32_t nv, const double* cin, double* w,
+                     int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
+                     void* stream);
 /* y = a*x + b*y with the scalars a = sa[0]*fa, b = sb[0]*fb read from device memory when
  * sa/sb are non-null (else 1): lets Lanczos use alpha/beta without a host round trip. */
 int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,

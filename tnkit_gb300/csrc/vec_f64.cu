@@ -1,10 +1,14 @@
-// Lanczos vector kernels (FP64, sm_103a): dot, norm, the two GEMV passes of classical
-// Gram-Schmidt, and scalar updates that read their scalars from device memory.
+// Lanczos vector kernels (FP64, sm_103a): dot, norm, the passes of classical Gram-Schmidt
+// (fused subtract / multi-dot / norm over one read of the basis), and scalar updates that read
+// their scalars from device memory.
 //
-// All are HBM-bound streams. Reductions are two-phase and deterministic: phase 1 writes one
-// partial per CTA (warp-shuffle, then shared-memory reduction), phase 2 sums the partials in a
-// fixed order in one CTA. Grids are multiples of the 152 SMs, capped so the partials fit the
+// All are HBM-bound streams. Reductions are deterministic: each CTA writes its partials
+// (warp-shuffle, then shared-memory reduction), and one CTA sums them in a fixed order -- the
+// last CTA of the same launch when the caller passes a counter, else a second launch. Grids are
+// the resident CTAs of all SMs (or multiples of the 152 SMs), capped so the partials fit the
 // caller's TNK_RED_ELEMS workspace.
+#include <atomic>
+
 #include "tnk_internal.cuh"
 
 namespace tnk {
@@ -13,7 +17,6 @@ namespace {
 constexpr int NT = 256;
 constexpr int NSM = 152;
 constexpr int MAXNV = 64;
-constexpr int MD_ROWS = 8;   // rows of V reduced per pass of the multidot kernel
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -67,44 +70,278 @@ __global__ void __launch_bounds__(NT) sum_partials(const double* __restrict__ re
     }
 }
 
-// Partial c[i] over this CTA's chunk of k, MD_ROWS rows of V at a time (w is re-read from L1).
-__global__ void __launch_bounds__(NT) multidot_partial(const double* __restrict__ V, int64_t ldv,
-                                                       int nv, const double* __restrict__ w,
-                                                       int64_t n, double* __restrict__ red) {
-    __shared__ double sh[NT / 32];
-    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int64_t k0 = blockIdx.x * chunk;
-    const int64_t k1 = min(n, k0 + chunk);
-    for (int i0 = 0; i0 < nv; i0 += MD_ROWS) {
-        double acc[MD_ROWS];
-#pragma unroll
-        for (int r = 0; r < MD_ROWS; ++r) acc[r] = 0.0;
-        for (int64_t k = k0 + threadIdx.x; k < k1; k += NT) {
-            const double wk = w[k];
-#pragma unroll
-            for (int r = 0; r < MD_ROWS; ++r)
-                if (i0 + r < nv) acc[r] = fma(V[(int64_t)(i0 + r) * ldv + k], wk, acc[r]);
-        }
-#pragma unroll
-        for (int r = 0; r < MD_ROWS; ++r) {
-            if (i0 + r >= nv) break;
-            const double s = block_sum(acc[r], sh);
-            if (threadIdx.x == 0) red[(int64_t)blockIdx.x * MAXNV + i0 + r] = s;
-        }
+// ---- fused classical Gram-Schmidt pass -------------------------------------------------------
+// One read of the basis rows V[0..nv) serves up to two steps of CGS2 (mode bits):
+//   CG_SUB  w[k] -= sum_i cin[i] V[i,k]
+//   CG_DOT  c[i] = sum_k V[i,k] w[k]             (w after the subtraction)
+//   CG_NRM  s = sqrt(sum_k w[k]^2)               (w after the subtraction)
+// On GB300 these passes are bound by the FP64 pipe (~0.9 TFLOP/s for scalar FP64), not by HBM,
+// so the kernel spends one FP64 FMA per element and row and little else: one thread per
+// column, the subtraction as two interleaved FMA chains (even and odd rows, joined by one add)
+// to halve its dependent latency, and shared-memory tiles small enough for several CTAs per SM,
+// whose warps hide the FP64 latency. The k range is cut into tiles of CG_TK columns that stream
+// through a ring of 2..8 stages in shared memory, filled with asynchronous 8-byte copies
+// (cp.async, zero fill past n); each thread copies and reads only its own column, so the ring
+// needs no barrier. Each CTA writes its partials to red[cta * PSTRIDE + row]. The sum over CTAs
+// runs in one CTA, in a fixed order: the partials are copied into shared memory in one batch
+// (16-byte cp.async.cg, so L2 and not a stale L1 line is read) and summed per row. With a
+// counter, that CTA is the last of the launch to finish (atomic ticket after a fence), which
+// also resets the counter; without one, finish_kernel is a second launch.
+constexpr int CG_SUB = 1, CG_DOT = 2, CG_NRM = 4;
+constexpr int PSTRIDE = MAXNV + 2;     // even: every CTA's partial row starts 16-byte aligned
+constexpr int CG_TK = 128;             // columns per tile = threads per CTA
+constexpr int CG_NT = CG_TK;
+constexpr int CG_RING_BYTES = 48 * 1024;
+constexpr int CG_MAX_STAGES = 8;
+
+__host__ __device__ inline int cg_stages(int nv) {
+    int s = CG_RING_BYTES / ((nv + 1) * CG_TK * (int)sizeof(double));
+    return s < 2 ? 2 : (s > CG_MAX_STAGES ? CG_MAX_STAGES : s);
+}
+
+__host__ __device__ inline int cg_ring_bytes(int nv) {
+    return cg_stages(nv) * (nv + 1) * CG_TK * (int)sizeof(double);
+}
+
+// partial rows of one CTA, rounded up to an even count (16-byte copies)
+__host__ __device__ inline int cg_prow(int mode, int nv) {
+    const int r = (mode & CG_DOT) && nv > 1 ? nv : 1;
+    return (r + 1) & ~1;
+}
+
+__device__ __forceinline__ void cp_async8(double* dst, const double* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src),
+                 "r"(valid ? 8 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async16_cg(double* dst, const double* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// wait until at most `pending` (0..CG_MAX_STAGES-1) of this thread's copy groups are in flight
+__device__ __forceinline__ void cp_async_wait_dyn(int pending) {
+    switch (pending) {
+        case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+        case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+        case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+        case 3: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+        case 4: asm volatile("cp.async.wait_group 4;\n" ::: "memory"); break;
+        case 5: asm volatile("cp.async.wait_group 5;\n" ::: "memory"); break;
+        case 6: asm volatile("cp.async.wait_group 6;\n" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 7;\n" ::: "memory"); break;
     }
 }
 
-__global__ void __launch_bounds__(NT) gemv_sub_kernel(const double* __restrict__ V, int64_t ldv,
-                                                      int nv, const double* __restrict__ c,
-                                                      double* __restrict__ w, int64_t n) {
-    __shared__ double cs[MAXNV];
-    if (threadIdx.x < nv) cs[threadIdx.x] = c[threadIdx.x];
-    __syncthreads();
-    for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n; k += (int64_t)gridDim.x * NT) {
-        double acc = w[k];
-        for (int i = 0; i < nv; ++i) acc = fma(-cs[i], V[(int64_t)i * ldv + k], acc);
-        w[k] = acc;
+// Sum the partials of `nb` CTAs (prow doubles each, the first `nrow` used) into out[0..nrow),
+// square-rooted when `root`. Runs in one whole CTA of CG_NT threads; `stage` holds nb * prow
+// doubles. Each row is split among CG_NT / nrow threads (strided CTA subsets), whose sums are
+// then added in a fixed order: the result does not depend on timing.
+__device__ void finish_partials(const double* red, int nb, int prow, int nrow, bool root,
+                                double* stage, double* out) {
+    __shared__ double part[CG_NT];
+    const int half = prow / 2;
+    for (int e = threadIdx.x; e < nb * half; e += blockDim.x) {
+        const int b = e / half, h = e - b * half;
+        cp_async16_cg(stage + (int64_t)b * prow + 2 * h, red + (int64_t)b * PSTRIDE + 2 * h);
     }
+    cp_async_commit();
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    const int G = nrow > 0 ? CG_NT / nrow : 1;       // threads per row (nrow <= 64)
+    const int idx = threadIdx.x;
+    if (idx < nrow * G) {
+        const int r = idx / G, g = idx - r * G;
+        double s = 0.0;
+        for (int b = g; b < nb; b += G) s += stage[(int64_t)b * prow + r];
+        part[idx] = s;
+    }
+    __syncthreads();
+    if (idx < nrow) {
+        double s = 0.0;
+        for (int g = 0; g < G; ++g) s += part[idx * G + g];
+        out[idx] = root ? sqrt(s) : s;
+    }
+}
+
+__global__ void __launch_bounds__(CG_NT) finish_kernel(const double* __restrict__ red, int nb,
+                                                      int prow, int nrow, int root,
+                                                      double* __restrict__ out) {
+    extern __shared__ __align__(16) double fin[];
+    finish_partials(red, nb, prow, nrow, root != 0, fin, out);
+}
+
+template <int NVB, int MODE>
+__global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V, int64_t ldv,
+                                                   int nv, const double* __restrict__ cin,
+                                                   double* __restrict__ w, int64_t n,
+                                                   double* __restrict__ red,
+                                                   unsigned* __restrict__ counter,
+                                                   double* __restrict__ out) {
+    constexpr bool SUB = (MODE & CG_SUB) != 0;
+    constexpr bool DOT = (MODE & CG_DOT) != 0;
+    constexpr bool NRM = (MODE & CG_NRM) != 0;
+    constexpr int NACC = DOT ? NVB : 1;
+    extern __shared__ __align__(16) double ring[];   // [stage][row 0: w, rows 1..nv: V][CG_TK]
+    __shared__ double cs[NVB];
+    __shared__ double sh[CG_NT / 32][NVB + 1];
+    __shared__ bool last;
+    const int t = threadIdx.x;
+    const int rows = nv + 1;
+    const int stages = cg_stages(nv);
+    if (SUB && t < NVB) cs[t] = t < nv ? -cin[t] : 0.0;
+    __syncthreads();
+    const int64_t ntiles = (n + CG_TK - 1) / CG_TK;
+
+    auto issue = [&](int64_t tile, int slot) {
+        if (tile < ntiles) {
+            const int64_t k = tile * CG_TK + t;
+            const bool ok = k < n;
+            const int64_t kk = ok ? k : 0;
+            double* st = ring + (int64_t)slot * rows * CG_TK + t;
+            cp_async8(st, w + kk, ok);
+            for (int i = 0; i < nv; ++i)
+                cp_async8(st + (i + 1) * CG_TK, V + (int64_t)i * ldv + kk, ok);
+        }
+        cp_async_commit();
+    };
+
+    double acc[NACC];
+#pragma unroll
+    for (int i = 0; i < NACC; ++i) acc[i] = 0.0;
+    double accn = 0.0;
+    int64_t tile = blockIdx.x;
+    for (int s = 0; s < stages - 1; ++s) issue(tile + (int64_t)s * gridDim.x, s);
+    int slot = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        cp_async_wait_dyn(stages - 2);
+        issue(tile + (int64_t)(stages - 1) * gridDim.x, slot == 0 ? stages - 1 : slot - 1);
+        const double* st = ring + (int64_t)slot * rows * CG_TK + t;
+        const int64_t k = tile * CG_TK + t;
+        double wk = st[0];
+        if (SUB) {
+            double s1 = 0.0;
+            int i = 0;
+            for (; i + 1 < nv; i += 2) {
+                wk = fma(cs[i], st[(i + 1) * CG_TK], wk);
+                s1 = fma(cs[i + 1], st[(i + 2) * CG_TK], s1);
+            }
+            if (i < nv) wk = fma(cs[i], st[(i + 1) * CG_TK], wk);
+            wk += s1;
+            if (k < n) w[k] = wk;
+        }
+        if (DOT) {
+#pragma unroll
+            for (int j = 0; j < NACC; ++j)
+                if (j < nv) acc[j] = fma(st[(j + 1) * CG_TK], wk, acc[j]);
+        }
+        if (NRM) accn = fma(wk, wk, accn);
+        slot = slot + 1 == stages ? 0 : slot + 1;
+    }
+    cp_async_wait_dyn(0);
+    if (!DOT && !NRM) return;
+    const int lane = t & 31, wid = t >> 5;
+    if (DOT) {
+#pragma unroll
+        for (int j = 0; j < NACC; ++j) {
+            if (j >= nv) break;
+            const double s = warp_sum(acc[j]);
+            if (lane == 0) sh[wid][j] = s;
+        }
+    }
+    if (NRM) {
+        const double s = warp_sum(accn);
+        if (lane == 0) sh[wid][0] = s;
+    }
+    __syncthreads();
+    const int nrow = DOT ? nv : 1;
+    double* part = red + (int64_t)blockIdx.x * PSTRIDE;
+    if (t < nrow) {
+        double s = 0.0;
+        for (int y = 0; y < CG_NT / 32; ++y) s += sh[y][t];
+        part[t] = s;
+    }
+    if (!counter) return;
+    __threadfence();
+    __syncthreads();
+    if (t == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the ring is idle now; the grid cap keeps gridDim.x * prow doubles within it
+    finish_partials(red, gridDim.x, cg_prow(MODE, nv), nrow, NRM, ring, out);
+    if (t == 0) *counter = 0u;
+}
+
+// Grid size: one CTA per tile, at most the resident CTAs of all SMs, and few enough that the
+// partials fit the ring (for the in-launch sum) and TNK_RED_ELEMS.
+template <int NVB, int MODE>
+int cgs_grid(int64_t n, int nv) {
+    // per device: the opt-in to the largest ring; per row count: the resident CTAs per SM
+    static std::atomic<unsigned long long> opted{0};
+    static std::atomic<int> nsm{0};
+    static std::atomic<int> occ_of[MAXNV + 1];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(opted.load(std::memory_order_acquire) & bit)) {
+        int big = 0;
+        for (int v = 0; v <= NVB; ++v) big = cg_ring_bytes(v) > big ? cg_ring_bytes(v) : big;
+        cudaFuncSetAttribute(cgs_kernel<NVB, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             big);
+        cudaFuncSetAttribute(finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             cg_ring_bytes(MAXNV));
+        int cnt = 0;
+        if (cudaDeviceGetAttribute(&cnt, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cnt < 1)
+            cnt = NSM;
+        nsm.store(cnt, std::memory_order_relaxed);
+        opted.fetch_or(bit, std::memory_order_acq_rel);
+    }
+    int occ = occ_of[nv].load(std::memory_order_relaxed);
+    if (occ < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cgs_kernel<NVB, MODE>, CG_NT,
+                                                          cg_ring_bytes(nv)) != cudaSuccess ||
+            occ < 1)
+            occ = 1;
+        occ_of[nv].store(occ, std::memory_order_relaxed);
+    }
+    int64_t cap = (int64_t)occ * nsm.load(std::memory_order_relaxed);
+    const int64_t fit = cg_ring_bytes(nv) / (cg_prow(MODE, nv) * (int)sizeof(double));
+    if (cap > fit) cap = fit;
+    if (cap > TNK_RED_ELEMS / PSTRIDE) cap = TNK_RED_ELEMS / PSTRIDE;
+    int64_t g = (n + CG_TK - 1) / CG_TK;
+    if (g > cap) g = cap;
+    return g < 1 ? 1 : (int)g;
+}
+
+template <int NVB, int MODE>
+int launch_cgs_t(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+                 double* red, unsigned* counter, double* out, cudaStream_t st) {
+    const int g = cgs_grid<NVB, MODE>(n, nv);
+    cgs_kernel<NVB, MODE><<<g, CG_NT, cg_ring_bytes(nv), st>>>(V, ldv, nv, cin, w, n, red,
+                                                               counter, out);
+    int rc = check_launch("cgs_kernel");
+    if (rc || counter || !(MODE & (CG_DOT | CG_NRM))) return rc;
+    const int prow = cg_prow(MODE, nv);
+    finish_kernel<<<1, CG_NT, g * prow * (int)sizeof(double), st>>>(
+        red, g, prow, (MODE & CG_DOT) ? nv : 1, (MODE & CG_NRM) ? 1 : 0, out);
+    return check_launch("finish_kernel");
+}
+
+// One launch of a fixed mode over nv <= 64 rows (NVB, the accumulator count, picked from nv).
+template <int MODE>
+int launch_cgs(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+               double* red, unsigned* counter, double* out, cudaStream_t st) {
+    if (nv <= 16) return launch_cgs_t<16, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    if (nv <= 32) return launch_cgs_t<32, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    return launch_cgs_t<64, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
 }
 
 __global__ void __launch_bounds__(NT) axpby_kernel(const double* __restrict__ x,
@@ -143,19 +380,15 @@ int vec_dot(const double* x, const double* y, int64_t n, double* out, double* re
 
 int vec_multidot(const double* V, int64_t ldv, int nv, const double* w, int64_t n, double* c,
                  double* red, cudaStream_t stream) {
-    if (!V || !w || !c || !red || n < 0 || nv < 0 || nv > MAXNV || ldv < n) {
+    if (!V || !w || !c || !red || ((uintptr_t)red & 15) || n < 0 || nv < 0 || nv > MAXNV ||
+        ldv < n) {
         set_error("multidot: bad argument (nv=%d, n=%lld, ldv=%lld)", nv, (long long)n,
                   (long long)ldv);
         return TNK_ERR_ARG;
     }
     if (nv == 0) return TNK_OK;
-    // partials: grid * MAXNV doubles must fit TNK_RED_ELEMS
-    const int g = grid_for(n, TNK_RED_ELEMS / MAXNV);
-    multidot_partial<<<g, NT, 0, stream>>>(V, ldv, nv, w, n, red);
-    int rc = check_launch("multidot_partial");
-    if (rc) return rc;
-    sum_partials<<<1, NT, 0, stream>>>(red, g, MAXNV, nv, 0, c);
-    return check_launch("sum_partials");
+    return launch_cgs<CG_DOT>(V, ldv, nv, nullptr, const_cast<double*>(w), n, red, nullptr, c,
+                              stream);
 }
 
 int vec_gemv_sub(const double* V, int64_t ldv, int nv, const double* c, double* w, int64_t n,
@@ -165,8 +398,33 @@ int vec_gemv_sub(const double* V, int64_t ldv, int nv, const double* c, double* 
         return TNK_ERR_ARG;
     }
     if (nv == 0 || n == 0) return TNK_OK;
-    gemv_sub_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(V, ldv, nv, c, w, n);
-    return check_launch("gemv_sub_kernel");
+    return launch_cgs<CG_SUB>(V, ldv, nv, c, w, n, nullptr, nullptr, nullptr, stream);
+}
+
+int vec_cgs_pass(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+                 double* out, int mode, double* red, unsigned* counter, cudaStream_t st) {
+    const bool sub = mode & CG_SUB, dot = mode & CG_DOT, nrm = mode & CG_NRM;
+    if (n < 0 || nv < 0 || nv > MAXNV || mode < 1 || mode > 7 || (dot && nrm) ||
+        (n > 0 && !w) || ((sub || dot) && (ldv < n || (n > 0 && nv > 0 && !V))) ||
+        (sub && !cin) ||
+        ((dot || nrm) && (!out || !red || ((uintptr_t)red & 15) || !counter))) {
+        set_error("cgs_pass: bad argument (mode=%d, nv=%d, n=%lld, ldv=%lld)", mode, nv,
+                  (long long)n, (long long)ldv);
+        return TNK_ERR_ARG;
+    }
+    switch (mode) {
+        case CG_SUB:
+            if (nv == 0) return TNK_OK;
+            return launch_cgs<CG_SUB>(V, ldv, nv, cin, w, n, nullptr, nullptr, nullptr, st);
+        case CG_DOT:
+            return launch_cgs<CG_DOT>(V, ldv, nv, cin, w, n, red, counter, out, st);
+        case CG_SUB | CG_DOT:
+            return launch_cgs<CG_SUB | CG_DOT>(V, ldv, nv, cin, w, n, red, counter, out, st);
+        case CG_NRM:
+            return launch_cgs<CG_NRM>(V, ldv, 0, nullptr, w, n, red, counter, out, st);
+        default:  // CG_SUB | CG_NRM
+            return launch_cgs<CG_SUB | CG_NRM>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    }
 }
 
 int vec_axpby(const double* x, double* y, int64_t n, const double* sa, double fa,

@@ -1,11 +1,19 @@
 """Thick-restart Lanczos on the GPU (tnkit/eigensolver.py:507-674).
 
-The Krylov basis (m+1 vectors) lives on the device; every vector operation is a tnk_* kernel:
-alpha = <v, w> and beta = ||w|| as deterministic two-phase reductions, the two classical
-Gram-Schmidt passes as one multi-dot plus one GEMV each, the three-term and arrowhead couplings
-as axpy/GEMV with their scalars read from device memory. The host reads two doubles per
-iteration (alpha, beta) for the projected (m x m) eigenproblem, which it solves with LAPACK, as
-the reference does; the restart's basis rotation is one grouped-GEMM launch.
+The Krylov basis (m+1 vectors) lives on the device. One iteration is the matvec and three fused
+classical Gram-Schmidt launches (tnk_cgs_pass_f64): c1 = V^T w; w -= V c1 with c2 = V^T w in the
+same read of V; w -= V c2 with beta = ||w|| in the same read -- the reference's CGS2
+(tnkit/eigensolver.py:581-595), which also removes the three-term and arrowhead couplings the
+reference subtracts first, with alpha = <v_j, H v_j> = c1[j]. Every reduction is deterministic
+and finishes inside its launch; the coefficients and beta land in a device record that one
+asynchronous copy brings to pinned host memory.
+
+The host solves the projected (<= m x m) eigenproblem with LAPACK, as the reference does
+(a tridiagonal solver for the lowest pair before the first restart, the full symmetric one after).
+Its work overlaps the GPU: the next iteration, which needs nothing from the host, is queued before
+the host waits for the current one, unless the residual trend says the current one is likely the
+last; a queued iteration that turns out not to be needed is discarded (it writes only the next
+basis row and the work vector). The restart's basis rotation is one grouped-GEMM launch.
 
 The algorithm, stopping rule (Ritz residual |beta * y_last| < tol), breakdown rule
 (beta < 1e-12 max(1, |alpha|)) and restart (k lowest Ritz vectors plus the residual direction,
@@ -14,39 +22,45 @@ arrowhead projected matrix) are the reference's.
 from __future__ import annotations
 
 import ctypes as C
-import time
 from typing import Callable, Optional
 
 import numpy as np
 import torch
+from scipy.linalg import eigh_tridiagonal
 
 from . import _lib
 from ._lib import GEMM_SEG, GEMM_TASK, GEMM_TILE
 from .plan import TILE_M, TILE_N
 
 _MAXNV = 64
+_REC = 1 + 2 * _MAXNV           # per-iteration device record: beta, c1[0:64], c2[0:64]
+_SUB, _DOT, _NRM = 1, 2, 4      # tnk_cgs_pass_f64 modes
 
 
 class _Dev:
-    """Device scratch of one solve: reduction workspace, scalar slots and a pinned mirror."""
+    """Device scratch of one solve: reduction workspace and completion counter, scalar slots,
+    two iteration records (device and pinned host, alternating) with their events."""
 
     def __init__(self, device):
         self.red = torch.empty(_lib.TNK_RED_ELEMS, dtype=torch.float64, device=device)
+        self.cnt = torch.zeros(4, dtype=torch.int32, device=device)
         self.sc = torch.zeros(8 + _MAXNV, dtype=torch.float64, device=device)
         self.host = torch.zeros(8, dtype=torch.float64, pin_memory=True)
+        self.rec = torch.zeros((2, _REC), dtype=torch.float64, device=device)
+        self.hrec = torch.zeros((2, _REC), dtype=torch.float64, pin_memory=True)
+        self.ev = [torch.cuda.Event(), torch.cuda.Event()]
         self.lib = _lib.lib()
         self.sp = _lib.stream_ptr()
 
     def addr(self, i):
         return self.sc.data_ptr() + 8 * i
 
+    def raddr(self, par, i):
+        return self.rec.data_ptr() + 8 * (par * _REC + i)
+
     def nrm2(self, x, slot):
         _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.addr(slot),
                                          self.red.data_ptr(), self.sp), "nrm2")
-
-    def dot(self, x, y, slot):
-        _lib.check(self.lib.tnk_dot_f64(x.data_ptr(), y.data_ptr(), x.numel(), self.addr(slot),
-                                        self.red.data_ptr(), self.sp), "dot")
 
     def axpby(self, x, y, fa, fb, sa=None, sb=None):
         _lib.check(self.lib.tnk_axpby_f64(x.data_ptr(), y.data_ptr(), x.numel(),
@@ -54,15 +68,14 @@ class _Dev:
                                           None if sb is None else self.addr(sb), fb, self.sp),
                    "axpby")
 
-    def scale_div(self, x, y, slot, f=1.0):
-        _lib.check(self.lib.tnk_scale_div_f64(x.data_ptr(), y.data_ptr(), x.numel(),
-                                              self.addr(slot), f, self.sp), "scale_div")
+    def scale_div(self, x, y, s_addr, f=1.0):
+        _lib.check(self.lib.tnk_scale_div_f64(x.data_ptr(), y.data_ptr(), x.numel(), s_addr, f,
+                                              self.sp), "scale_div")
 
-    def multidot(self, V, nv, w):
-        n = w.numel()
-        _lib.check(self.lib.tnk_multidot_f64(V.data_ptr(), V.stride(0), nv, w.data_ptr(), n,
-                                             self.addr(8), self.red.data_ptr(), self.sp),
-                   "multidot")
+    def cgs(self, V, nv, cin, w, out, mode):
+        _lib.check(self.lib.tnk_cgs_pass_f64(V.data_ptr(), V.stride(0), nv, cin, w.data_ptr(),
+                                             w.numel(), out, mode, self.red.data_ptr(),
+                                             self.cnt.data_ptr(), self.sp), "cgs_pass")
 
     def gemv_sub(self, V, nv, w):
         _lib.check(self.lib.tnk_gemv_sub_f64(V.data_ptr(), V.stride(0), nv, self.addr(8),
@@ -71,10 +84,33 @@ class _Dev:
     def set_coeffs(self, c: np.ndarray):
         self.sc[8:8 + len(c)].copy_(torch.as_tensor(np.ascontiguousarray(c, np.float64)))
 
-    def read(self, n=2):
-        self.host[:n].copy_(self.sc[:n], non_blocking=True)
+    def read_slot(self, i):
+        self.host[i:i + 1].copy_(self.sc[i:i + 1], non_blocking=True)
         torch.cuda.current_stream().synchronize()
-        return self.host[:n].tolist()
+        return float(self.host[i])
+
+    def issue(self, matvec, V, w, j, count, scale):
+        """Queue iteration `count` (basis row j): [V[j] = w / beta of the previous iteration],
+        w = H V[j], CGS2 against V[0..j], beta; then the record's copy to the host and its event.
+        Returns the record parity."""
+        par = count & 1
+        if scale:
+            self.scale_div(w, V[j], self.raddr(par ^ 1, 0))
+        matvec(V[j], w)
+        nv = j + 1
+        c1, c2 = self.raddr(par, 1), self.raddr(par, 1 + _MAXNV)
+        self.cgs(V, nv, None, w, c1, _DOT)
+        self.cgs(V, nv, c1, w, c2, _SUB | _DOT)
+        self.cgs(V, nv, c2, w, self.raddr(par, 0), _SUB | _NRM)
+        self.hrec[par].copy_(self.rec[par], non_blocking=True)
+        self.ev[par].record()
+        return par
+
+    def wait(self, par, j):
+        """(alpha, beta) of the iteration recorded in `par` (basis row j)."""
+        self.ev[par].synchronize()
+        h = self.hrec[par]
+        return float(h[1 + j]), float(h[0])
 
     def rotate(self, Y: np.ndarray, V: torch.Tensor, out: torch.Tensor):
         """out (kk x n) = Y^T (kk x cur) @ V[:cur] as one grouped-GEMM launch."""
@@ -99,111 +135,119 @@ class _Dev:
         return A, t_task, t_seg, t_tl       # keep alive until the stream passes them
 
 
+def _lowest(T: np.ndarray, cur: int, tridiagonal: bool):
+    """Lowest eigenpair of the projected matrix T[:cur, :cur]."""
+    if cur == 1:
+        return float(T[0, 0]), np.array([1.0])
+    if tridiagonal:
+        ev, evec = eigh_tridiagonal(np.diagonal(T)[:cur].copy(),
+                                    np.diagonal(T, 1)[:cur - 1].copy(), select="i",
+                                    select_range=(0, 0), check_finite=False)
+    else:
+        ev, evec = np.linalg.eigh(T[:cur, :cur])
+    return float(ev[0]), evec[:, 0]
+
+
 def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8,
                            max_iter: int = 200, m: int = 40, k: int = 10,
-                           timers: Optional[dict] = None, basis: Optional[torch.Tensor] = None,
-                           stall: int = 0):
+                           basis: Optional[torch.Tensor] = None, stall: int = 0,
+                           speculate: bool = True):
     """Lowest eigenpair of the operator `matvec(x, out) -> out` from the start `v0` (float64
     CUDA vector). Returns (theta, x, info) like the reference; x is normalised.
 
     stall > 0 also stops when the Ritz residual has improved by less than 10 % over the last
-    `stall` iterations (info["stalled"]): the floor of a low-precision operator."""
+    `stall` iterations (info["stalled"]): the floor of a low-precision operator.
+    speculate=False waits for every iteration before queuing the next (no discarded matvec)."""
     if k >= m:
         k = max(1, m // 2)
     if m + 1 > _MAXNV:
         raise ValueError(f"restart window m={m} exceeds {_MAXNV - 1}")
+    if max_iter < 1:
+        raise ValueError("max_iter must be >= 1")
     dev = v0.device
     D = _Dev(dev)
     n = v0.numel()
     v0 = v0.reshape(-1)
     D.nrm2(v0, 2)
-    D.host[2:3].copy_(D.sc[2:3], non_blocking=True)
-    torch.cuda.current_stream().synchronize()
-    n0 = float(D.host[2])
+    n0 = D.read_slot(2)
     if not np.isfinite(n0) or n0 < 1e-300:
-        return 0.0, v0, {"iters": 0, "converged": False, "restarts": 0}
+        return 0.0, v0, {"iters": 0, "converged": False, "restarts": 0, "matvecs": 0}
     Vb = basis if (basis is not None and basis.shape[0] >= m + 1 and basis.shape[1] == n) \
         else torch.empty((m + 1, n), dtype=torch.float64, device=dev)
-    D.scale_div(v0, Vb[0], 2)
+    D.scale_div(v0, Vb[0], D.addr(2))
     w = torch.empty(n, dtype=torch.float64, device=dev)
     T = np.zeros((m + 1, m + 1))
-    nV, n_kept, border = 1, 0, None
-    beta_prev, v_prev = 0.0, None
+    n_kept = 0
     theta, y = 0.0, np.array([1.0])
-    converged, restarts, it, j = False, 0, 0, 0
+    converged, stalled, restarts, it = False, False, 0, 0
     keep = []
     hist = []
-    stalled = False
-    tm = timers if timers is not None else None
-    while it < max_iter:
-        t0 = time.perf_counter() if tm is not None else 0.0
-        v = Vb[j]
-        matvec(v, w)
-        if n_kept and j == n_kept:
-            D.set_coeffs(border)
-            D.gemv_sub(Vb, n_kept, w)
-        elif j > 0:
-            D.axpby(v_prev, w, -beta_prev, 1.0)
-        D.dot(v, w, 0)
-        D.axpby(v, w, -1.0, 1.0, sa=0)
-        for _ in range(2):
-            D.multidot(Vb, nV, w)
-            D.gemv_sub(Vb, nV, w)
-        D.nrm2(w, 1)
-        alpha, beta = D.read(2)
-        if tm is not None:
-            tm["device"] = tm.get("device", 0.0) + time.perf_counter() - t0
+    res = None
+    issued = 1
+    pending = [(0, D.issue(matvec, Vb, w, 0, 0, scale=False))]
+
+    def likely_last():
+        # the iteration being waited for converges if its residual falls below tol: predict it
+        # from the last two residuals (geometric trend) and skip queuing past it when it would
+        if len(hist) < 2 or hist[-2] <= 0.0:
+            return False
+        q = min(1.0, hist[-1] / hist[-2])
+        return hist[-1] * q < 10.0 * tol
+
+    while True:
+        j, par = pending.pop(0)
+        if (speculate and not pending and j + 1 < m and it + 1 < max_iter
+                and not likely_last()):
+            pending.append((j + 1, D.issue(matvec, Vb, w, j + 1, issued, scale=True)))
+            issued += 1
+        alpha, beta = D.wait(par, j)
         T[j, j] = alpha
         cur = j + 1
-        if cur == 1:
-            th, y = alpha, np.array([1.0])
-        else:
-            ev, evec = np.linalg.eigh(T[:cur, :cur])
-            th, y = float(ev[0]), evec[:, 0]
+        th, y = _lowest(T, cur, n_kept == 0)
         it += 1
         res = abs(beta) * abs(float(y[-1]))
+        hist.append(res)
         breakdown = (not np.isfinite(beta) or not np.isfinite(alpha)
                      or beta < 1e-12 * max(1.0, abs(alpha)))
         theta = th
         if breakdown or res < tol:
             converged = True
             break
-        if stall:
-            hist.append(res)
-            if len(hist) > stall and res > 0.9 * hist[-stall - 1]:
-                stalled = True
-                break
-        if cur >= m:                                 # thick restart
+        if stall and len(hist) > stall and res > 0.9 * hist[-stall - 1]:
+            stalled = True
+            break
+        if it >= max_iter:
+            break
+        if cur >= m:                                 # thick restart (nothing queued here)
             ev, evec = np.linalg.eigh(T[:cur, :cur])
             kk = min(k, cur - 1)
             Yk = evec[:, :kk]
             tmp = torch.empty((kk, n), dtype=torch.float64, device=dev)
             keep = D.rotate(Yk, Vb[:cur], tmp)
             D.axpby(tmp.reshape(-1), Vb[:kk].reshape(-1), 1.0, 0.0)
-            D.scale_div(w, Vb[kk], 1)
-            nV = kk + 1
             T[:] = 0.0
             border = beta * np.asarray(Yk[cur - 1, :], dtype=np.float64)
             for i in range(kk):
                 T[i, i] = ev[i]
                 T[i, kk] = T[kk, i] = border[i]
-            n_kept, j = kk, kk
-            beta_prev, v_prev = 0.0, None
+            n_kept = kk
             y = np.zeros(kk + 1)
             y[0] = 1.0
             restarts += 1
+            pending.append((kk, D.issue(matvec, Vb, w, kk, issued, scale=True)))
+            issued += 1
             continue
         T[j, j + 1] = T[j + 1, j] = beta
-        v_prev, beta_prev = v, beta
-        D.scale_div(w, Vb[j + 1], 1)
-        nV = j + 2
-        j += 1
-    ny = min(len(y), nV)
+        if not pending:
+            pending.append((j + 1, D.issue(matvec, Vb, w, j + 1, issued, scale=True)))
+            issued += 1
+    ny = len(y)
     x = torch.zeros(n, dtype=torch.float64, device=dev)
     D.set_coeffs(-np.asarray(y[:ny], np.float64))
     D.gemv_sub(Vb, ny, x)
     D.nrm2(x, 3)
-    D.scale_div(x, x, 3)
+    D.scale_div(x, x, D.addr(3))
     del keep
     return theta, x, {"iters": it, "converged": converged, "restarts": restarts,
-                      "stalled": stalled, "residual": res if it else None}
+                      "stalled": stalled, "residual": res, "matvecs": issued,
+                      "discarded": issued - it}
