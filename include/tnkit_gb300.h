@@ -323,6 +323,19 @@ int tnk_zgemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c,
 int tnk_zaxpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,
                    const double* sb, double fb, void* stream);
 
+/* ----------------------------------------------------------------------------------------
+ * Truncation: the per-sector factorisation of tnkit/blocks.py:1380-1462 with method='gram'
+ * (the block SVD through the smaller Gram matrix, tnkit/blocks.py:1345-1377) on cuSOLVER and
+ * cuBLAS. M is a row-major R x C block; U (R x k) and Vh (k x C) are written row-major, S (k)
+ * descending (stable order), k = min(R, C). The call synchronises its stream and returns when
+ * the outputs are written; S_host (optional, k doubles) receives a host copy of S. It allocates
+ * nothing: `ws` (256-byte aligned) holds at least tnk_svd_gram_ws_f64(R, C) bytes. Calls on
+ * different streams from different host threads run concurrently (handles are per thread).
+ * ---------------------------------------------------------------------------------------- */
+int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes);
+int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U, double* S, double* Vh,
+                     void* ws, int64_t ws_bytes, double* S_host, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,90 @@
+"""The per-sector Gram factorisation of the truncation (tnk_svd_gram_f64, the reference's
+method='gram', tnkit/blocks.py:1345-1377) against numpy's SVD and the torch statement of the same
+method: orthonormal factors, reconstruction, singular values in descending stable order, tall,
+wide, square and one-row/one-column blocks."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tnkit_gb300 import build
+    build.build()
+
+
+def _decaying(R, C, seed, span=6.0):
+    rng = np.random.default_rng(seed)
+    k = min(R, C)
+    U, _ = np.linalg.qr(rng.standard_normal((R, k)))
+    V, _ = np.linalg.qr(rng.standard_normal((C, k)))
+    s = 10.0 ** (-np.linspace(0.0, span, k))
+    return (U * s) @ V.T, s
+
+
+@pytest.mark.parametrize("R,C", [(1, 1), (1, 7), (7, 1), (40, 40), (300, 120), (120, 300),
+                                 (522, 519)])
+def test_native_gram_matches_svd(R, C):
+    from tnkit_gb300.linalg import _svd_gram, _svd_gram_native
+    M, s = _decaying(R, C, R * 1000 + C)
+    Md = torch.as_tensor(M, device="cuda")
+    U, S, Vh, s_host = _svd_gram_native(Md)
+    torch.cuda.synchronize()
+    k = min(R, C)
+    assert U.shape == (R, k) and S.shape == (k,) and Vh.shape == (k, C)
+    Uh, Sh, Vhh = U.cpu().numpy(), S.cpu().numpy(), Vh.cpu().numpy()
+    assert np.array_equal(Sh, s_host)
+    assert np.all(np.diff(Sh) <= 0)
+    # through the Gram matrix the values are exact to ~1e-16 of the largest squared
+    assert np.abs(Sh - s).max() <= 1e-10 * s[0]
+    assert np.abs(Uh.T @ Uh - np.eye(k)).max() <= 1e-12
+    assert np.abs(Vhh @ Vhh.T - np.eye(k)).max() <= 1e-12
+    # S = |diag R| drops R's off-diagonal; the reference's own bar for both methods is 1e-10 of
+    # the largest value (tests/test_blocks.py:563-586)
+    assert np.abs((Uh * Sh) @ Vhh - M).max() <= 1e-10 * s[0]
+    # the torch statement of the same method gives the same factors up to column signs
+    U2, S2, Vh2 = _svd_gram(Md)
+    assert np.abs(S2.cpu().numpy() - Sh).max() <= 1e-10 * s[0]
+    big = Sh > 1e-2 * Sh[0]          # vectors well separated at FP64 Gram precision
+    for a, b in ((Uh[:, big], U2.cpu().numpy()[:, big]), (Vhh[big].T, Vh2.cpu().numpy()[big].T)):
+        sg = np.sign(np.sum(a * b, axis=0))
+        assert np.abs(a - b * sg).max() <= 1e-9
+
+
+def test_native_gram_rejects_bad_workspace():
+    import ctypes as C
+    from tnkit_gb300 import _lib
+    lib = _lib.lib()
+    M = torch.ones((4, 3), dtype=torch.float64, device="cuda")
+    out = torch.empty(64, dtype=torch.float64, device="cuda")
+    ws = torch.empty(64, dtype=torch.uint8, device="cuda")
+    nb = C.c_int64()
+    assert lib.tnk_svd_gram_ws_f64(4, 3, C.byref(nb)) == 0 and nb.value > 64
+    rc = lib.tnk_svd_gram_f64(M.data_ptr(), 4, 3, out.data_ptr(), out.data_ptr(),
+                              out.data_ptr(), ws.data_ptr(), 64, None, _lib.stream_ptr())
+    assert rc == _lib.TNK_ERR_SIZE
+
+
+def test_truncated_svd_gram_native_matches_torch_path():
+    """The bond truncation with the native factorisation keeps the same sectors and values as
+    the torch statement of the method, and reconstructs the kept part."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(3)
+    a = Leg((-1, 1), (5, 7), 1)
+    b = Leg((-1, 1), (6, 4), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size)
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    U, S, Vh, disc = LA.truncated_svd(m, 6, scale="none", method="gram")
+    full = np.linalg.svd(h[:30].reshape(5, 6), compute_uv=False).tolist() + \
+        np.linalg.svd(h[30:].reshape(7, 4), compute_uv=False).tolist()
+    full = np.sort(full)[::-1]
+    assert np.allclose(np.sort(S.cpu().numpy())[::-1], full[:6], rtol=1e-12, atol=0)
+    assert abs(disc - float(np.sum(full[6:] ** 2))) <= 1e-12 * float(np.sum(full ** 2))

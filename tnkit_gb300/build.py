@@ -65,7 +65,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"]
+    libdir = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "lib64")
+    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static", "-L", libdir,
+           "-lcusolver", "-lcublas", "-Xlinker", f"-rpath={libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -8,12 +8,16 @@ SVD with the global cut across sectors, the per-block LQ of the initial canonica
                           (-sigma, position), new bond sectors labelled by the row charge
   lq                      tnkit/blocks.py:1465-1495 (right=True)
 
-The per-sector factorisations call cuSOLVER through torch.linalg (svd, qr): the truncation is
-kept in FP64 on the GPU; only the singular values cross to the host, once per bond.
+The per-sector factorisations run on cuSOLVER/cuBLAS, FP64 on the GPU, from a thread pool with one
+stream per sector: method='gram' on real blocks is one library call per sector
+(tnk_svd_gram_f64, which releases the interpreter lock and hands back S on the host), 'svd' and
+complex blocks go through torch.linalg. Only the singular values cross to the host, once per
+bond.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
+import ctypes as C
 import threading
 from typing import Tuple
 
@@ -113,7 +117,8 @@ class _Concurrent:
             with torch.cuda.stream(streams[i]):
                 out = fn(mats[i])
                 for t in out:
-                    t.record_stream(main)
+                    if isinstance(t, torch.Tensor):
+                        t.record_stream(main)
                 return out
         res = list(self.pool.map(run, range(len(mats))))
         for s in streams:
@@ -129,6 +134,25 @@ def _concurrent() -> _Concurrent:
     if _CONC is None:
         _CONC = _Concurrent()
     return _CONC
+
+
+def _svd_gram_native(M: torch.Tensor):
+    """U, S, Vh (and S on the host) of one real FP64 CUDA block by tnk_svd_gram_f64: the same
+    factorisation as _svd_gram in one library call that holds no interpreter lock."""
+    R, Cc = M.shape
+    k = min(R, Cc)
+    lib = _lib.lib()
+    nb = C.c_int64()
+    _lib.check(lib.tnk_svd_gram_ws_f64(R, Cc, C.byref(nb)), "svd_gram_ws")
+    ws = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=M.device)
+    U = torch.empty((R, k), dtype=torch.float64, device=M.device)
+    S = torch.empty(k, dtype=torch.float64, device=M.device)
+    Vh = torch.empty((k, Cc), dtype=torch.float64, device=M.device)
+    s_host = np.empty(k, dtype=np.float64)
+    _lib.check(lib.tnk_svd_gram_f64(M.data_ptr(), R, Cc, U.data_ptr(), S.data_ptr(),
+                                    Vh.data_ptr(), ws.data_ptr(), ws.numel(),
+                                    s_host.ctypes.data, _lib.stream_ptr()), "svd_gram")
+    return U, S, Vh, s_host
 
 
 def _svd_gram(M: torch.Tensor):
@@ -166,9 +190,10 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     lr, lc = m.layout.legs
     blocks = list(_blocks(m))
     if method == "gram":
-        fn = _svd_gram
+        fn = _svd_gram_native if (m.data.is_cuda and m.data.dtype == torch.float64) \
+            else (lambda M: _svd_gram(M) + (None,))
     elif method == "svd":
-        fn = lambda M: torch.linalg.svd(M, full_matrices=False, driver=driver)
+        fn = lambda M: tuple(torch.linalg.svd(M, full_matrices=False, driver=driver)) + (None,)
     else:
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
     mats = [M for _, _, M in blocks]
@@ -176,10 +201,13 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
         facs = _concurrent().map(fn, mats, m.data.device)
     else:
         facs = [fn(M) for M in mats]
-    parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh) in zip(blocks, facs)]
+    parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
     if not parts:
         raise ValueError("the matrix has no allowed blocks")
-    s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
+    if all(f[3] is not None for f in facs):
+        s_host = np.concatenate([f[3] for f in facs])
+    else:
+        s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
     owner = np.concatenate([np.full(len(p[3]), j) for j, p in enumerate(parts)])
     order = np.lexsort((np.arange(s_host.size), -s_host))
     k = min(int(chi), s_host.size)
@@ -211,10 +239,15 @@ def _zero_like(q):
 def lq(m: BlockTensor):
     """m = L Q per block, Q with orthonormal rows (the new bond labelled by the row charge)."""
     lr, lc = m.layout.legs
-    new = []
-    for r, c, M in _blocks(m):
+    blocks = list(_blocks(m))
+
+    def fac(M):
         q, t = torch.linalg.qr(M.mH)
-        new.append((_row_label(lr, r), r, c, t.mH.contiguous(), q.mH.contiguous()))
+        return t.mH.contiguous(), q.mH.contiguous()
+    mats = [M for _, _, M in blocks]
+    facs = _concurrent().map(fac, mats, m.data.device) if len(mats) > 1 and m.data.is_cuda \
+        else [fac(M) for M in mats]
+    new = [(_row_label(lr, r), r, c, a, b) for (r, c, _), (a, b) in zip(blocks, facs)]
     new.sort(key=lambda x: x[0])
     bond = Leg(tuple(x[0] for x in new), tuple(int(x[3].shape[1]) for x in new), 1)
     A = torch.cat([a.reshape(-1) for _, _, _, a, _ in sorted(new, key=lambda x: x[1])])
