@@ -295,6 +295,15 @@ int tnk_gemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c, 
 int tnk_cgs_pass_f64(const double* V, int64_t ldv, int32_t nv, const double* cin, double* w,
                      int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
                      void* stream);
+/* The same pass on FP32 vectors (FP32 arithmetic; coefficients and results in double): the
+ * Krylov basis of the tensor-core stage of the mixed-precision solve, whose operator is only
+ * ~1e-6 accurate, is kept in FP32. */
+int tnk_cgs_pass_f32(const float* V, int64_t ldv, int32_t nv, const double* cin, float* w,
+                     int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
+                     void* stream);
+/* y = x * (f / s[0]) on FP32 vectors, s on the device (double). */
+int tnk_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,
+                      void* stream);
 /* y = a*x + b*y with the scalars a = sa[0]*fa, b = sb[0]*fb read from device memory when
  * sa/sb are non-null (else 1): lets Lanczos use alpha/beta without a host round trip. */
 int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,

@@ -103,3 +103,28 @@ def test_ff_dmrg_matches_reference(prec):
     E, M, info = dmrg(_xxz_blocks(64), 64, charge=0, seed=1, n_sweeps=len(ref["energies"]),
                       tol=0, rtol=0, expand=0, precision=prec)
     assert abs(E - ref["E"]) <= 1e-12 * abs(ref["E"]), (E, ref["E"])
+
+
+@pytest.mark.parametrize("scale", [4, 1])
+def test_float_float_env_updates_match_fp64(scale):
+    """Left and right environment updates in float-float against FP64 at the chi=1024 mid-bond
+    sectors (scaled down by `scale`): ~1e-14 relative to the largest entry."""
+    from tnkit_gb300 import ops, workloads
+    from tnkit_gb300.layout import Leg, layout_of
+    from tnkit_gb300.tensor import BlockTensor
+    dims = [max(1, d // scale) for d in workloads.C2_MID_DIMS]
+    th, L, W1, W2, R = workloads.mid_bond_problem(dims=dims, seed=11)
+    bl, phys = th.layout.legs[0], th.layout.legs[1]
+    # the neighbouring bond: odd charges -9..9 (one spin more or less), dims between the mid's
+    odd = tuple(range(-9, 10, 2))
+    dodd = (dims[0],) + tuple(max(1, (a + b) // 2) for a, b in zip(dims, dims[1:])) + (dims[-1],)
+    rng = np.random.default_rng(3)
+    A_l = layout_of((bl, phys, Leg(odd, dodd, -1)), 0)
+    A = BlockTensor(A_l, torch.as_tensor(rng.standard_normal(A_l.size), device="cuda"))
+    B_l = layout_of((Leg(odd, dodd, 1), phys, bl.flip()), 0)
+    B = BlockTensor(B_l, torch.as_tensor(rng.standard_normal(B_l.size), device="cuda"))
+    for f, env, site, W in ((ops.update_left_env, L, A, W1), (ops.update_right_env, R, B, W2)):
+        ref = f(env, site, W).data
+        got = f(env, site, W, precision="ff").data
+        assert got.shape == ref.shape
+        assert _rel(got, ref) <= 1e-13, (f.__name__, _rel(got, ref))

@@ -146,3 +146,52 @@ def test_pipelined_lanczos_without_speculation_agrees():
     assert i1["iters"] == i2["iters"] and i2["discarded"] == 0 and i1["discarded"] <= 1
     assert abs(e1 - ev) <= 1e-10 * abs(ev) and abs(e2 - ev) <= 1e-10 * abs(ev)
     assert abs(abs(float(torch.dot(x1, x2))) - 1.0) <= 1e-9
+
+
+@pytest.mark.parametrize("nv", [1, 16, 33])
+def test_cgs_f32_modes_match_numpy(ctx, nv):
+    """The FP32 pass: FP32 arithmetic, so the bar is FP32 rounding of the summed magnitudes."""
+    n = 200003
+    V, w, c = _data(nv, n, n, 100 + nv)
+    V32, w32 = V.astype(np.float32), w.astype(np.float32)
+    Vd = torch.as_tensor(V32, device="cuda")
+    cd = torch.as_tensor(c, device="cuda")
+    lib = ctx.lib
+    out = torch.zeros(66, dtype=torch.float64, device="cuda")
+
+    def run(wd, mode, cin=None):
+        return lib.tnk_cgs_pass_f32(Vd.data_ptr(), n, nv,
+                                    None if cin is None else cin.data_ptr(), wd.data_ptr(), n,
+                                    out.data_ptr(), mode, ctx.red.data_ptr(),
+                                    ctx.cnt.data_ptr(), ctx.sp)
+    Vn, wn = V32[:nv].astype(np.float64), w32.astype(np.float64)
+    wd = torch.as_tensor(w32, device="cuda")
+    assert run(wd, DOT) == 0
+    tol = 4e-6 * (np.abs(Vn) @ np.abs(wn))
+    assert np.all(np.abs(out[:nv].cpu().numpy() - Vn @ wn) <= tol)
+    ws = wn - c[:nv] @ Vn
+    assert run(wd, SUB | NRM, cd) == 0
+    scale = np.abs(wn) + np.abs(c[:nv]) @ np.abs(Vn)
+    # one FP32 rounding per row of the FMA chains (and of the coefficients)
+    assert np.all(np.abs(wd.cpu().numpy() - ws) <= (nv + 2) * 1.2e-7 * scale)
+    assert abs(out[0].item() - np.linalg.norm(ws)) <= (nv + 2) * 1.2e-7 * np.linalg.norm(scale)
+    assert int(ctx.cnt.abs().sum().item()) == 0
+
+
+def test_lanczos_fp32_basis_matches_eigvalsh():
+    """The FP32-basis Lanczos (tensor-core stage of the mixed solve) reaches FP32-level accuracy
+    and restarts like the FP64 one."""
+    from tnkit_gb300.lanczos import lanczos_ground_restart
+    rng = np.random.default_rng(8)
+    n = 600
+    A = rng.standard_normal((n, n))
+    A = (A + A.T) / 2
+    H32 = torch.as_tensor(A, dtype=torch.float32, device="cuda")
+    v0 = torch.as_tensor(rng.standard_normal(n), device="cuda")
+    mv = lambda v, out: torch.mv(H32, v, out=out)
+    e, x, info = lanczos_ground_restart(mv, v0, tol=1e-4, max_iter=600, m=30, k=8,
+                                        dtype=torch.float32)
+    ev, evec = np.linalg.eigh(A)
+    assert x.dtype == torch.float32 and info["converged"] and info["restarts"] > 0
+    assert abs(e - ev[0]) <= 1e-5 * abs(ev[0])
+    assert abs(abs(float(np.dot(x.double().cpu().numpy(), evec[:, 0]))) - 1.0) <= 1e-4

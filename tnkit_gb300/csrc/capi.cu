@@ -24,6 +24,9 @@ int vec_axpby(const double*, double*, int64_t, const double*, double, const doub
 int vec_scale_div(const double*, double*, int64_t, const double*, double, cudaStream_t);
 int vec_cgs_pass(const double*, int64_t, int, const double*, double*, int64_t, double*, int,
                  double*, unsigned*, cudaStream_t);
+int vec_cgs_pass_f32(const float*, int64_t, int, const double*, float*, int64_t, double*, int,
+                     double*, unsigned*, cudaStream_t);
+int vec_scale_div_f32(const float*, float*, int64_t, const double*, double, cudaStream_t);
 
 // The three stages of a plan3 on the operand slots (x0, x1, x2, ws).
 static int run_plan3(const tnk_plan3* p, const double* x0, const double* x1, const double* x2,
@@ -157,6 +160,18 @@ int tnk_cgs_pass_f64(const double* V, int64_t ldv, int32_t nv, const double* cin
                      int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
                      void* stream) {
     return vec_cgs_pass(V, ldv, nv, cin, w, n, out, mode, red, counter, (cudaStream_t)stream);
+}
+
+int tnk_cgs_pass_f32(const float* V, int64_t ldv, int32_t nv, const double* cin, float* w,
+                     int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
+                     void* stream) {
+    return vec_cgs_pass_f32(V, ldv, nv, cin, w, n, out, mode, red, counter,
+                            (cudaStream_t)stream);
+}
+
+int tnk_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,
+                      void* stream) {
+    return vec_scale_div_f32(x, y, n, s, f, (cudaStream_t)stream);
 }
 
 int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,

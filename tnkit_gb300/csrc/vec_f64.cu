@@ -94,13 +94,14 @@ constexpr int CG_NT = CG_TK;
 constexpr int CG_RING_BYTES = 48 * 1024;
 constexpr int CG_MAX_STAGES = 8;
 
-__host__ __device__ inline int cg_stages(int nv) {
-    int s = CG_RING_BYTES / ((nv + 1) * CG_TK * (int)sizeof(double));
+// ring stages and bytes for nv rows of `es`-byte elements
+__host__ __device__ inline int cg_stages(int nv, int es) {
+    int s = CG_RING_BYTES / ((nv + 1) * CG_TK * es);
     return s < 2 ? 2 : (s > CG_MAX_STAGES ? CG_MAX_STAGES : s);
 }
 
-__host__ __device__ inline int cg_ring_bytes(int nv) {
-    return cg_stages(nv) * (nv + 1) * CG_TK * (int)sizeof(double);
+__host__ __device__ inline int cg_ring_bytes(int nv, int es) {
+    return cg_stages(nv, es) * (nv + 1) * CG_TK * es;
 }
 
 // partial rows of one CTA, rounded up to an even count (16-byte copies)
@@ -109,10 +110,17 @@ __host__ __device__ inline int cg_prow(int mode, int nv) {
     return (r + 1) & ~1;
 }
 
-__device__ __forceinline__ void cp_async8(double* dst, const double* src, bool valid) {
+__device__ __forceinline__ void cp_async_elem(double* dst, const double* src, bool valid) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src),
                  "r"(valid ? 8 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_elem(float* dst, const float* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src),
+                 "r"(valid ? 4 : 0)
                  : "memory");
 }
 
@@ -140,47 +148,58 @@ __device__ __forceinline__ void cp_async_wait_dyn(int pending) {
 }
 
 // Sum the partials of `nb` CTAs (prow doubles each, the first `nrow` used) into out[0..nrow),
-// square-rooted when `root`. Runs in one whole CTA of CG_NT threads; `stage` holds nb * prow
-// doubles. Each row is split among CG_NT / nrow threads (strided CTA subsets), whose sums are
-// then added in a fixed order: the result does not depend on timing.
+// square-rooted when `root`. Runs in one whole CTA of CG_NT threads. The partials pass through
+// `stage` (stage_elems doubles) in chunks of CTAs, each chunk copied in one batch; each row is
+// split among CG_NT / nrow threads (strided CTA subsets, summed in increasing CTA order), whose
+// sums are then added in a fixed order: the result does not depend on timing.
 __device__ void finish_partials(const double* red, int nb, int prow, int nrow, bool root,
-                                double* stage, double* out) {
+                                double* stage, int stage_elems, double* out) {
     __shared__ double part[CG_NT];
     const int half = prow / 2;
-    for (int e = threadIdx.x; e < nb * half; e += blockDim.x) {
-        const int b = e / half, h = e - b * half;
-        cp_async16_cg(stage + (int64_t)b * prow + 2 * h, red + (int64_t)b * PSTRIDE + 2 * h);
-    }
-    cp_async_commit();
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    __syncthreads();
     const int G = nrow > 0 ? CG_NT / nrow : 1;       // threads per row (nrow <= 64)
     const int idx = threadIdx.x;
-    if (idx < nrow * G) {
-        const int r = idx / G, g = idx - r * G;
-        double s = 0.0;
-        for (int b = g; b < nb; b += G) s += stage[(int64_t)b * prow + r];
-        part[idx] = s;
+    const int r = idx / G, g = idx - r * G;
+    const bool active = idx < nrow * G;
+    const int cap = stage_elems / prow > 0 ? stage_elems / prow : 1;
+    double s = 0.0;
+    for (int b0 = 0; b0 < nb; b0 += cap) {
+        const int b1 = nb - b0 < cap ? nb : b0 + cap;
+        __syncthreads();                              // the previous chunk has been read
+        for (int e = idx; e < (b1 - b0) * half; e += blockDim.x) {
+            const int b = e / half, h = e - b * half;
+            cp_async16_cg(stage + (int64_t)b * prow + 2 * h,
+                          red + (int64_t)(b0 + b) * PSTRIDE + 2 * h);
+        }
+        cp_async_commit();
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        if (active) {
+            int b = b0 + ((g - b0 % G) % G + G) % G;  // first b >= b0 with b = g (mod G)
+            for (; b < b1; b += G) s += stage[(int64_t)(b - b0) * prow + r];
+        }
     }
+    if (active) part[idx] = s;
     __syncthreads();
     if (idx < nrow) {
-        double s = 0.0;
-        for (int g = 0; g < G; ++g) s += part[idx * G + g];
-        out[idx] = root ? sqrt(s) : s;
+        double t = 0.0;
+        for (int q = 0; q < G; ++q) t += part[idx * G + q];
+        out[idx] = root ? sqrt(t) : t;
     }
 }
+
+constexpr int CG_FIN_ELEMS = 4096;                   // staging of finish_kernel (32 KB)
 
 __global__ void __launch_bounds__(CG_NT) finish_kernel(const double* __restrict__ red, int nb,
                                                       int prow, int nrow, int root,
                                                       double* __restrict__ out) {
-    extern __shared__ __align__(16) double fin[];
-    finish_partials(red, nb, prow, nrow, root != 0, fin, out);
+    __shared__ __align__(16) double fin[CG_FIN_ELEMS];
+    finish_partials(red, nb, prow, nrow, root != 0, fin, CG_FIN_ELEMS, out);
 }
 
-template <int NVB, int MODE>
-__global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V, int64_t ldv,
-                                                   int nv, const double* __restrict__ cin,
-                                                   double* __restrict__ w, int64_t n,
+template <typename T, int NVB, int MODE>
+__global__ void __launch_bounds__(CG_NT) cgs_kernel(const T* __restrict__ V, int64_t ldv, int nv,
+                                                   const double* __restrict__ cin,
+                                                   T* __restrict__ w, int64_t n,
                                                    double* __restrict__ red,
                                                    unsigned* __restrict__ counter,
                                                    double* __restrict__ out) {
@@ -188,14 +207,15 @@ __global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V
     constexpr bool DOT = (MODE & CG_DOT) != 0;
     constexpr bool NRM = (MODE & CG_NRM) != 0;
     constexpr int NACC = DOT ? NVB : 1;
-    extern __shared__ __align__(16) double ring[];   // [stage][row 0: w, rows 1..nv: V][CG_TK]
-    __shared__ double cs[NVB];
+    extern __shared__ __align__(16) unsigned char ring_raw[];
+    T* ring = reinterpret_cast<T*>(ring_raw);        // [stage][row 0: w, rows 1..nv: V][CG_TK]
+    __shared__ T cs[NVB];
     __shared__ double sh[CG_NT / 32][NVB + 1];
     __shared__ bool last;
     const int t = threadIdx.x;
     const int rows = nv + 1;
-    const int stages = cg_stages(nv);
-    if (SUB && t < NVB) cs[t] = t < nv ? -cin[t] : 0.0;
+    const int stages = cg_stages(nv, (int)sizeof(T));
+    if (SUB && t < NVB) cs[t] = t < nv ? (T)(-cin[t]) : (T)0;
     __syncthreads();
     const int64_t ntiles = (n + CG_TK - 1) / CG_TK;
 
@@ -204,29 +224,29 @@ __global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V
             const int64_t k = tile * CG_TK + t;
             const bool ok = k < n;
             const int64_t kk = ok ? k : 0;
-            double* st = ring + (int64_t)slot * rows * CG_TK + t;
-            cp_async8(st, w + kk, ok);
+            T* st = ring + (int64_t)slot * rows * CG_TK + t;
+            cp_async_elem(st, w + kk, ok);
             for (int i = 0; i < nv; ++i)
-                cp_async8(st + (i + 1) * CG_TK, V + (int64_t)i * ldv + kk, ok);
+                cp_async_elem(st + (i + 1) * CG_TK, V + (int64_t)i * ldv + kk, ok);
         }
         cp_async_commit();
     };
 
-    double acc[NACC];
+    T acc[NACC];
 #pragma unroll
-    for (int i = 0; i < NACC; ++i) acc[i] = 0.0;
-    double accn = 0.0;
+    for (int i = 0; i < NACC; ++i) acc[i] = (T)0;
+    T accn = (T)0;
     int64_t tile = blockIdx.x;
     for (int s = 0; s < stages - 1; ++s) issue(tile + (int64_t)s * gridDim.x, s);
     int slot = 0;
     for (; tile < ntiles; tile += gridDim.x) {
         cp_async_wait_dyn(stages - 2);
         issue(tile + (int64_t)(stages - 1) * gridDim.x, slot == 0 ? stages - 1 : slot - 1);
-        const double* st = ring + (int64_t)slot * rows * CG_TK + t;
+        const T* st = ring + (int64_t)slot * rows * CG_TK + t;
         const int64_t k = tile * CG_TK + t;
-        double wk = st[0];
+        T wk = st[0];
         if (SUB) {
-            double s1 = 0.0;
+            T s1 = (T)0;
             int i = 0;
             for (; i + 1 < nv; i += 2) {
                 wk = fma(cs[i], st[(i + 1) * CG_TK], wk);
@@ -251,12 +271,12 @@ __global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V
 #pragma unroll
         for (int j = 0; j < NACC; ++j) {
             if (j >= nv) break;
-            const double s = warp_sum(acc[j]);
+            const double s = warp_sum((double)acc[j]);
             if (lane == 0) sh[wid][j] = s;
         }
     }
     if (NRM) {
-        const double s = warp_sum(accn);
+        const double s = warp_sum((double)accn);
         if (lane == 0) sh[wid][0] = s;
     }
     __syncthreads();
@@ -274,15 +294,17 @@ __global__ void __launch_bounds__(CG_NT) cgs_kernel(const double* __restrict__ V
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // the ring is idle now; the grid cap keeps gridDim.x * prow doubles within it
-    finish_partials(red, gridDim.x, cg_prow(MODE, nv), nrow, NRM, ring, out);
+    // the ring is idle now: it stages the partials
+    finish_partials(red, gridDim.x, cg_prow(MODE, nv), nrow, NRM,
+                    reinterpret_cast<double*>(ring_raw),
+                    stages * rows * CG_TK * (int)sizeof(T) / (int)sizeof(double), out);
     if (t == 0) *counter = 0u;
 }
 
-// Grid size: one CTA per tile, at most the resident CTAs of all SMs, and few enough that the
-// partials fit the ring (for the in-launch sum) and TNK_RED_ELEMS.
-template <int NVB, int MODE>
+// Grid size: one CTA per tile, at most the resident CTAs of all SMs and TNK_RED_ELEMS / PSTRIDE.
+template <typename T, int NVB, int MODE>
 int cgs_grid(int64_t n, int nv) {
+    constexpr int ES = (int)sizeof(T);
     // per device: the opt-in to the largest ring; per row count: the resident CTAs per SM
     static std::atomic<unsigned long long> opted{0};
     static std::atomic<int> nsm{0};
@@ -292,11 +314,10 @@ int cgs_grid(int64_t n, int nv) {
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(opted.load(std::memory_order_acquire) & bit)) {
         int big = 0;
-        for (int v = 0; v <= NVB; ++v) big = cg_ring_bytes(v) > big ? cg_ring_bytes(v) : big;
-        cudaFuncSetAttribute(cgs_kernel<NVB, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             big);
-        cudaFuncSetAttribute(finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             cg_ring_bytes(MAXNV));
+        for (int v = 0; v <= NVB; ++v)
+            big = cg_ring_bytes(v, ES) > big ? cg_ring_bytes(v, ES) : big;
+        cudaFuncSetAttribute(cgs_kernel<T, NVB, MODE>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, big);
         int cnt = 0;
         if (cudaDeviceGetAttribute(&cnt, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cnt < 1)
@@ -306,42 +327,40 @@ int cgs_grid(int64_t n, int nv) {
     }
     int occ = occ_of[nv].load(std::memory_order_relaxed);
     if (occ < 1) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cgs_kernel<NVB, MODE>, CG_NT,
-                                                          cg_ring_bytes(nv)) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cgs_kernel<T, NVB, MODE>, CG_NT,
+                                                          cg_ring_bytes(nv, ES)) !=
+                cudaSuccess ||
             occ < 1)
             occ = 1;
         occ_of[nv].store(occ, std::memory_order_relaxed);
     }
     int64_t cap = (int64_t)occ * nsm.load(std::memory_order_relaxed);
-    const int64_t fit = cg_ring_bytes(nv) / (cg_prow(MODE, nv) * (int)sizeof(double));
-    if (cap > fit) cap = fit;
     if (cap > TNK_RED_ELEMS / PSTRIDE) cap = TNK_RED_ELEMS / PSTRIDE;
     int64_t g = (n + CG_TK - 1) / CG_TK;
     if (g > cap) g = cap;
     return g < 1 ? 1 : (int)g;
 }
 
-template <int NVB, int MODE>
-int launch_cgs_t(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+template <typename T, int NVB, int MODE>
+int launch_cgs_t(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64_t n,
                  double* red, unsigned* counter, double* out, cudaStream_t st) {
-    const int g = cgs_grid<NVB, MODE>(n, nv);
-    cgs_kernel<NVB, MODE><<<g, CG_NT, cg_ring_bytes(nv), st>>>(V, ldv, nv, cin, w, n, red,
-                                                               counter, out);
+    const int g = cgs_grid<T, NVB, MODE>(n, nv);
+    cgs_kernel<T, NVB, MODE><<<g, CG_NT, cg_ring_bytes(nv, (int)sizeof(T)), st>>>(
+        V, ldv, nv, cin, w, n, red, counter, out);
     int rc = check_launch("cgs_kernel");
     if (rc || counter || !(MODE & (CG_DOT | CG_NRM))) return rc;
-    const int prow = cg_prow(MODE, nv);
-    finish_kernel<<<1, CG_NT, g * prow * (int)sizeof(double), st>>>(
-        red, g, prow, (MODE & CG_DOT) ? nv : 1, (MODE & CG_NRM) ? 1 : 0, out);
+    finish_kernel<<<1, CG_NT, 0, st>>>(red, g, cg_prow(MODE, nv), (MODE & CG_DOT) ? nv : 1,
+                                       (MODE & CG_NRM) ? 1 : 0, out);
     return check_launch("finish_kernel");
 }
 
 // One launch of a fixed mode over nv <= 64 rows (NVB, the accumulator count, picked from nv).
-template <int MODE>
-int launch_cgs(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+template <int MODE, typename T>
+int launch_cgs(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64_t n,
                double* red, unsigned* counter, double* out, cudaStream_t st) {
-    if (nv <= 16) return launch_cgs_t<16, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
-    if (nv <= 32) return launch_cgs_t<32, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
-    return launch_cgs_t<64, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    if (nv <= 16) return launch_cgs_t<T, 16, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    if (nv <= 32) return launch_cgs_t<T, 32, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+    return launch_cgs_t<T, 64, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
 }
 
 __global__ void __launch_bounds__(NT) axpby_kernel(const double* __restrict__ x,
@@ -352,6 +371,14 @@ __global__ void __launch_bounds__(NT) axpby_kernel(const double* __restrict__ x,
     const double b = (sb ? sb[0] : 1.0) * fb;
     for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n; k += (int64_t)gridDim.x * NT)
         y[k] = (b == 0.0) ? a * x[k] : fma(a, x[k], b * y[k]);
+}
+
+__global__ void __launch_bounds__(NT) scale_div_f32_kernel(const float* __restrict__ x,
+                                                           float* __restrict__ y, int64_t n,
+                                                           const double* s, double f) {
+    const float a = (float)(f / s[0]);
+    for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n; k += (int64_t)gridDim.x * NT)
+        y[k] = x[k] * a;
 }
 
 __global__ void __launch_bounds__(NT) scale_div_kernel(const double* __restrict__ x,
@@ -387,8 +414,8 @@ int vec_multidot(const double* V, int64_t ldv, int nv, const double* w, int64_t 
         return TNK_ERR_ARG;
     }
     if (nv == 0) return TNK_OK;
-    return launch_cgs<CG_DOT>(V, ldv, nv, nullptr, const_cast<double*>(w), n, red, nullptr, c,
-                              stream);
+    return launch_cgs<CG_DOT, double>(V, ldv, nv, nullptr, const_cast<double*>(w), n, red,
+                                      nullptr, c, stream);
 }
 
 int vec_gemv_sub(const double* V, int64_t ldv, int nv, const double* c, double* w, int64_t n,
@@ -401,8 +428,9 @@ int vec_gemv_sub(const double* V, int64_t ldv, int nv, const double* c, double* 
     return launch_cgs<CG_SUB>(V, ldv, nv, c, w, n, nullptr, nullptr, nullptr, stream);
 }
 
-int vec_cgs_pass(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
-                 double* out, int mode, double* red, unsigned* counter, cudaStream_t st) {
+template <typename T>
+int cgs_pass_t(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64_t n, double* out,
+               int mode, double* red, unsigned* counter, cudaStream_t st) {
     const bool sub = mode & CG_SUB, dot = mode & CG_DOT, nrm = mode & CG_NRM;
     if (n < 0 || nv < 0 || nv > MAXNV || mode < 1 || mode > 7 || (dot && nrm) ||
         (n > 0 && !w) || ((sub || dot) && (ldv < n || (n > 0 && nv > 0 && !V))) ||
@@ -427,6 +455,17 @@ int vec_cgs_pass(const double* V, int64_t ldv, int nv, const double* cin, double
     }
 }
 
+int vec_cgs_pass(const double* V, int64_t ldv, int nv, const double* cin, double* w, int64_t n,
+                 double* out, int mode, double* red, unsigned* counter, cudaStream_t st) {
+    return cgs_pass_t<double>(V, ldv, nv, cin, w, n, out, mode, red, counter, st);
+}
+
+int vec_cgs_pass_f32(const float* V, int64_t ldv, int nv, const double* cin, float* w,
+                     int64_t n, double* out, int mode, double* red, unsigned* counter,
+                     cudaStream_t st) {
+    return cgs_pass_t<float>(V, ldv, nv, cin, w, n, out, mode, red, counter, st);
+}
+
 int vec_axpby(const double* x, double* y, int64_t n, const double* sa, double fa,
               const double* sb, double fb, cudaStream_t stream) {
     if (!x || !y || n < 0) {
@@ -447,6 +486,17 @@ int vec_scale_div(const double* x, double* y, int64_t n, const double* s, double
     if (n == 0) return TNK_OK;
     scale_div_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(x, y, n, s, f);
     return check_launch("scale_div_kernel");
+}
+
+int vec_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,
+                      cudaStream_t stream) {
+    if (!x || !y || !s || n < 0) {
+        set_error("scale_div_f32: bad argument");
+        return TNK_ERR_ARG;
+    }
+    if (n == 0) return TNK_OK;
+    scale_div_f32_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(x, y, n, s, f);
+    return check_launch("scale_div_f32_kernel");
 }
 
 }  // namespace tnk

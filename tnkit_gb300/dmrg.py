@@ -56,6 +56,8 @@ class DMRGOptions:
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
     svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
+    env_precision: str = "f64"            # 'f64' or 'ff': environment updates in float-float
+                                          # (~2x faster; ~10x larger energy error, ~1e-13)
 
 
 def _resolve(options, kw) -> DMRGOptions:
@@ -151,6 +153,9 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     for i in range(N - 1, 0, -1):
         R[i] = ops.update_right_env(R[i + 1], M[i], W[i])
 
+    if o.env_precision not in ("f64", "ff"):
+        raise ValueError("env_precision must be 'f64' or 'ff'")
+    env_prec = o.env_precision
     energies, sweep_s, alphas = [], [], []
     phase = {"eig": 0.0, "trunc": 0.0, "env": 0.0}
     counts = {"lo": 0, "hi": 0}
@@ -203,9 +208,9 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         phase["trunc"] += time.perf_counter() - t0
         t0 = time.perf_counter()
         if right:
-            L[i + 1] = ops.update_left_env(L[i], M[i], W[i])
+            L[i + 1] = ops.update_left_env(L[i], M[i], W[i], precision=env_prec)
         else:
-            R[i + 1] = ops.update_right_env(R[i + 2], M[i + 1], W[i + 1])
+            R[i + 1] = ops.update_right_env(R[i + 2], M[i + 1], W[i + 1], precision=env_prec)
         sync()
         phase["env"] += time.perf_counter() - t0
         return e

@@ -21,7 +21,6 @@ arrowhead projected matrix) are the reference's.
 """
 from __future__ import annotations
 
-import ctypes as C
 from typing import Callable, Optional
 
 import numpy as np
@@ -41,7 +40,8 @@ class _Dev:
     """Device scratch of one solve: reduction workspace and completion counter, scalar slots,
     two iteration records (device and pinned host, alternating) with their events."""
 
-    def __init__(self, device):
+    def __init__(self, device, dtype=torch.float64):
+        self.f32 = dtype == torch.float32
         self.red = torch.empty(_lib.TNK_RED_ELEMS, dtype=torch.float64, device=device)
         self.cnt = torch.zeros(4, dtype=torch.int32, device=device)
         self.sc = torch.zeros(8 + _MAXNV, dtype=torch.float64, device=device)
@@ -59,27 +59,28 @@ class _Dev:
         return self.rec.data_ptr() + 8 * (par * _REC + i)
 
     def nrm2(self, x, slot):
+        if x.dtype == torch.float32:
+            _lib.check(self.lib.tnk_cgs_pass_f32(None, x.numel(), 0, None, x.data_ptr(),
+                                                 x.numel(), self.addr(slot), _NRM,
+                                                 self.red.data_ptr(), self.cnt.data_ptr(),
+                                                 self.sp), "nrm2")
+            return
         _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.addr(slot),
                                          self.red.data_ptr(), self.sp), "nrm2")
 
-    def axpby(self, x, y, fa, fb, sa=None, sb=None):
-        _lib.check(self.lib.tnk_axpby_f64(x.data_ptr(), y.data_ptr(), x.numel(),
-                                          None if sa is None else self.addr(sa), fa,
-                                          None if sb is None else self.addr(sb), fb, self.sp),
-                   "axpby")
-
     def scale_div(self, x, y, s_addr, f=1.0):
-        _lib.check(self.lib.tnk_scale_div_f64(x.data_ptr(), y.data_ptr(), x.numel(), s_addr, f,
-                                              self.sp), "scale_div")
+        fn = self.lib.tnk_scale_div_f32 if x.dtype == torch.float32 else \
+            self.lib.tnk_scale_div_f64
+        _lib.check(fn(x.data_ptr(), y.data_ptr(), x.numel(), s_addr, f, self.sp), "scale_div")
 
     def cgs(self, V, nv, cin, w, out, mode):
-        _lib.check(self.lib.tnk_cgs_pass_f64(V.data_ptr(), V.stride(0), nv, cin, w.data_ptr(),
-                                             w.numel(), out, mode, self.red.data_ptr(),
-                                             self.cnt.data_ptr(), self.sp), "cgs_pass")
+        fn = self.lib.tnk_cgs_pass_f32 if self.f32 else self.lib.tnk_cgs_pass_f64
+        _lib.check(fn(V.data_ptr(), V.stride(0), nv, cin, w.data_ptr(), w.numel(), out, mode,
+                      self.red.data_ptr(), self.cnt.data_ptr(), self.sp), "cgs_pass")
 
     def gemv_sub(self, V, nv, w):
-        _lib.check(self.lib.tnk_gemv_sub_f64(V.data_ptr(), V.stride(0), nv, self.addr(8),
-                                             w.data_ptr(), w.numel(), self.sp), "gemv_sub")
+        """w -= V[:nv]^T c with c in the coefficient slots (set_coeffs)."""
+        self.cgs(V, nv, self.addr(8), w, None, _SUB)
 
     def set_coeffs(self, c: np.ndarray):
         self.sc[8:8 + len(c)].copy_(torch.as_tensor(np.ascontiguousarray(c, np.float64)))
@@ -113,9 +114,14 @@ class _Dev:
         return float(h[1 + j]), float(h[0])
 
     def rotate(self, Y: np.ndarray, V: torch.Tensor, out: torch.Tensor):
-        """out (kk x n) = Y^T (kk x cur) @ V[:cur] as one grouped-GEMM launch."""
+        """out (kk x n) = Y^T (kk x cur) @ V[:cur] as one grouped-GEMM launch (FP64), or one
+        library GEMM for an FP32 basis."""
         cur, kk = Y.shape
         n = V.shape[1]
+        if V.dtype == torch.float32:
+            A = torch.as_tensor(np.ascontiguousarray(Y.T), dtype=torch.float32, device=V.device)
+            torch.mm(A, V, out=out)
+            return (A,)
         A = torch.as_tensor(np.ascontiguousarray(Y.T), dtype=torch.float64, device=V.device)
         task = np.array([(0, n, kk, n, 0, 1, 0)], dtype=GEMM_TASK)
         seg = np.array([(0, 0, cur, 1, V.stride(0), 1, cur, 0, 1, 0, 0, 1.0)], dtype=GEMM_SEG)
@@ -151,31 +157,42 @@ def _lowest(T: np.ndarray, cur: int, tridiagonal: bool):
 def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8,
                            max_iter: int = 200, m: int = 40, k: int = 10,
                            basis: Optional[torch.Tensor] = None, stall: int = 0,
-                           speculate: bool = True):
+                           speculate: bool = True, dtype=torch.float64):
     """Lowest eigenpair of the operator `matvec(x, out) -> out` from the start `v0` (float64
     CUDA vector). Returns (theta, x, info) like the reference; x is normalised.
 
     stall > 0 also stops when the Ritz residual has improved by less than 10 % over the last
     `stall` iterations (info["stalled"]): the floor of a low-precision operator.
-    speculate=False waits for every iteration before queuing the next (no discarded matvec)."""
+    speculate=False waits for every iteration before queuing the next (no discarded matvec).
+    dtype=torch.float32 keeps the Krylov basis, the operator's vectors and x in FP32 (for an
+    operator that is itself only FP32-accurate); the scalars stay FP64."""
     if k >= m:
         k = max(1, m // 2)
     if m + 1 > _MAXNV:
         raise ValueError(f"restart window m={m} exceeds {_MAXNV - 1}")
     if max_iter < 1:
         raise ValueError("max_iter must be >= 1")
+    if dtype not in (torch.float64, torch.float32):
+        raise ValueError("dtype must be torch.float64 or torch.float32")
     dev = v0.device
-    D = _Dev(dev)
+    D = _Dev(dev, dtype)
     n = v0.numel()
     v0 = v0.reshape(-1)
     D.nrm2(v0, 2)
     n0 = D.read_slot(2)
     if not np.isfinite(n0) or n0 < 1e-300:
-        return 0.0, v0, {"iters": 0, "converged": False, "restarts": 0, "matvecs": 0}
+        return 0.0, v0.to(dtype), {"iters": 0, "converged": False, "restarts": 0, "matvecs": 0}
+    if basis is not None and basis.dtype != dtype:
+        flat = basis.reshape(-1).view(dtype)         # the same storage, reinterpreted
+        basis = flat[:(m + 1) * n].view(m + 1, n) if flat.numel() >= (m + 1) * n else None
     Vb = basis if (basis is not None and basis.shape[0] >= m + 1 and basis.shape[1] == n) \
-        else torch.empty((m + 1, n), dtype=torch.float64, device=dev)
-    D.scale_div(v0, Vb[0], D.addr(2))
-    w = torch.empty(n, dtype=torch.float64, device=dev)
+        else torch.empty((m + 1, n), dtype=dtype, device=dev)
+    if dtype == torch.float64:
+        D.scale_div(v0, Vb[0], D.addr(2))
+    else:
+        Vb[0].copy_(v0)
+        D.scale_div(Vb[0], Vb[0], D.addr(2))
+    w = torch.empty(n, dtype=dtype, device=dev)
     T = np.zeros((m + 1, m + 1))
     n_kept = 0
     theta, y = 0.0, np.array([1.0])
@@ -222,9 +239,9 @@ def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8
             ev, evec = np.linalg.eigh(T[:cur, :cur])
             kk = min(k, cur - 1)
             Yk = evec[:, :kk]
-            tmp = torch.empty((kk, n), dtype=torch.float64, device=dev)
+            tmp = torch.empty((kk, n), dtype=dtype, device=dev)
             keep = D.rotate(Yk, Vb[:cur], tmp)
-            D.axpby(tmp.reshape(-1), Vb[:kk].reshape(-1), 1.0, 0.0)
+            Vb[:kk].copy_(tmp)
             T[:] = 0.0
             border = beta * np.asarray(Yk[cur - 1, :], dtype=np.float64)
             for i in range(kk):
@@ -242,7 +259,7 @@ def lanczos_ground_restart(matvec: Callable, v0: torch.Tensor, tol: float = 1e-8
             pending.append((j + 1, D.issue(matvec, Vb, w, j + 1, issued, scale=True)))
             issued += 1
     ny = len(y)
-    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    x = torch.zeros(n, dtype=dtype, device=dev)
     D.set_coeffs(-np.asarray(y[:ny], np.float64))
     D.gemv_sub(Vb, ny, x)
     D.nrm2(x, 3)

@@ -2,9 +2,11 @@
 
 The two-site H_eff is applied on the tcgen05 tensor cores (TF32 inputs, FP32 accumulation in
 TMEM; by default each operand split into TF32 hi/lo parts, three MMAs per product, ~1e-6
-relative), with FP64 vectors in and out. Lanczos itself -- reorthogonalisation, the projected
-eigenproblem, norms and dot products -- stays FP64, as in the reference's
-`lanczos_ground_mixed` (tnkit/eigensolver.py:677-725): stage 1 converges the Ritz residual with
+relative). The tensor-core stage keeps its Krylov basis in FP32 -- the operator is no more
+accurate than that, and FP32 Gram-Schmidt runs on the FP32 pipes at half the bytes -- with the
+projected eigenproblem, norms and dot products accumulated in FP64; the polish stage is the FP64
+(or float-float) Lanczos, as in the reference's `lanczos_ground_mixed`
+(tnkit/eigensolver.py:677-725): stage 1 converges the Ritz residual with
 the cheap matvec to `tol_lo` (or until the residual stops improving, the floor the TF32 operator
 allows), stage 2 restarts FP64 Lanczos from that vector to `tol` (at most `polish` iterations
 when given). The reference refuses this mode on block tensors (tnkit/_dmrg.py:531-532); here it
@@ -87,6 +89,26 @@ class TwoSiteOperatorTC:
                                 f"a bounded wait timed out (code {e}); results are invalid")
 
 
+class _F32Vectors:
+    """An operator on FP64 vectors applied to FP32 vectors (conversions on the device around
+    it), for the FP32 Krylov basis of the tensor-core stage."""
+
+    def __init__(self, op, n: int, device):
+        self.op = op
+        self.xd = torch.empty(n, dtype=torch.float64, device=device)
+        self.yd = torch.empty(n, dtype=torch.float64, device=device)
+
+    @property
+    def calls(self):
+        return self.op.calls
+
+    def __call__(self, x: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+        self.xd.copy_(x)
+        self.op(self.xd, self.yd)
+        out.copy_(self.yd)
+        return out
+
+
 def _fp64_residual(op64, v: torch.Tensor):
     """(rayleigh quotient, residual norm) of v in FP64: one FP64 matvec."""
     w = op64(v)
@@ -120,11 +142,12 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
     else:
         if r0 >= switch * tol_lo:
             op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
-            e_lo, x, info_lo = lanczos_ground_restart(op_lo, v0, tol=max(tol_lo, tol),
-                                                      max_iter=max_iter, m=m, k=k, basis=basis,
-                                                      stall=8)
+            e_lo, x32, info_lo = lanczos_ground_restart(
+                _F32Vectors(op_lo, v0.numel(), v0.device), v0, tol=max(tol_lo, tol),
+                max_iter=max_iter, m=m, k=k, basis=basis, stall=8, dtype=torch.float32)
             op_lo.check_device_error()
             n_lo = op_lo.calls
+            x = x32.double()
         e, x, info_hi = lanczos_ground_restart(op64, x, tol=tol,
                                                max_iter=max_iter if polish is None else polish,
                                                m=m, k=k, basis=basis)

@@ -210,18 +210,37 @@ def plan_one_site(M: Layout, L: BlockTensor, W: BlockTensor, R: BlockTensor,
         (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
 
 
-def plan_left(L: Layout, A: Layout, W: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+def plan_left(L: Layout, A: Layout, W: BlockTensor, device, cplx: bool = False,
+              ff: bool = False) -> DevicePlan3:
     key = ("left", L, A, _mpo_key(W))
     host = lambda: P.plan_left_env(L, A, (W.layout, _host_of(W)))
-    return _PLANS.get_or(key + (str(device), cplx), lambda: DevicePlan3(
-        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
+    return _PLANS.get_or(key + (str(device), cplx, ff), lambda: DevicePlan3(
+        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device, ff=ff))
 
 
-def plan_right(R: Layout, B: Layout, W: BlockTensor, device, cplx: bool = False) -> DevicePlan3:
+def plan_right(R: Layout, B: Layout, W: BlockTensor, device, cplx: bool = False,
+               ff: bool = False) -> DevicePlan3:
     key = ("right", R, B, _mpo_key(W))
     host = lambda: P.plan_right_env(R, B, (W.layout, _host_of(W)))
-    return _PLANS.get_or(key + (str(device), cplx), lambda: DevicePlan3(
-        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device))
+    return _PLANS.get_or(key + (str(device), cplx, ff), lambda: DevicePlan3(
+        (_cplx if cplx else (lambda h: h))(_real_plan(key, host)), device, ff=ff))
+
+
+def _env_ff(p: DevicePlan3, site: torch.Tensor, env: torch.Tensor, y: torch.Tensor):
+    """An environment update in float-float arithmetic: the site tensor and the old environment
+    split once into (hi, lo) pairs after the plan's workspace, then tnk_contract3_ff (slots:
+    site, env, site)."""
+    ns, ne = site.numel(), env.numel()
+    need = p.ws_elems
+    ws = workspace(need + ns + ne, y.device)
+    lib, sp = _lib.lib(), _lib.stream_ptr()
+    s2 = ws.data_ptr() + 8 * need
+    e2 = s2 + 8 * ns
+    _lib.check(lib.tnk_ff_split(site.data_ptr(), s2, ns, sp), "ff split")
+    _lib.check(lib.tnk_ff_split(env.data_ptr(), e2, ne, sp), "ff split")
+    _lib.check(lib.tnk_contract3_ff(C.byref(p.c), s2, e2, s2, y.data_ptr(), ws.data_ptr(), need,
+                                    sp), "tnk_contract3_ff")
+    return y
 
 
 def plan_tdot(a: Layout, b: Layout, nc: int, device, cplx: bool = False) -> DeviceGemmPlan:
@@ -264,19 +283,32 @@ def apply_one_site(M: BlockTensor, L: BlockTensor, W: BlockTensor, R: BlockTenso
     return BlockTensor(p.out_layout, y)
 
 
-def update_left_env(L: BlockTensor, A: BlockTensor, W: BlockTensor) -> BlockTensor:
+def update_left_env(L: BlockTensor, A: BlockTensor, W: BlockTensor,
+                    precision: str = "f64") -> BlockTensor:
+    """L' = A^* L W A (tnkit/_dmrg.py:216-223); precision 'ff' runs it in float-float on real
+    tensors (the FP32 CUDA cores, ~1e-14 relative)."""
     c = _require_cuda(L.data, A.data)
-    p = plan_left(L.layout, A.layout, W, A.data.device, c)
+    ff = precision == "ff" and not c
+    p = plan_left(L.layout, A.layout, W, A.data.device, c, ff=ff)
     y = _out(p, A.data)
-    p.run("tnk_update_left_env_f64", A.data, L.data, A.data, y, None)
+    if ff:
+        _env_ff(p, A.data, L.data, y)
+    else:
+        p.run("tnk_update_left_env_f64", A.data, L.data, A.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
-def update_right_env(R: BlockTensor, B: BlockTensor, W: BlockTensor) -> BlockTensor:
+def update_right_env(R: BlockTensor, B: BlockTensor, W: BlockTensor,
+                     precision: str = "f64") -> BlockTensor:
+    """R' = B R W B^* (tnkit/_dmrg.py:224-231); precision 'ff' as in update_left_env."""
     c = _require_cuda(R.data, B.data)
-    p = plan_right(R.layout, B.layout, W, B.data.device, c)
+    ff = precision == "ff" and not c
+    p = plan_right(R.layout, B.layout, W, B.data.device, c, ff=ff)
     y = _out(p, B.data)
-    p.run("tnk_update_right_env_f64", B.data, R.data, B.data, y, None)
+    if ff:
+        _env_ff(p, B.data, R.data, y)
+    else:
+        p.run("tnk_update_right_env_f64", B.data, R.data, B.data, y, None)
     return BlockTensor(p.out_layout, y)
 
 
