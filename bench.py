@@ -232,6 +232,9 @@ def main():
     torch.cuda.synchronize()
     t_steps = [a.elapsed_time(b) / 1e3 for a, b in evs]
     t_dev = float(sum(t_steps))
+    # kernels one matvec launches: the stages of the plan that have work
+    per_step = sum(1 for k in (len(hp.g1[2]), len(hp.c2[2]), len(hp.g3[2]), len(hp.c4[2]))
+                   if k > 0)
 
     # --- per-stage kernel timing (same stream, CUDA events around each launch) ---
     lib = _lib.lib()
@@ -327,18 +330,28 @@ def main():
                          "frac": achieved / dgemm,
                          "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (torch.matmul "
                                         "float64); MEASURED_PEAKS.json has no FP64 figure",
-                         "traffic": None,
+                         # DRAM bytes read + written by the two gemm_f64_kernel launches of
+                         # one matvec, from `ncu --set full --clock-control none -k
+                         # regex:gemm_f64 -s 2 -c 3 python bench.py --steps 2 --warmup 1
+                         # --no-cpu` (14.73 MB + 34.15 MB): the operands L, theta, R once; the
+                         # intermediates stay in the 129 MB L2
+                         "traffic": 48.88e6,
+                         "traffic_unit": "bytes per matvec (stages 1+3)",
                          "stage_ms": {"gemm1": t_g1 * 1e3, "comb": t_c2 * 1e3,
                                       "gemm3": t_g3 * 1e3}},
             "e2e": {"value": e2e, "unit": "GFLOP/s", "h2d_bytes_per_step": x.numel() * 8,
                     "d2h_bytes_per_step": x.numel() * 8, "max_rel_err_vs_device": err_e2e},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": per_step * args.steps,
             "clocks": clocks}
     line["mixed"] = mixed_leg(torch, dev, th, L, W1, W2, R, y, flush, flops_ref, parts,
                               args.steps, ms)
     line["float_float"] = ff_leg(torch, th, L, W1, W2, R, y, flush, flops_ref, parts,
                                  args.steps, ms, dgemm)
-    line["gpu_launches"] += 7 * args.steps
+    # launches of this library's kernels per step in each timed leg (the headline region is the
+    # device-resident FP64 matvec); the mixed leg: staging, two tcgen05 GEMMs, FP32 combination;
+    # the float-float leg: theta split, two GEMMs, combination, split-K sum when present
+    line["gpu_launches_per_step"] = {"fp64": per_step, "e2e": per_step, "mixed": 4,
+                                     "float_float": per_step + 1}
     if args.sweep:
         line["sweep"] = sweep_leg(torch, args)
     if not args.no_cpu:

@@ -153,7 +153,7 @@ int tnk_update_right_env_f64(const tnk_plan3* plan, const double* R, const doubl
  * callback or signal-safe section, a fixed pre-sized memory pool, an embedding or binding with
  * no device allocator): no counterpart in the reference. Instead of a caller workspace it uses
  * one fixed scratch array in the library's device memory, TNK_NOALLOC_SCRATCH_ELEMS doubles
- * (64 MiB, enough for the chi=1024 U(1) XXZ mid bond, which needs 6.5 M), held on every GPU that
+ * (64 MiB, enough for the chi=1024 U(1) XXZ mid bond, which needs 7.9 M), held on every GPU that
  * loads the library until the process exits. Plans needing more scratch get TNK_ERR_SIZE. The
  * first call on each device looks up the array's device address (cudaGetSymbolAddress) with that
  * device current; make that first call before any stream capture. All calls share the array, so
