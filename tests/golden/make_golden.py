@@ -8,6 +8,7 @@ usage:
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py small      # seconds
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py dmrg       # a few minutes
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py c2         # ~25 min on 8 cores
+  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py hubbard    # a minute
 
 Modes:
   small  Block and dense local problems (L, W1, W2, R, theta) dumped from real reference DMRG
@@ -18,6 +19,11 @@ Modes:
          chi=32 dense; XXZ N=12 U(1); XXZ N=64 U(1) at chi=64/128).  -> dmrg_small.json
   c2     The XXZ N=64 U(1) chi=1024 six-sweep run: energies, sweep times, matvec counts and every
          bond's sector dims.  -> c2_xxz_n64_chi1024.json
+  hubbard  The Fermi-Hubbard chain (t=1, U=4, half filling) under U(1) x U(1) (N_up, N_dn)
+         blocks, with the hand-written width-6 MPO of tnkit_gb300/workloads.py: the
+         reference's block MPO tensor of a bulk site, its seeded random block MPS, and the
+         per-sweep energies of its block DMRG (N=6 chi=16, N=8 chi=32), with the exact ground
+         energy of N=6 from the dense Hamiltonian.  -> hubbard_u1u1.npz, hubbard_u1u1.json
   tdvp   Two-site TDVP of the XXZ N=10 chain on complex U(1) blocks from a seeded random state:
          the initial tensors, the reference's Krylov exponential on a fixed vector, and the
          state vector after 4 steps of dt=0.05.  -> tdvp_xxz10.npz, tdvp_xxz10.json
@@ -255,6 +261,59 @@ def mode_c2(ref):
     print("E", E)
 
 
+def mode_hubbard(ref):
+    """U(1) x U(1) Hubbard runs of the reference (ProductSymmetry of two U(1)s)."""
+    from tnkit import dmrg, get_backend, U1, to_block_mpo
+    from tnkit.symmetry import ProductSymmetry
+    from tnkit.block_backend import random_block_mps
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tnkit_gb300.workloads import hubbard_mpo, HUBBARD_SITE_CHARGES
+    sym = ProductSymmetry((U1(), U1()))
+    be = get_backend("numpy-real")
+    arrays, meta = {}, {}
+    W = hubbard_mpo(6, 1.0, 4.0)
+    Wb, _ = to_block_mpo(W, [list(HUBBARD_SITE_CHARGES)] * 6, be, sym=sym)
+    w = Wb[2]
+    meta["mpo_site2"] = {"legs": [{"charges": [list(c) for c in l.charges],
+                                   "dims": list(l.dims), "sign": l.sign} for l in w.legs]}
+    arrays["mpo_site2"] = np.asarray(w.data, dtype=np.float64)
+    M = random_block_mps(Wb, 16, be, (3, 3), np.random.default_rng(1))
+    meta["mps_seed1_chi16"] = [{"legs": [{"charges": [list(c) for c in l.charges],
+                                          "dims": list(l.dims), "sign": l.sign}
+                                         for l in m.legs]} for m in M]
+    for i in (0, 2):
+        arrays[f"mps_seed1_chi16_site{i}"] = np.asarray(M[i].data, dtype=np.float64)
+    # exact ground energy of N=6 at half filling from the dense MPO
+    T = W[0][0]
+    for Wn in W[1:]:
+        T = np.einsum("wab,wxcd->xacbd", T, Wn)
+        T = T.reshape(T.shape[0], T.shape[1] * T.shape[2], -1)
+    H = T[0]
+    q = np.array([[0, 0], [1, 0], [0, 1], [1, 1]])
+    import itertools
+    idx = [i for i, ss in enumerate(itertools.product(range(4), repeat=6))
+           if tuple(q[list(ss)].sum(0)) == (3, 3)]
+    meta["n6_exact_E"] = float(np.linalg.eigvalsh(H[np.ix_(idx, idx)])[0])
+    runs = {}
+    for N, chi, sweeps in ((6, 16, 4), (8, 32, 3)):
+        Wn = hubbard_mpo(N, 1.0, 4.0)
+        Wbn, _ = to_block_mpo(Wn, [list(HUBBARD_SITE_CHARGES)] * N, be, sym=sym)
+        t0 = time.perf_counter()
+        E, mps, info = dmrg(Wbn, chi, charge=(N // 2, N // 2), seed=1, n_sweeps=sweeps, tol=0,
+                            rtol=0, expand=0, backend="numpy-real")
+        runs[f"n{N}_chi{chi}"] = {
+            "E": float(E), "energies": [float(e) for e in info["energies"]],
+            "discarded_weight": float(info["discarded_weight"]),
+            "bonds": [{"charges": [list(c) for c in m.legs[2].charges],
+                       "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
+            "wall_s": time.perf_counter() - t0}
+        print(N, chi, E, flush=True)
+    meta["runs"] = runs
+    np.savez(os.path.join(HERE, "hubbard_u1u1.npz"), **arrays)
+    with open(os.path.join(HERE, "hubbard_u1u1.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 def _dense_vector(mps):
     """The state vector of a block MPS with every leg in sector order (its flat amplitudes)."""
     v = np.ones((1,), complex)
@@ -305,8 +364,9 @@ def mode_tdvp(ref):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp"])
+    ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp", "hubbard"])
     ap.add_argument("--ref", default="/root/reference")
     a = ap.parse_args()
     ref = _import_ref(a.ref)
-    {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2, "tdvp": mode_tdvp}[a.mode](ref)
+    {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2, "tdvp": mode_tdvp,
+     "hubbard": mode_hubbard}[a.mode](ref)

@@ -84,3 +84,24 @@ def test_block_dmrg_gram_truncation_matches_reference(N, chi):
     E, M, info = dmrg(_xxz_blocks(N), chi, charge=0, seed=1, n_sweeps=len(ref["energies"]),
                       tol=0, rtol=0, expand=0, svd_method="gram")
     assert abs(E - ref["E"]) <= 1e-10, (E, ref["E"])
+
+
+@pytest.mark.parametrize("N,chi", [(6, 16), (8, 32)])
+def test_hubbard_u1xu1_every_sweep_matches_reference(N, chi):
+    """The Fermi-Hubbard chain under U(1) x U(1) (N_up, N_dn) blocks, half filling: the same
+    seeded start as the reference, its final energy to 1e-12 relative and every sweep's to
+    1e-10 (a sweep still far from convergence depends on where each local Lanczos stops, at a
+    1e-9 residual), every bond's (N_up, N_dn) sectors at the end."""
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.dmrg import dmrg
+    from tnkit_gb300.mpo import to_block_mpo
+    ref = json.load(open(os.path.join(GOLDEN, "hubbard_u1u1.json")))["runs"][f"n{N}_chi{chi}"]
+    Wb, _ = to_block_mpo(workloads.hubbard_mpo(N), [workloads.HUBBARD_SITE_CHARGES] * N)
+    E, M, info = dmrg(Wb, chi, charge=(N // 2, N // 2), seed=1, n_sweeps=len(ref["energies"]),
+                      tol=0, rtol=0, expand=0)
+    assert abs(E - ref["E"]) <= 1e-12 * abs(ref["E"]), (E, ref["E"])
+    assert np.allclose(info["energies"], ref["energies"], rtol=1e-10, atol=0), \
+        (info["energies"], ref["energies"])
+    for m, b in zip(M, ref["bonds"]):
+        assert [list(c) for c in m.legs[2].charges] == b["charges"]
+        assert list(m.legs[2].dims) == b["dims"]

@@ -4,6 +4,10 @@
   to_block_mpo      tnkit/block_backend.py:211-256  (legs (wl, wr, s, s'), signs (+1,-1,+1,-1))
   random_block_mps  tnkit/block_backend.py:259-311  (bond sectors, numpy RNG, canonical order)
 
+Charges are U(1) ints or, for a product of U(1)s (the (N_up, N_down) labels of the Hubbard
+chain), tuples sorted lexicographically with the first factor most significant, as the
+reference's ProductSymmetry orders them (tnkit/symmetry.py:169-240).
+
 These run on the host once per problem; the results are uploaded to the GPU. The random MPS
 draws the same numbers from the same generator as the reference, so a seeded run starts from
 the reference's own initial state.
@@ -19,16 +23,32 @@ from .layout import Leg, layout_of, from_dense_np
 from .tensor import BlockTensor
 
 
-def _u1_leg(q, sign=1):
-    q = np.asarray(q, dtype=np.int64)
-    c, n = np.unique(q, return_counts=True)
-    return (Leg(tuple(int(x) for x in c), tuple(int(x) for x in n), sign),
-            np.argsort(q, kind="stable"))
+def _label_rows(q):
+    """Charges as an int array (n, factors) and whether they are tuples (a product of U(1)s)."""
+    a = np.asarray(q, dtype=np.int64)
+    if a.ndim == 1:
+        return a.reshape(-1, 1), False
+    return a.reshape(len(a), -1), True
+
+
+def _as_label(row, product: bool):
+    return tuple(int(v) for v in row) if product else int(row[0])
+
+
+def _leg_from_charges(q, sign=1):
+    """The leg whose dense index i has charge q[i], and the dense indices in sector order (stable
+    within a sector); sectors sorted lexicographically, the first factor most significant
+    (tnkit/blocks.py:104-118, tnkit/symmetry.py:169-240)."""
+    a, product = _label_rows(q)
+    uniq, inv, counts = np.unique(a, axis=0, return_inverse=True, return_counts=True)
+    return (Leg(tuple(_as_label(r, product) for r in uniq), tuple(int(n) for n in counts), sign),
+            np.argsort(np.ravel(inv), kind="stable"))
 
 
 def mpo_charges(mpo: Sequence[np.ndarray], site_charges, tol: float = 0.0):
-    """U(1) charge of every MPO channel, one int array per MPO bond (left boundary trivial).
-    Channels no nonzero path connects to both ends get charge 0 (they carry nothing)."""
+    """The charge of every MPO channel, one array per MPO bond (left boundary trivial): int
+    arrays for U(1) site charges, (channels, factors) arrays for tuple charges (U(1) x U(1) ...).
+    Channels no nonzero path connects to both ends get the trivial charge (they carry nothing)."""
     nz = [(np.abs(np.asarray(W)) > tol).any(axis=(2, 3)) for W in mpo]
     fwd = [np.ones(nz[0].shape[0], bool)]
     for m in nz:
@@ -37,25 +57,31 @@ def mpo_charges(mpo: Sequence[np.ndarray], site_charges, tol: float = 0.0):
     for m in reversed(nz):
         bwd.append(m[:, bwd[-1]].any(1))
     live = [f & b for f, b in zip(fwd, reversed(bwd))]
-    out = [np.zeros(np.shape(mpo[0])[0], np.int64)]
+    q0, product = _label_rows(site_charges[0])
+    nf = q0.shape[1]
+    out = [np.zeros((np.shape(mpo[0])[0], nf), np.int64)]
     for n, (W, q) in enumerate(zip(mpo, site_charges)):
         W = np.asarray(W)
+        qa, _ = _label_rows(q)
         a, b, s, t = np.nonzero(np.abs(W) > tol)
         keep = live[n][a] & live[n + 1][b]
-        vals = out[-1][a[keep]] + np.asarray(q)[s[keep]] - np.asarray(q)[t[keep]]
-        qr = np.zeros(W.shape[1], np.int64)
+        vals = out[-1][a[keep]] + qa[s[keep]] - qa[t[keep]]
+        bk = b[keep]
+        qr = np.zeros((W.shape[1], nf), np.int64)
         for j in np.flatnonzero(live[n + 1]):
-            v = np.unique(vals[b[keep] == j])
+            v = np.unique(vals[bk == j], axis=0)
             if len(v) != 1:
                 raise ValueError(f"MPO site {n}, right channel {j}: charges {v.tolist()} "
                                  "(write the terms with charged operators such as S+ S-)")
             qr[j] = v[0]
         out.append(qr)
-    return out
+    return out if product else [c[:, 0].copy() for c in out]
 
 
 def to_block_mpo(mpo: Sequence[np.ndarray], site_charges, device="cuda", tol: float = 0.0):
-    """A dense MPO as block tensors (U(1)); returns (tensors, orders) like the reference."""
+    """A dense MPO as block tensors under U(1) (int site charges) or a product of U(1)s (tuple
+    site charges, e.g. (N_up, N_down)); returns (tensors, orders) like the reference
+    (tnkit/block_backend.py:211-256)."""
     chans = mpo_charges(mpo, site_charges, tol)
     out, orders = [], []
     for n, W in enumerate(mpo):
@@ -64,8 +90,8 @@ def to_block_mpo(mpo: Sequence[np.ndarray], site_charges, device="cuda", tol: fl
             if np.abs(W.imag).max() > 1e-12 * max(1.0, np.abs(W.real).max()):
                 raise TypeError("complex MPO entries need a complex backend")
             W = W.real
-        (cl, ol), (cr, orr) = _u1_leg(chans[n]), _u1_leg(chans[n + 1])
-        p, op = _u1_leg(site_charges[n])
+        (cl, ol), (cr, orr) = _leg_from_charges(chans[n]), _leg_from_charges(chans[n + 1])
+        p, op = _leg_from_charges(site_charges[n])
         x = W.astype(np.float64)
         for i, o in enumerate((ol, orr, op, op)):
             x = np.take(x, o, axis=i)
@@ -89,21 +115,34 @@ def dense_mpo(mpo: Sequence[np.ndarray], device="cuda"):
     return out
 
 
-def random_block_mps(mpo: Sequence[BlockTensor], chi: int, charge: int, rng,
+def _fuse(a, b, sign=1):
+    if isinstance(a, tuple):
+        return tuple(x + sign * y for x, y in zip(a, b))
+    return a + sign * b
+
+
+def random_block_mps(mpo: Sequence[BlockTensor], chi: int, charge, rng,
                      device="cuda") -> List[BlockTensor]:
-    """Random block MPS of total charge `charge`, bonds of at most `chi` states, drawn from `rng`
-    in the reference's order (one standard_normal(size) per site, canonical layout)."""
+    """Random block MPS of total charge `charge` (an int, or a tuple for a product of U(1)s),
+    bonds of at most `chi` states, drawn from `rng` in the reference's order (one
+    standard_normal(size) per site, canonical layout; tnkit/block_backend.py:259-311)."""
     phys = [W.legs[2] for W in mpo]
+    product = isinstance(phys[0].charges[0], tuple)
+    if product:
+        charge = tuple(int(c) for c in charge)
+        unit = tuple(0 for _ in phys[0].charges[0])
+    else:
+        unit = 0
 
     def grow(counts, leg, sign):
         out = {}
         for c, n in counts.items():
             for a, d in zip(leg.charges, leg.dims):
-                c2 = c + (a if sign > 0 else -a)
+                c2 = _fuse(c, a, 1 if sign > 0 else -1)
                 out[c2] = out.get(c2, 0) + n * d
         return out
 
-    left, right = [{0: 1}], [{charge: 1}]
+    left, right = [{unit: 1}], [{charge: 1}]
     for p in phys:
         left.append(grow(left[-1], p, 1))
     for p in reversed(phys):
@@ -111,7 +150,7 @@ def random_block_mps(mpo: Sequence[BlockTensor], chi: int, charge: int, rng,
     right.reverse()
     if charge not in left[-1]:
         raise ValueError(f"no state of these sites has total charge {charge!r}")
-    bonds, cand = [], {0}
+    bonds, cand = [], {unit}
     for n, (lc, rc) in enumerate(zip(left, right)):
         w = {c: min(lc[c], rc[c]) for c in cand if c in rc}
         keep = sorted(w, key=lambda c: (-w[c], c))[:chi]
@@ -121,14 +160,14 @@ def random_block_mps(mpo: Sequence[BlockTensor], chi: int, charge: int, rng,
             dims[max(dims, key=dims.get)] -= 1
         bonds.append(dims)
         if n < len(phys):
-            cand = {c + a for c in keep for a in phys[n].charges}
+            cand = {_fuse(c, a) for c in keep for a in phys[n].charges}
     for n in range(len(phys) - 1, -1, -1):
-        prv = {c - a for c in bonds[n + 1] for a in phys[n].charges}
+        prv = {_fuse(c, a, -1) for c in bonds[n + 1] for a in phys[n].charges}
         bonds[n] = {c: d for c, d in bonds[n].items() if c in prv}
     legs = [Leg(tuple(sorted(b)), tuple(b[c] for c in sorted(b)), 1) for b in bonds]
     out = []
     for n, p in enumerate(phys):
-        lay = layout_of((legs[n], p, legs[n + 1].flip()), 0)
+        lay = layout_of((legs[n], p, legs[n + 1].flip()), unit)
         host = rng.standard_normal((lay.size,))
         out.append(BlockTensor(lay, torch.as_tensor(host, device=device)))
     return out

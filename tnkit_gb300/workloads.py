@@ -4,6 +4,10 @@
                         (the bulk tensor of the reference's bench/profile/fused_dmrg_check.py:48-53)
   tfim_mpo(N, g)        open transverse-field Ising chain, H = -sum XX - g sum Z, width 3
                         (tnkit/models.py:50-95 with h = 0)
+  hubbard_mpo(N, t, U)  open Fermi-Hubbard chain H = -t sum (c+_{i s} c_{i+1 s} + h.c.)
+                        + U sum n_{i up} n_{i dn}, one d=4 site per orbital (|0>, |up>, |dn>,
+                        |up dn>), Jordan-Wigner strings inside the MPO, width 6; site charges
+                        (N_up, N_dn) for U(1) x U(1) blocks (HUBBARD_SITE_CHARGES)
   mid_bond_problem      random U(1) environments and two-site block of a chain's bond, with given
                         sector dims: the local problem one Lanczos matvec sees.
 """
@@ -48,6 +52,38 @@ def tfim_mpo(N: int, g: float = 1.0):
     W = np.zeros((3, 3, 2, 2))
     W[0, 0], W[0, 1], W[0, 2], W[1, 2], W[2, 2] = np.eye(2), sx, -g * sz, -sx, np.eye(2)
     return open_chain(W, N)
+
+
+# (N_up, N_dn) of the local states |0>, |up>, |dn>, |up dn>
+HUBBARD_SITE_CHARGES = ((0, 0), (1, 0), (0, 1), (1, 1))
+
+
+def hubbard_bulk(t: float = 1.0, U: float = 4.0) -> np.ndarray:
+    """Bulk MPO tensor (6, 6, 4, 4) of the Fermi-Hubbard chain. The fermions are ordered
+    (1 up, 1 dn, 2 up, 2 dn, ...) with Jordan-Wigner strings: with hard-core a_s on a site,
+    F_s = (-1)^n_s and F = F_up F_dn, c+_{j up} c_{j+1 up} = (a+_up F)_j (a_up)_{j+1},
+    c+_{j+1 up} c_{j up} = (F a_up)_j (a+_up)_{j+1}, c+_{j dn} c_{j+1 dn} =
+    (F_up a+_dn F)_j (F_up a_dn)_{j+1}, c+_{j+1 dn} c_{j dn} = (F F_up a_dn)_j (F_up a+_dn)_{j+1}.
+    Channels: idle, the four hops, done."""
+    e = lambda i, j: np.outer(np.eye(4)[i], np.eye(4)[j])
+    a_up = e(0, 1) + e(2, 3)
+    a_dn = e(0, 2) + e(1, 3)
+    n_up, n_dn = np.diag([0.0, 1.0, 0.0, 1.0]), np.diag([0.0, 0.0, 1.0, 1.0])
+    f_up, f_dn = np.diag([1.0, -1.0, 1.0, -1.0]), np.diag([1.0, 1.0, -1.0, -1.0])
+    f = f_up @ f_dn
+    i4 = np.eye(4)
+    W = np.zeros((6, 6, 4, 4))
+    W[0, 0], W[5, 5] = i4, i4
+    W[0, 1], W[1, 5] = a_up.T @ f, -t * a_up
+    W[0, 2], W[2, 5] = f @ a_up, -t * a_up.T
+    W[0, 3], W[3, 5] = f_up @ a_dn.T @ f, -t * f_up @ a_dn
+    W[0, 4], W[4, 5] = f @ f_up @ a_dn, -t * f_up @ a_dn.T
+    W[0, 5] = U * n_up @ n_dn
+    return W
+
+
+def hubbard_mpo(N: int, t: float = 1.0, U: float = 4.0):
+    return open_chain(hubbard_bulk(t, U), N)
 
 
 def mid_bond_problem(charges: Sequence[int] = C2_MID_CHARGES,
