@@ -175,6 +175,7 @@ def main():
                     help="also run the whole chi=1024 DMRG (6 sweeps, FP64 and mixed): minutes")
     ap.add_argument("--sweep-chi", type=int, default=1024)
     ap.add_argument("--sweep-n", type=int, default=64)
+    ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
     ap.add_argument("--sweep-precisions", default="f64,ff,mixed,mixed-ff")
@@ -461,31 +462,45 @@ def ff_leg(torch, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps, ms64, d
 
 
 def sweep_leg(torch, args):
-    """The whole U(1) XXZ DMRG at chi (6 sweeps, seed 1, expand 0) in FP64 and mixed precision,
-    with the reference's own FP64 result (tests/golden/c2_xxz_n64_chi1024.json) as the oracle."""
+    """The whole DMRG at chi (seed 1, expand 0) in each precision: the U(1) XXZ chain, with the
+    reference's own FP64 result (tests/golden/c2_xxz_n64_chi1024.json) as the oracle at N=64
+    chi=1024, or the half-filled Fermi-Hubbard chain (t=1, U=4) under U(1) x U(1) (N_up, N_dn)
+    blocks, compared with the FP64 run."""
     from tnkit_gb300 import workloads
     from tnkit_gb300.dmrg import dmrg
     from tnkit_gb300.mpo import to_block_mpo
     N, chi = args.sweep_n, args.sweep_chi
-    out = {"workload": f"U(1) XXZ N={N} chi={chi}, {args.sweeps} sweeps, seed 1, expand 0, "
+    if args.sweep_model == "hubbard":
+        name = f"Fermi-Hubbard t=1 U=4 half filling, U(1)xU(1), N={N} chi={chi}"
+        make = lambda: to_block_mpo(workloads.hubbard_mpo(N, 1.0, 4.0),
+                                    [workloads.HUBBARD_SITE_CHARGES] * N)[0]
+        charge = (N // 2, N // 2)
+    else:
+        name = f"U(1) XXZ N={N} chi={chi}"
+        make = lambda: to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
+        charge = 0
+    out = {"workload": f"{name}, {args.sweeps} sweeps, seed 1, expand 0, "
                        f"truncation '{args.svd_method}'"}
     ref = None
     gp = os.path.join(HERE, "tests", "golden", "c2_xxz_n64_chi1024.json")
-    if N == 64 and chi == 1024 and os.path.exists(gp):
+    if args.sweep_model == "xxz" and N == 64 and chi == 1024 and os.path.exists(gp):
         ref = json.load(open(gp))
         out["reference_E"] = ref["E"]
         out["reference_sweep_s"] = ref["sweep_s"]
     precs = [p for p in args.sweep_precisions.split(",") if p]
     for prec in precs:
-        Wb = to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
+        Wb = make()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E, M, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=args.sweeps, tol=0, rtol=0,
+        E, M, info = dmrg(Wb, chi, charge=charge, seed=1, n_sweeps=args.sweeps, tol=0, rtol=0,
                           expand=0, precision=prec, svd_method=args.svd_method)
         torch.cuda.synchronize()
         rec = {"E": E, "energies": info["energies"], "sweep_s": info["sweep_s"],
                "total_s": time.perf_counter() - t0, "phase_time": info["phase_time"],
-               "matvecs": info["mixed_counts"], "discarded_weight": info["discarded_weight"]}
+               "matvecs": info["mixed_counts"], "discarded_weight": info["discarded_weight"],
+               "mid_bond": {"sectors": len(M[N // 2].legs[0].dims),
+                            "dim": int(sum(M[N // 2].legs[0].dims)),
+                            "largest_sector": int(max(M[N // 2].legs[0].dims))}}
         if ref is not None:
             rec["abs_dE_vs_reference"] = abs(E - ref["E"])
         out[prec] = rec
