@@ -46,6 +46,19 @@ def xxz_mpo(N: int, delta: float = 1.0):
     return open_chain(xxz_bulk(delta), N)
 
 
+def xxz_disordered_mpo(J: Sequence[float], delta: float = 1.0):
+    """Open XXZ chain H = sum_i J_i [(S+S- + S-S+)/2 + delta Sz Sz]_{i,i+1} with one coupling per
+    bond (len(J) = N - 1): the bond's J_i sits on the left site's outgoing channels."""
+    N = len(J) + 1
+    out = []
+    for i in range(N):
+        W = xxz_bulk(delta)
+        j = J[i] if i < N - 1 else 1.0
+        W[0, 1:4] *= j
+        out.append(W[0:1] if i == 0 else W[:, 4:5] if i == N - 1 else W)
+    return out
+
+
 def tfim_mpo(N: int, g: float = 1.0):
     sx = np.array([[0.0, 1.0], [1.0, 0.0]])
     sz = np.diag([1.0, -1.0])
