@@ -88,3 +88,31 @@ def test_truncated_svd_gram_native_matches_torch_path():
     full = np.sort(full)[::-1]
     assert np.allclose(np.sort(S.cpu().numpy())[::-1], full[:6], rtol=1e-12, atol=0)
     assert abs(disc - float(np.sum(full[6:] ** 2))) <= 1e-12 * float(np.sum(full ** 2))
+
+
+def test_host_split_matches_gpu_only():
+    """The sectors split between the GPU and host LAPACK give the same truncation as all on the
+    GPU or all on the host: kept values, bond sectors, discarded weight, reconstruction."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(9)
+    a = Leg((-3, -1, 1, 3), (40, 260, 250, 30), 1)
+    b = Leg((-3, -1, 1, 3), (35, 240, 255, 45), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size) * np.repeat(
+        10.0 ** -np.linspace(0, 4, lay.nblocks), [int(x) for x in lay.sizes])
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    res = {w: LA.truncated_svd(m, 300, scale="none", method="gram", host=w)
+           for w in ("auto", "never", "always")}
+    Ua, Sa, Va, da = res["never"]
+    for w in ("auto", "always"):
+        U, S, V, d = res[w]
+        assert U.layout.legs == Ua.layout.legs and V.layout.legs == Va.layout.legs
+        assert torch.allclose(S, Sa, rtol=1e-10, atol=1e-14 * float(Sa.max()))
+        assert abs(d - da) <= 1e-10 * max(da, 1e-300) + 1e-24
+        rec = to_dense_np(U.layout, U.data.cpu().numpy()) * S.cpu().numpy()[None, :] @ \
+            to_dense_np(V.layout, V.data.cpu().numpy())
+        rec0 = to_dense_np(Ua.layout, Ua.data.cpu().numpy()) * Sa.cpu().numpy()[None, :] @ \
+            to_dense_np(Va.layout, Va.data.cpu().numpy())
+        assert np.abs(rec - rec0).max() <= 1e-10 * float(Sa.max())

@@ -108,14 +108,16 @@ class _Concurrent:
             return self.streams[key]
 
     def map(self, fn, mats, device):
+        """fn(M) for each M (or fn[i](M_i) when fn is a list), one stream per item."""
         main = torch.cuda.current_stream(device)
         streams = [self.stream(device, i) for i in range(len(mats))]
         for s in streams:
             s.wait_stream(main)
+        fns = fn if isinstance(fn, (list, tuple)) else [fn] * len(mats)
 
         def run(i):
             with torch.cuda.stream(streams[i]):
-                out = fn(mats[i])
+                out = fns[i](mats[i])
                 for t in out:
                     if isinstance(t, torch.Tensor):
                         t.record_stream(main)
@@ -155,6 +157,87 @@ def _svd_gram_native(M: torch.Tensor):
     return U, S, Vh, s_host
 
 
+# --- host co-processing of the truncation -----------------------------------------------------
+# A chi=1024 bond's two or three largest sectors (~500 rows) are latency-bound in cuSOLVER (a
+# 522-row syevd is ~14 ms and two of them barely overlap), while the host's cores are idle
+# during the truncation. Sectors are split between the GPU path and host LAPACK (numpy, the
+# reference's own numpy branch of method='gram') by a greedy makespan on measured costs; numpy
+# releases the interpreter lock inside LAPACK. The host library's thread count is lowered to a
+# quarter of the cores for the duration (with more, its threads and cuSOLVER's host work slow
+# each other down).
+_GPU_MS_PER_ROW = 14.0 / 522          # cuSOLVER path: ~linear in n (latency-bound)
+_HOST_MS_522 = 28.6                   # numpy path with a quarter of the cores: ~n^2.1
+_HOST_BLAS = {"lib": None, "tried": False}
+
+
+def _host_blas():
+    """(set, get) of numpy's bundled OpenBLAS thread count, or None when not found."""
+    if not _HOST_BLAS["tried"]:
+        _HOST_BLAS["tried"] = True
+        import glob
+        import os
+        base = os.path.join(os.path.dirname(os.path.dirname(np.__file__)), "numpy.libs")
+        for path in sorted(glob.glob(os.path.join(base, "libscipy_openblas*.so*"))):
+            try:
+                lib = C.CDLL(path)
+                set_, get_ = (lib.scipy_openblas_set_num_threads64_,
+                              lib.scipy_openblas_get_num_threads64_)
+            except (OSError, AttributeError):
+                continue
+            set_.argtypes, set_.restype = [C.c_int], None
+            get_.argtypes, get_.restype = [], C.c_int
+            _HOST_BLAS["lib"] = (set_, get_)
+            break
+    return _HOST_BLAS["lib"]
+
+
+def _assign_sectors(shapes, host_ok: bool):
+    """Per sector True for the host path: greedy over sectors by decreasing size, each to the
+    side (a queue each) that finishes it first."""
+    if not host_ok or len(shapes) < 2:
+        return [False] * len(shapes)
+    order = sorted(range(len(shapes)), key=lambda i: -min(shapes[i]))
+    t_gpu = t_host = 0.0
+    out = [False] * len(shapes)
+    for i in order:
+        n = min(shapes[i])
+        g = _GPU_MS_PER_ROW * n + 0.4
+        h = _HOST_MS_522 * (n / 522.0) ** 2.1 + 0.05
+        if t_host + h < t_gpu + g:
+            out[i], t_host = True, t_host + h
+        else:
+            t_gpu += g
+    return out
+
+
+def _svd_gram_host(M: torch.Tensor):
+    """The Gram factorisation of one block on the host (numpy / LAPACK), results back on the
+    device: the reference's numpy branch (tnkit/blocks.py:1345-1377)."""
+    Mh = M.cpu().numpy()
+    R, Cc = Mh.shape
+    if R >= Cc:
+        _, V = np.linalg.eigh(Mh.T @ Mh)
+        V = V[:, ::-1]
+        Q, Rr = np.linalg.qr(Mh @ V)
+    else:
+        _, Uh = np.linalg.eigh(Mh @ Mh.T)
+        Uh = Uh[:, ::-1]
+        Q, Rr = np.linalg.qr(Mh.T @ Uh)
+    d = np.diagonal(Rr)
+    S = np.abs(d)
+    Q = Q * np.where(S > 0, d / np.where(S > 0, S, 1.0), 1.0)
+    o = np.argsort(-S, kind="stable")
+    S, Q = S[o], Q[:, o]
+    if R >= Cc:
+        U, Vh = Q, V[:, o].T
+    else:
+        U, Vh = Uh[:, o], Q.T
+    dev = M.device
+    return (torch.as_tensor(np.ascontiguousarray(U), device=dev),
+            torch.as_tensor(S, device=dev),
+            torch.as_tensor(np.ascontiguousarray(Vh), device=dev), S)
+
+
 def _svd_gram(M: torch.Tensor):
     """U, S (descending), Vh of one block through the smaller Gram matrix: Hermitian eigh, then
     a QR that re-orthonormalises the computed singular vectors (the reference's method='gram',
@@ -180,11 +263,15 @@ def _svd_gram(M: torch.Tensor):
 
 
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
-                  method: str = "svd", normalize: bool = True):
+                  method: str = "svd", normalize: bool = True, host: str = "auto"):
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
+    With method='gram', `host` chooses where the sectors are factored: 'auto' (split between the
+    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only).
     Returns U, S (device vector, normalised when scale != 'none'), Vh, disc (absolute)."""
+    if host not in ("auto", "never", "always"):
+        raise ValueError("host must be 'auto', 'never' or 'always'")
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
     lr, lc = m.layout.legs
@@ -198,7 +285,24 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
     mats = [M for _, _, M in blocks]
     if len(mats) > 1 and m.data.is_cuda:
-        facs = _concurrent().map(fn, mats, m.data.device)
+        if method == "gram" and fn is _svd_gram_native and host != "never":
+            blas = _host_blas()
+            on_host = _assign_sectors([tuple(M.shape) for M in mats], blas is not None) \
+                if host == "auto" else [True] * len(mats)
+            fns = [_svd_gram_host if h else _svd_gram_native for h in on_host]
+            if any(on_host) and blas is not None:
+                prev = blas[1]()
+                # a quarter of the cores: with more, the truncation of a chi=1024 mid bond is
+                # no faster than on the GPU alone (46 ms); with 4 of 16 it takes 32 ms
+                blas[0](max(1, prev // 4))
+                try:
+                    facs = _concurrent().map(fns, mats, m.data.device)
+                finally:
+                    blas[0](prev)
+            else:
+                facs = _concurrent().map(fns, mats, m.data.device)
+        else:
+            facs = _concurrent().map(fn, mats, m.data.device)
     else:
         facs = [fn(M) for M in mats]
     parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
