@@ -179,6 +179,9 @@ def main():
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
     ap.add_argument("--sweep-precisions", default="f64,ff,mixed,mixed-ff")
+    ap.add_argument("--mixed-schedule", default="bond", choices=["bond", "sweep"],
+                    help="mixed modes: polish every bond, or tensor-core-only opening sweeps")
+    ap.add_argument("--polish-sweeps", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()
@@ -480,7 +483,9 @@ def sweep_leg(torch, args):
         make = lambda: to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
         charge = 0
     out = {"workload": f"{name}, {args.sweeps} sweeps, seed 1, expand 0, "
-                       f"truncation '{args.svd_method}'"}
+                       f"truncation '{args.svd_method}', mixed schedule '{args.mixed_schedule}'"
+                       + (f" ({args.polish_sweeps} polished sweeps)"
+                          if args.mixed_schedule == "sweep" else "")}
     ref = None
     gp = os.path.join(HERE, "tests", "golden", "c2_xxz_n64_chi1024.json")
     if args.sweep_model == "xxz" and N == 64 and chi == 1024 and os.path.exists(gp):
@@ -493,7 +498,8 @@ def sweep_leg(torch, args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         E, M, info = dmrg(Wb, chi, charge=charge, seed=1, n_sweeps=args.sweeps, tol=0, rtol=0,
-                          expand=0, precision=prec, svd_method=args.svd_method)
+                          expand=0, precision=prec, svd_method=args.svd_method,
+                          mixed_schedule=args.mixed_schedule, polish_sweeps=args.polish_sweeps)
         torch.cuda.synchronize()
         rec = {"E": E, "energies": info["energies"], "sweep_s": info["sweep_s"],
                "total_s": time.perf_counter() - t0, "phase_time": info["phase_time"],

@@ -344,6 +344,11 @@ int tnk_zaxpby_f64(const double* x, double* y, int64_t n, const double* sa, doub
 int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes);
 int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U, double* S, double* Vh,
                      void* ws, int64_t ws_bytes, double* S_host, void* stream);
+/* The same in FP32 (S_host still double): the truncations of the opening sweeps of the mixed
+ * schedule, whose local solves are only tensor-core accurate. */
+int tnk_svd_gram_ws_f32(int64_t R, int64_t C, int64_t* bytes);
+int tnk_svd_gram_f32(const float* M, int64_t R, int64_t C, float* U, float* S, float* Vh,
+                     void* ws, int64_t ws_bytes, double* S_host, void* stream);
 
 #ifdef __cplusplus
 }

@@ -128,3 +128,16 @@ def test_float_float_env_updates_match_fp64(scale):
         got = f(env, site, W, precision="ff").data
         assert got.shape == ref.shape
         assert _rel(got, ref) <= 1e-13, (f.__name__, _rel(got, ref))
+
+
+@pytest.mark.parametrize("prec,polish", [("mixed-ff", 2), ("mixed-ff", 1), ("mixed", 1)])
+def test_sweep_schedule_reaches_fp64_energy(prec, polish):
+    """mixed_schedule='sweep': the opening sweeps on the tensor cores alone, the last one or two
+    polished (float-float or FP64), end within 1e-10 of the FP64 run's energy."""
+    from tnkit_gb300.dmrg import dmrg
+    kw = dict(charge=0, seed=1, n_sweeps=6, tol=0, rtol=0, expand=0)
+    E64, _, _ = dmrg(_xxz_blocks(32), 64, **kw)
+    E, M, info = dmrg(_xxz_blocks(32), 64, precision=prec, mixed_schedule="sweep",
+                      polish_sweeps=polish, **kw)
+    assert info["mixed_counts"]["lo"] > info["mixed_counts"]["hi"] > 0
+    assert abs(E - E64) <= 1e-10 * abs(E64), (E, E64)

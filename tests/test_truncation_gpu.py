@@ -116,3 +116,23 @@ def test_host_split_matches_gpu_only():
         rec0 = to_dense_np(Ua.layout, Ua.data.cpu().numpy()) * Sa.cpu().numpy()[None, :] @ \
             to_dense_np(Va.layout, Va.data.cpu().numpy())
         assert np.abs(rec - rec0).max() <= 1e-10 * float(Sa.max())
+
+
+def test_fp32_truncation_close_to_fp64():
+    """dtype=float32 (the opening sweeps of the mixed schedule): the same kept sectors, values
+    within FP32-Gram accuracy, FP32-orthonormal factors returned in FP64."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(10)
+    a = Leg((-1, 1), (150, 120), 1)
+    b = Leg((-1, 1), (140, 130), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size)
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    U, S, V, d = LA.truncated_svd(m, 60, scale="none", method="gram")
+    U3, S3, V3, d3 = LA.truncated_svd(m, 60, scale="none", method="gram", dtype=torch.float32)
+    assert U3.data.dtype == torch.float64 and U3.layout.legs == U.layout.legs
+    assert float((S3 - S).abs().max()) <= 1e-5 * float(S.max())
+    Ud = to_dense_np(U3.layout, U3.data.cpu().numpy())
+    assert np.abs(Ud.T @ Ud - np.eye(Ud.shape[1])).max() <= 1e-5

@@ -60,42 +60,43 @@ struct Layout {
 
 inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 
+template <typename T> struct La;
+
+template <typename T>
 int sizes(int64_t R, int64_t C, Handles* h, Layout* L) {
     const int64_t n = R < C ? R : C, m = R < C ? C : R;
     int lw_ev = 0, lw_qr = 0, lw_or = 0;
-    if (cusolverDnDsyevd_bufferSize(h->sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                    (int)n, nullptr, (int)n, nullptr, &lw_ev) !=
-            CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDgeqrf_bufferSize(h->sol, (int)m, (int)n, nullptr, (int)m, &lw_qr) !=
-            CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDorgqr_bufferSize(h->sol, (int)m, (int)n, (int)n, nullptr, (int)m, nullptr,
-                                    &lw_or) != CUSOLVER_STATUS_SUCCESS) {
+    if (La<T>::syevd_ws(h->sol, (int)n, &lw_ev) != CUSOLVER_STATUS_SUCCESS ||
+        La<T>::geqrf_ws(h->sol, (int)m, (int)n, &lw_qr) != CUSOLVER_STATUS_SUCCESS ||
+        La<T>::orgqr_ws(h->sol, (int)m, (int)n, &lw_or) != CUSOLVER_STATUS_SUCCESS) {
         tnk::set_error("svd_gram: cuSOLVER workspace query failed (R=%lld, C=%lld)",
                        (long long)R, (long long)C);
         return TNK_ERR_CUDA;
     }
-    int lw = std::max(lw_ev, std::max(lw_qr, lw_or));
+    const int lw = std::max(lw_ev, std::max(lw_qr, lw_or));
+    const size_t es = sizeof(T);
     size_t o = 0;
-    L->G = o; o += up(sizeof(double) * n * n);
-    L->Y = o; o += up(sizeof(double) * m * n);
-    L->w = o; o += up(sizeof(double) * n);
-    L->tau = o; o += up(sizeof(double) * n);
-    L->sign = o; o += up(sizeof(double) * n);
+    L->G = o; o += up(es * n * n);
+    L->Y = o; o += up(es * m * n);
+    L->w = o; o += up(es * n);
+    L->tau = o; o += up(es * n);
+    L->sign = o; o += up(es * n);
     L->perm = o; o += up(sizeof(int) * n);
     L->info = o; o += up(sizeof(int) * 4);
-    L->work = o; o += up(sizeof(double) * (size_t)lw);
+    L->work = o; o += up(es * (size_t)lw);
     L->total = o;
     return TNK_OK;
 }
 
 // Reverse the column order of an n x n column-major matrix in place (eigenvectors ascending ->
 // descending).
-__global__ void flip_cols(double* __restrict__ A, int64_t n) {
+template <typename T>
+__global__ void flip_cols(T* __restrict__ A, int64_t n) {
     const int64_t total = n * (n / 2);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = e / n, r = e - j * n;
-        const double a = A[j * n + r];
+        const T a = A[j * n + r];
         A[j * n + r] = A[(n - 1 - j) * n + r];
         A[(n - 1 - j) * n + r] = a;
     }
@@ -104,9 +105,10 @@ __global__ void flip_cols(double* __restrict__ A, int64_t n) {
 // Output column j is column perm[j] of the column-major src (ld, `rows` rows), times
 // sign[perm[j]] when sign is given; written row-major as rows x k (transpose = 0:
 // dst[r * k + j]) or k x rows (transpose = 1: dst[j * rows + r]).
-__global__ void gather_cols(const double* __restrict__ src, int64_t ld, int64_t rows,
-                            const int* __restrict__ perm, const double* __restrict__ sign,
-                            int64_t k, double* __restrict__ dst, int transpose) {
+template <typename T>
+__global__ void gather_cols(const T* __restrict__ src, int64_t ld, int64_t rows,
+                            const int* __restrict__ perm, const T* __restrict__ sign, int64_t k,
+                            T* __restrict__ dst, int transpose) {
     const int64_t total = rows * k;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -119,7 +121,7 @@ __global__ void gather_cols(const double* __restrict__ src, int64_t ld, int64_t 
             j = e - r * k;
         }
         const int p = perm[j];
-        double v = src[(int64_t)p * ld + r];
+        T v = src[(int64_t)p * ld + r];
         if (sign) v *= sign[p];
         dst[e] = v;
     }
@@ -141,9 +143,86 @@ int check_sol(cusolverStatus_t s, const char* what) {
     return TNK_OK;
 }
 
+// cuBLAS / cuSOLVER entry points by element type
+template <> struct La<double> {
+    static cublasStatus_t syrk(cublasHandle_t h, cublasOperation_t tr, int n, int k,
+                               const double* A, int lda, double* C, int ldc) {
+        const double one = 1.0, zero = 0.0;
+        return cublasDsyrk(h, CUBLAS_FILL_MODE_LOWER, tr, n, k, &one, A, lda, &zero, C, ldc);
+    }
+    static cublasStatus_t gemm(cublasHandle_t h, cublasOperation_t ta, int m, int n, int k,
+                               const double* A, int lda, const double* B, int ldb, double* C,
+                               int ldc) {
+        const double one = 1.0, zero = 0.0;
+        return cublasDgemm(h, ta, CUBLAS_OP_N, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+    }
+    static cusolverStatus_t syevd_ws(cusolverDnHandle_t h, int n, int* lw) {
+        return cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                           n, nullptr, n, nullptr, lw);
+    }
+    static cusolverStatus_t geqrf_ws(cusolverDnHandle_t h, int m, int n, int* lw) {
+        return cusolverDnDgeqrf_bufferSize(h, m, n, nullptr, m, lw);
+    }
+    static cusolverStatus_t orgqr_ws(cusolverDnHandle_t h, int m, int n, int* lw) {
+        return cusolverDnDorgqr_bufferSize(h, m, n, n, nullptr, m, nullptr, lw);
+    }
+    static cusolverStatus_t syevd(cusolverDnHandle_t h, int n, double* A, double* w,
+                                  double* work, int lw, int* info) {
+        return cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, w,
+                                work, lw, info);
+    }
+    static cusolverStatus_t geqrf(cusolverDnHandle_t h, int m, int n, double* A, double* tau,
+                                  double* work, int lw, int* info) {
+        return cusolverDnDgeqrf(h, m, n, A, m, tau, work, lw, info);
+    }
+    static cusolverStatus_t orgqr(cusolverDnHandle_t h, int m, int n, double* A,
+                                  const double* tau, double* work, int lw, int* info) {
+        return cusolverDnDorgqr(h, m, n, n, A, m, tau, work, lw, info);
+    }
+};
+template <> struct La<float> {
+    static cublasStatus_t syrk(cublasHandle_t h, cublasOperation_t tr, int n, int k,
+                               const float* A, int lda, float* C, int ldc) {
+        const float one = 1.0f, zero = 0.0f;
+        return cublasSsyrk(h, CUBLAS_FILL_MODE_LOWER, tr, n, k, &one, A, lda, &zero, C, ldc);
+    }
+    static cublasStatus_t gemm(cublasHandle_t h, cublasOperation_t ta, int m, int n, int k,
+                               const float* A, int lda, const float* B, int ldb, float* C,
+                               int ldc) {
+        const float one = 1.0f, zero = 0.0f;
+        return cublasSgemm(h, ta, CUBLAS_OP_N, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+    }
+    static cusolverStatus_t syevd_ws(cusolverDnHandle_t h, int n, int* lw) {
+        return cusolverDnSsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                           n, nullptr, n, nullptr, lw);
+    }
+    static cusolverStatus_t geqrf_ws(cusolverDnHandle_t h, int m, int n, int* lw) {
+        return cusolverDnSgeqrf_bufferSize(h, m, n, nullptr, m, lw);
+    }
+    static cusolverStatus_t orgqr_ws(cusolverDnHandle_t h, int m, int n, int* lw) {
+        return cusolverDnSorgqr_bufferSize(h, m, n, n, nullptr, m, nullptr, lw);
+    }
+    static cusolverStatus_t syevd(cusolverDnHandle_t h, int n, float* A, float* w, float* work,
+                                  int lw, int* info) {
+        return cusolverDnSsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, w,
+                                work, lw, info);
+    }
+    static cusolverStatus_t geqrf(cusolverDnHandle_t h, int m, int n, float* A, float* tau,
+                                  float* work, int lw, int* info) {
+        return cusolverDnSgeqrf(h, m, n, A, m, tau, work, lw, info);
+    }
+    static cusolverStatus_t orgqr(cusolverDnHandle_t h, int m, int n, float* A,
+                                  const float* tau, float* work, int lw, int* info) {
+        return cusolverDnSorgqr(h, m, n, n, A, m, tau, work, lw, info);
+    }
+};
+
 }  // namespace
 
-extern "C" int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes) {
+namespace {
+
+template <typename T>
+int svd_gram_ws(int64_t R, int64_t C, int64_t* bytes) {
     if (R < 1 || C < 1 || !bytes || R * C > (int64_t)1 << 30) {
         tnk::set_error("svd_gram_ws: bad argument");
         return TNK_ERR_ARG;
@@ -152,20 +231,19 @@ extern "C" int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes) {
     int rc = handles_for_current_device(&h);
     if (rc) return rc;
     Layout L;
-    rc = sizes(R, C, h, &L);
+    rc = sizes<T>(R, C, h, &L);
     if (rc) return rc;
     *bytes = (int64_t)L.total;
     return TNK_OK;
 }
 
-extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U, double* S,
-                                double* Vh, void* ws, int64_t ws_bytes, double* S_host,
-                                void* stream) {
+template <typename T>
+int svd_gram(const T* M, int64_t R, int64_t C, T* U, T* S, T* Vh, void* ws, int64_t ws_bytes,
+             double* S_host, cudaStream_t st) {
     if (!M || !U || !S || !Vh || !ws || R < 1 || C < 1 || R * C > (int64_t)1 << 30) {
         tnk::set_error("svd_gram: bad argument");
         return TNK_ERR_ARG;
     }
-    cudaStream_t st = (cudaStream_t)stream;
     cudaPointerAttributes pa;
     if (cudaPointerGetAttributes(&pa, M) != cudaSuccess || pa.type != cudaMemoryTypeDevice) {
         tnk::set_error("svd_gram: M is not device memory");
@@ -179,7 +257,7 @@ extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U
     int rc = handles_for_current_device(&h);
     if (rc) return rc;
     Layout L;
-    rc = sizes(R, C, h, &L);
+    rc = sizes<T>(R, C, h, &L);
     if (rc) return rc;
     if (ws_bytes < (int64_t)L.total || ((uintptr_t)ws & 255)) {
         tnk::set_error("svd_gram: workspace of %lld bytes (256-aligned) needed, got %lld",
@@ -190,61 +268,44 @@ extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U
         (rc = check_sol(cusolverDnSetStream(h->sol, st), "cusolverDnSetStream")))
         return rc;
     char* base = static_cast<char*>(ws);
-    double* G = reinterpret_cast<double*>(base + L.G);
-    double* Y = reinterpret_cast<double*>(base + L.Y);
-    double* w = reinterpret_cast<double*>(base + L.w);
-    double* tau = reinterpret_cast<double*>(base + L.tau);
-    double* sgn = reinterpret_cast<double*>(base + L.sign);
+    T* G = reinterpret_cast<T*>(base + L.G);
+    T* Y = reinterpret_cast<T*>(base + L.Y);
+    T* w = reinterpret_cast<T*>(base + L.w);
+    T* tau = reinterpret_cast<T*>(base + L.tau);
+    T* sgn = reinterpret_cast<T*>(base + L.sign);
     int* perm = reinterpret_cast<int*>(base + L.perm);
     int* info = reinterpret_cast<int*>(base + L.info);
-    double* work = reinterpret_cast<double*>(base + L.work);
-    const int lwork = (int)((L.total - L.work) / sizeof(double));
+    T* work = reinterpret_cast<T*>(base + L.work);
+    const int lwork = (int)((L.total - L.work) / sizeof(T));
     const bool tall = R >= C;
     const int n = (int)(tall ? C : R), m = (int)(tall ? R : C);
-    const double one = 1.0, zero = 0.0;
-    // X = M^T is C x R column-major (ld C)
-    if (tall) {
-        // G = M^T M = X X^T (C x C); Y = M V = X^T V (R x C, ld R)
-        rc = check_blas(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, (int)R,
-                                    &one, M, (int)C, &zero, G, n), "syrk");
-    } else {
-        // G = M M^T = X^T X (R x R); Y = M^T U = X U (C x R, ld C)
-        rc = check_blas(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, (int)C,
-                                    &one, M, (int)C, &zero, G, n), "syrk");
-    }
+    // X = M^T is C x R column-major (ld C): G = M^T M = X X^T (tall) or M M^T = X^T X (wide)
+    rc = check_blas(La<T>::syrk(h->blas, tall ? CUBLAS_OP_N : CUBLAS_OP_T, n,
+                                (int)(tall ? R : C), M, (int)C, G, n), "syrk");
     if (rc) return rc;
-    if ((rc = check_sol(cusolverDnDsyevd(h->sol, CUSOLVER_EIG_MODE_VECTOR,
-                                         CUBLAS_FILL_MODE_LOWER, n, G, n, w, work, lwork, info),
-                        "syevd")))
-        return rc;
+    if ((rc = check_sol(La<T>::syevd(h->sol, n, G, w, work, lwork, info), "syevd"))) return rc;
     const int threads = 256;
     auto blocks = [&](int64_t e) {
         int64_t b = (e + threads - 1) / threads;
         return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
     };
     // eigenvectors in descending order of the eigenvalue
-    flip_cols<<<blocks((int64_t)n * (n / 2)), threads, 0, st>>>(G, n);
+    flip_cols<T><<<blocks((int64_t)n * (n / 2)), threads, 0, st>>>(G, n);
     if ((rc = tnk::check_launch("flip_cols"))) return rc;
     // Y = M V (R x C, tall) or M^T U (C x R, wide), column-major with ld m
-    if (tall)
-        rc = check_blas(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, m, n, n, &one, M,
-                                    (int)C, G, n, &zero, Y, m), "gemm");
-    else
-        rc = check_blas(cublasDgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, n, &one, M,
-                                    (int)C, G, n, &zero, Y, m), "gemm");
+    rc = check_blas(La<T>::gemm(h->blas, tall ? CUBLAS_OP_T : CUBLAS_OP_N, m, n, n, M, (int)C,
+                                G, n, Y, m), "gemm");
     if (rc) return rc;
-    if ((rc = check_sol(cusolverDnDgeqrf(h->sol, m, n, Y, m, tau, work, lwork, info + 1),
-                        "geqrf")))
+    if ((rc = check_sol(La<T>::geqrf(h->sol, m, n, Y, tau, work, lwork, info + 1), "geqrf")))
         return rc;
     // d = diag(R) to the host (the sort happens there)
-    std::vector<double> d(n), s(n), sg(n);
-    if (cudaMemcpy2DAsync(d.data(), sizeof(double), Y, sizeof(double) * (m + 1), sizeof(double),
-                          n, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+    std::vector<T> d(n);
+    if (cudaMemcpy2DAsync(d.data(), sizeof(T), Y, sizeof(T) * (m + 1), sizeof(T), n,
+                          cudaMemcpyDeviceToHost, st) != cudaSuccess) {
         tnk::set_error("svd_gram: diagonal copy failed");
         return TNK_ERR_CUDA;
     }
-    if ((rc = check_sol(cusolverDnDorgqr(h->sol, m, n, n, Y, m, tau, work, lwork, info + 2),
-                        "orgqr")))
+    if ((rc = check_sol(La<T>::orgqr(h->sol, m, n, Y, tau, work, lwork, info + 2), "orgqr")))
         return rc;
     int hinfo[3] = {0, 0, 0};
     if (cudaMemcpyAsync(hinfo, info, sizeof(hinfo), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -257,35 +318,38 @@ extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U
                        hinfo[0], hinfo[1], hinfo[2], (long long)R, (long long)C);
         return TNK_ERR_CUDA;
     }
+    std::vector<T> sv(n), sg(n);
     for (int j = 0; j < n; ++j) {
-        s[j] = d[j] < 0 ? -d[j] : d[j];
-        sg[j] = s[j] > 0 ? d[j] / s[j] : 1.0;
+        sv[j] = d[j] < 0 ? -d[j] : d[j];
+        sg[j] = sv[j] > 0 ? d[j] / sv[j] : (T)1;
     }
     std::vector<int> o(n);
     std::iota(o.begin(), o.end(), 0);
-    std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return s[a] > s[b]; });
-    std::vector<double> so(n);
-    for (int j = 0; j < n; ++j) so[j] = s[o[j]];
-    if (S_host) std::copy(so.begin(), so.end(), S_host);
+    std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return sv[a] > sv[b]; });
+    std::vector<T> so(n);
+    for (int j = 0; j < n; ++j) so[j] = sv[o[j]];
+    if (S_host)
+        for (int j = 0; j < n; ++j) S_host[j] = (double)so[j];
     if (cudaMemcpyAsync(perm, o.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
-        cudaMemcpyAsync(sgn, sg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st) !=
+        cudaMemcpyAsync(sgn, sg.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
-        cudaMemcpyAsync(S, so.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st) !=
+        cudaMemcpyAsync(S, so.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st) !=
             cudaSuccess) {
         tnk::set_error("svd_gram: upload of the order failed");
         return TNK_ERR_CUDA;
     }
     if (tall) {
         // U = Q[:, o] * sign (R x n row-major); Vh = (V flipped)[:, o]^T (n x C row-major)
-        gather_cols<<<blocks((int64_t)R * n), threads, 0, st>>>(Y, m, R, perm, sgn, n, U, 0);
-        gather_cols<<<blocks((int64_t)C * n), threads, 0, st>>>(G, n, C, perm, nullptr, n, Vh,
-                                                                1);
+        gather_cols<T><<<blocks((int64_t)R * n), threads, 0, st>>>(Y, m, R, perm, sgn, n, U, 0);
+        gather_cols<T><<<blocks((int64_t)C * n), threads, 0, st>>>(G, n, C, perm, nullptr, n,
+                                                                   Vh, 1);
     } else {
         // U = (U flipped)[:, o] (R x n row-major); Vh = (Q[:, o] * sign)^T (n x C row-major)
-        gather_cols<<<blocks((int64_t)R * n), threads, 0, st>>>(G, n, R, perm, nullptr, n, U,
-                                                                0);
-        gather_cols<<<blocks((int64_t)C * n), threads, 0, st>>>(Y, m, C, perm, sgn, n, Vh, 1);
+        gather_cols<T><<<blocks((int64_t)R * n), threads, 0, st>>>(G, n, R, perm, nullptr, n, U,
+                                                                   0);
+        gather_cols<T><<<blocks((int64_t)C * n), threads, 0, st>>>(Y, m, C, perm, sgn, n, Vh,
+                                                                   1);
     }
     rc = tnk::check_launch("gather_cols");
     if (rc) return rc;
@@ -294,4 +358,26 @@ extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U
         return TNK_ERR_CUDA;
     }
     return TNK_OK;
+}
+
+}  // namespace
+
+extern "C" int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes) {
+    return svd_gram_ws<double>(R, C, bytes);
+}
+
+extern "C" int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U, double* S,
+                                double* Vh, void* ws, int64_t ws_bytes, double* S_host,
+                                void* stream) {
+    return svd_gram<double>(M, R, C, U, S, Vh, ws, ws_bytes, S_host, (cudaStream_t)stream);
+}
+
+extern "C" int tnk_svd_gram_ws_f32(int64_t R, int64_t C, int64_t* bytes) {
+    return svd_gram_ws<float>(R, C, bytes);
+}
+
+extern "C" int tnk_svd_gram_f32(const float* M, int64_t R, int64_t C, float* U, float* S,
+                                float* Vh, void* ws, int64_t ws_bytes, double* S_host,
+                                void* stream) {
+    return svd_gram<float>(M, R, C, U, S, Vh, ws, ws_bytes, S_host, (cudaStream_t)stream);
 }

@@ -24,6 +24,27 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Transposed warp reduction of G (16 or 32) values per lane: on return, lane l holds the sum
+// over the warp's lanes of their v[l % G] (G = 16: both half-warps added at the end). Each step
+// sends the half of the values a lane does not keep to its partner and adds the half it
+// receives: G - 1 shuffle-adds instead of 5 per value, in a fixed order (deterministic).
+template <int G>
+__device__ __forceinline__ double warp_transpose_sum(double (&v)[G]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int s = G / 2; s >= 1; s >>= 1) {
+        const bool up = (lane & s) != 0;
+#pragma unroll
+        for (int i = 0; i < s; ++i) {
+            const double keep = up ? v[i + s] : v[i];
+            const double send = up ? v[i] : v[i + s];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+        }
+    }
+    if (G == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 16);
+    return v[0];
+}
+
 // Block-wide sum; result valid in thread 0. `sh` holds NT/32 doubles.
 __device__ __forceinline__ double block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -268,11 +289,15 @@ __global__ void __launch_bounds__(CG_NT) cgs_kernel(const T* __restrict__ V, int
     if (!DOT && !NRM) return;
     const int lane = t & 31, wid = t >> 5;
     if (DOT) {
+        constexpr int G = NACC < 32 ? NACC : 32;
 #pragma unroll
-        for (int j = 0; j < NACC; ++j) {
-            if (j >= nv) break;
-            const double s = warp_sum((double)acc[j]);
-            if (lane == 0) sh[wid][j] = s;
+        for (int g = 0; g < NACC / G; ++g) {
+            double v[G];
+#pragma unroll
+            for (int i = 0; i < G; ++i) v[i] = (double)acc[g * G + i];
+            const double s = warp_transpose_sum<G>(v);
+            const int row = g * G + (lane % G);
+            if (lane < G && row < nv) sh[wid][row] = s;
         }
     }
     if (NRM) {

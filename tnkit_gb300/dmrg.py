@@ -9,7 +9,9 @@ environments and MPS tensors stay on the device.
 
 Options keep the reference's names and defaults where this backend implements them
 (`n_sweeps`, `tol`, `rtol`, `eig_tol`, `eig`, `warm_start`, `max_iter`, `restart_m`, `restart_k`,
-`seed`, `init_mps`, `charge`, `verbose`, `sites`, `expand`, `trunc`, `backend`, `precision`). The
+`seed`, `init_mps`, `charge`, `verbose`, `sites`, `expand`, `trunc`, `backend`, `precision`;
+`mixed_schedule='sweep'` solves the opening sweeps on the tensor cores alone and polishes only
+the last `polish_sweeps`). The
 block default of the reference expands the subspace in the opening sweeps; subspace expansion is
 not part of this backend, so `expand` must be 0 (or None, read as 0) and other values raise.
 """
@@ -53,6 +55,10 @@ class DMRGOptions:
                                     # (tensor-core Lanczos, then an FP64 / float-float polish)
     mixed_tol_lo: float = 1e-4
     polish: int = 2                  # FP64 polish restarts allowed after the mixed stage
+    mixed_schedule: str = "bond"     # 'bond': tensor-core stage then polish at every bond;
+                                     # 'sweep': tensor-core solves alone in all but the last
+                                     # `polish_sweeps` sweeps, the per-bond mixed solve there
+    polish_sweeps: int = 2
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
     svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
@@ -110,6 +116,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     o = _resolve(options, kw)
     if o.precision not in ("f64", "ff", "mixed", "mixed-ff"):
         raise ValueError("precision must be 'f64', 'ff', 'mixed' or 'mixed-ff'")
+    if o.mixed_schedule not in ("bond", "sweep"):
+        raise ValueError("mixed_schedule must be 'bond' or 'sweep'")
     if o.sites != 2:
         raise NotImplementedError("this backend runs two-site DMRG (sites=2)")
     if o.trunc != "svd":
@@ -168,7 +176,10 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     def eigsolve(theta: BlockTensor, i: int):
         nonlocal mv_calls
         hi = "ff" if o.precision in ("ff", "mixed-ff") else "f64"
-        op = ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1], R[i + 2], precision=hi)
+        tc_only = (o.precision in ("mixed", "mixed-ff") and o.mixed_schedule == "sweep"
+                   and sweep_no["n"] < o.n_sweeps - max(0, o.polish_sweeps))
+        op = None if tc_only else ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1],
+                                                      R[i + 2], precision=hi)
         n = theta.layout.size
         mi = o.max_iter if o.max_iter is not None else min(n, max(200, 4 * chi))
         need = (o.restart_m + 1) * n
@@ -182,12 +193,12 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
             e, x, info = mixed_ground(theta.layout, L[i], W[i], W[i + 1], R[i + 2], op, v0,
                                       tol=o.eig_tol, max_iter=mi, m=o.restart_m,
                                       k=o.restart_k, tol_lo=o.mixed_tol_lo, basis=Vb,
-                                      counts=counts)
+                                      counts=counts, tc_only=tc_only)
         else:
             e, x, info = lanczos_ground_restart(op, v0, tol=o.eig_tol, max_iter=mi,
                                                 m=o.restart_m, k=o.restart_k, basis=Vb)
             counts["hi"] += op.calls
-        mv_calls += info.get("matvecs", op.calls)
+        mv_calls += info["matvecs"] if "matvecs" in info else op.calls
         return e, BlockTensor(theta.layout, x)
 
     def solve_block(i: int, right: bool):
@@ -217,7 +228,9 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
 
     prev_E, E = None, None
     sweep = 0
+    sweep_no = {"n": 0}
     for sweep in range(o.n_sweeps):
+        sweep_no["n"] = sweep
         sync()
         ts = time.perf_counter()
         alphas.append(0.0)

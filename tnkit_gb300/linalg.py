@@ -139,21 +139,24 @@ def _concurrent() -> _Concurrent:
 
 
 def _svd_gram_native(M: torch.Tensor):
-    """U, S, Vh (and S on the host) of one real FP64 CUDA block by tnk_svd_gram_f64: the same
-    factorisation as _svd_gram in one library call that holds no interpreter lock."""
+    """U, S, Vh (and S on the host) of one real CUDA block (FP64, or FP32) by
+    tnk_svd_gram_f64 / _f32: the same factorisation as _svd_gram in one library call that holds
+    no interpreter lock."""
     R, Cc = M.shape
     k = min(R, Cc)
     lib = _lib.lib()
+    f32 = M.dtype == torch.float32
+    ws_fn, fn = ((lib.tnk_svd_gram_ws_f32, lib.tnk_svd_gram_f32) if f32 else
+                 (lib.tnk_svd_gram_ws_f64, lib.tnk_svd_gram_f64))
     nb = C.c_int64()
-    _lib.check(lib.tnk_svd_gram_ws_f64(R, Cc, C.byref(nb)), "svd_gram_ws")
+    _lib.check(ws_fn(R, Cc, C.byref(nb)), "svd_gram_ws")
     ws = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=M.device)
-    U = torch.empty((R, k), dtype=torch.float64, device=M.device)
-    S = torch.empty(k, dtype=torch.float64, device=M.device)
-    Vh = torch.empty((k, Cc), dtype=torch.float64, device=M.device)
+    U = torch.empty((R, k), dtype=M.dtype, device=M.device)
+    S = torch.empty(k, dtype=M.dtype, device=M.device)
+    Vh = torch.empty((k, Cc), dtype=M.dtype, device=M.device)
     s_host = np.empty(k, dtype=np.float64)
-    _lib.check(lib.tnk_svd_gram_f64(M.data_ptr(), R, Cc, U.data_ptr(), S.data_ptr(),
-                                    Vh.data_ptr(), ws.data_ptr(), ws.numel(),
-                                    s_host.ctypes.data, _lib.stream_ptr()), "svd_gram")
+    _lib.check(fn(M.data_ptr(), R, Cc, U.data_ptr(), S.data_ptr(), Vh.data_ptr(),
+                  ws.data_ptr(), ws.numel(), s_host.ctypes.data, _lib.stream_ptr()), "svd_gram")
     return U, S, Vh, s_host
 
 
@@ -235,7 +238,19 @@ def _svd_gram_host(M: torch.Tensor):
     dev = M.device
     return (torch.as_tensor(np.ascontiguousarray(U), device=dev),
             torch.as_tensor(S, device=dev),
-            torch.as_tensor(np.ascontiguousarray(Vh), device=dev), S)
+            torch.as_tensor(np.ascontiguousarray(Vh), device=dev), S.astype(np.float64))
+
+
+def _with_fp64_fallback(fn):
+    """fn on an FP32 block, refactored in FP64 (results cast back) when the FP32 eigensolver
+    does not converge: a Gram spectrum spanning ~18 decades can defeat it."""
+    def run(M):
+        try:
+            return fn(M)
+        except (_lib.TnkError, np.linalg.LinAlgError):
+            U, S, Vh, h = fn(M.double())
+            return U.float(), S.float(), Vh.float(), h
+    return run
 
 
 def _svd_gram(M: torch.Tensor):
@@ -263,22 +278,30 @@ def _svd_gram(M: torch.Tensor):
 
 
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
-                  method: str = "svd", normalize: bool = True, host: str = "auto"):
+                  method: str = "svd", normalize: bool = True, host: str = "auto",
+                  dtype=torch.float64):
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
     With method='gram', `host` chooses where the sectors are factored: 'auto' (split between the
-    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only).
+    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only); dtype=float32
+    factors the blocks in FP32 (results returned in FP64; a sector whose FP32 eigensolver does
+    not converge is redone in FP64). Inside a DMRG sweep near convergence the FP32 Gram matrix
+    loses the small singular values and the environments built on its factors drift, so the
+    sweep driver does not use it.
     Returns U, S (device vector, normalised when scale != 'none'), Vh, disc (absolute)."""
     if host not in ("auto", "never", "always"):
         raise ValueError("host must be 'auto', 'never' or 'always'")
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
     lr, lc = m.layout.legs
-    blocks = list(_blocks(m))
+    low = dtype == torch.float32 and m.data.dtype == torch.float64
+    if low and method != "gram":
+        raise ValueError("an FP32 truncation needs method='gram'")
+    blocks = list(_blocks(BlockTensor(m.layout, m.data.float()) if low else m))
     if method == "gram":
         fn = _svd_gram_native if (m.data.is_cuda and m.data.dtype == torch.float64) \
-            else (lambda M: _svd_gram(M) + (None,))
+            else (lambda M: tuple(_svd_gram(M)) + (None,))
     elif method == "svd":
         fn = lambda M: tuple(torch.linalg.svd(M, full_matrices=False, driver=driver)) + (None,)
     else:
@@ -290,6 +313,8 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
             on_host = _assign_sectors([tuple(M.shape) for M in mats], blas is not None) \
                 if host == "auto" else [True] * len(mats)
             fns = [_svd_gram_host if h else _svd_gram_native for h in on_host]
+            if low:
+                fns = [_with_fp64_fallback(f) for f in fns]
             if any(on_host) and blas is not None:
                 prev = blas[1]()
                 # a quarter of the cores: with more, the truncation of a chi=1024 mid bond is
@@ -302,9 +327,12 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
             else:
                 facs = _concurrent().map(fns, mats, m.data.device)
         else:
-            facs = _concurrent().map(fn, mats, m.data.device)
+            facs = _concurrent().map(_with_fp64_fallback(fn) if low else fn, mats,
+                                     m.data.device)
     else:
-        facs = [fn(M) for M in mats]
+        facs = [(_with_fp64_fallback(fn) if low else fn)(M) for M in mats]
+    if low:
+        facs = [(U.double(), S.double(), Vh.double(), h) for U, S, Vh, h in facs]
     parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
     if not parts:
         raise ValueError("the matrix has no allowed blocks")

@@ -122,14 +122,29 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
                  R: BlockTensor, op64, v0: torch.Tensor, tol: float = 1e-9,
                  max_iter: int = 200, m: int = 40, k: int = 10, tol_lo: float = 1e-4,
                  basis=None, counts=None, passes: int = 3, polish: Optional[int] = None,
-                 switch: float = 10.0):
+                 switch: float = 10.0, tc_only: bool = False):
     """Lowest eigenpair of H_eff: tensor-core Lanczos to tol_lo, then FP64 Lanczos to tol.
 
     The warm start's FP64 residual is checked first (one FP64 matvec): a start already within
     `switch` * tol_lo of convergence -- late sweeps -- goes straight to the FP64 solve, which
     needs few iterations there and which the tensor-core operator (relative accuracy ~1e-6)
     could not improve; a start farther out -- the opening sweeps, bond growth -- spends its
-    many iterations on the tensor cores."""
+    many iterations on the tensor cores.
+
+    tc_only=True runs the tensor-core stage alone (to tol_lo, or until its residual stalls) and
+    returns its vector: the local solve of the opening sweeps of the 'sweep' schedule."""
+    if tc_only:
+        op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
+        e_lo, x32, info_lo = lanczos_ground_restart(
+            _F32Vectors(op_lo, v0.numel(), v0.device), v0, tol=tol_lo, max_iter=max_iter, m=m,
+            k=k, basis=basis, stall=8, dtype=torch.float32)
+        op_lo.check_device_error()
+        if counts is not None:
+            counts["lo"] = counts.get("lo", 0) + op_lo.calls
+        x = x32.double()
+        x = x / torch.linalg.vector_norm(x)
+        return e_lo, x, {"iters": info_lo["iters"], "converged": info_lo["converged"],
+                         "e_lo": e_lo, "n_lo": op_lo.calls, "n_hi": 0, "matvecs": op_lo.calls}
     c0 = getattr(op64, "calls", 0)
     th0, r0 = _fp64_residual(op64, v0)
     n_lo = 0
