@@ -344,6 +344,14 @@ int tnk_zaxpby_f64(const double* x, double* y, int64_t n, const double* sa, doub
 int tnk_svd_gram_ws_f64(int64_t R, int64_t C, int64_t* bytes);
 int tnk_svd_gram_f64(const double* M, int64_t R, int64_t C, double* U, double* S, double* Vh,
                      void* ws, int64_t ws_bytes, double* S_host, void* stream);
+/* The same with the side the sweep keeps canonical taken straight from its own Gram matrix
+ * (no QR): orth = 1 gives U orthonormal (eigenvectors of M M^T) and Vh = diag(1/S) U^T M,
+ * orth = 2 gives Vh orthonormal (eigenvectors of M^T M) and U = M V diag(1/S), with
+ * S = sqrt(max(lambda, 0)) descending; orth = 0 is tnk_svd_gram_f64. */
+int tnk_svd_gram_ws2_f64(int64_t R, int64_t C, int32_t orth, int64_t* bytes);
+int tnk_svd_gram2_f64(const double* M, int64_t R, int64_t C, int32_t orth, double* U,
+                      double* S, double* Vh, void* ws, int64_t ws_bytes, double* S_host,
+                      void* stream);
 /* The same in FP32 (S_host still double): the truncations of the opening sweeps of the mixed
  * schedule, whose local solves are only tensor-core accurate. */
 int tnk_svd_gram_ws_f32(int64_t R, int64_t C, int64_t* bytes);

@@ -136,3 +136,31 @@ def test_fp32_truncation_close_to_fp64():
     assert float((S3 - S).abs().max()) <= 1e-5 * float(S.max())
     Ud = to_dense_np(U3.layout, U3.data.cpu().numpy())
     assert np.abs(Ud.T @ Ud - np.eye(Ud.shape[1])).max() <= 1e-5
+
+
+@pytest.mark.parametrize("scale", ["right", "left"])
+@pytest.mark.parametrize("host", ["never", "always"])
+def test_direct_gram_side_matches_qr_form(scale, host):
+    """The canonical side straight from its own Gram matrix (no QR) against the reference's
+    QR form: the same kept values and bond, an orthonormal kept side, the same truncated
+    matrix."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(12)
+    a = Leg((-1, 1), (90, 120), 1)
+    b = Leg((-1, 1), (100, 110), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size) * np.repeat(10.0 ** -np.linspace(0, 3, lay.nblocks),
+                                                   [int(x) for x in lay.sizes])
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    d = lambda t: to_dense_np(t.layout, t.data.cpu().numpy())
+    U, S, V, disc = LA.truncated_svd(m, 80, scale=scale, method="gram", host=host)
+    U0, S0, V0, disc0 = LA.truncated_svd(m, 80, scale=scale, method="gram", host=host,
+                                         gram_qr=True)
+    assert U.layout.legs == U0.layout.legs
+    assert float((S - S0).abs().max()) <= 1e-10 * float(S0.max())
+    assert abs(disc - disc0) <= 1e-9 * max(disc0, 1e-300)
+    iso = d(U) if scale == "right" else d(V).T
+    assert np.abs(iso.T @ iso - np.eye(iso.shape[1])).max() <= 1e-12
+    assert np.abs(d(U) @ d(V) - d(U0) @ d(V0)).max() <= 1e-10

@@ -96,6 +96,8 @@ _SIGS = {
     "tnk_scale_div_f32": ([_P, _P, _I64, _P, _D, _P], C.c_int),
     "tnk_svd_gram_ws_f64": ([_I64, _I64, _P], C.c_int),
     "tnk_svd_gram_f64": ([_P, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P], C.c_int),
+    "tnk_svd_gram_ws2_f64": ([_I64, _I64, _I32, _P], C.c_int),
+    "tnk_svd_gram2_f64": ([_P, _I64, _I64, _I32, _P, _P, _P, _P, _I64, _P, _P], C.c_int),
     "tnk_svd_gram_ws_f32": ([_I64, _I64, _P], C.c_int),
     "tnk_svd_gram_f32": ([_P, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P], C.c_int),
     "tnk_apply_two_site_f64_noalloc": ([_P, _P, _P, _P, _P, _P], C.c_int),

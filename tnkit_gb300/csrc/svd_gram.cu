@@ -16,6 +16,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cmath>
 #include <numeric>
 #include <vector>
 
@@ -63,12 +64,15 @@ inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 template <typename T> struct La;
 
 template <typename T>
-int sizes(int64_t R, int64_t C, Handles* h, Layout* L) {
-    const int64_t n = R < C ? R : C, m = R < C ? C : R;
+int sizes(int64_t R, int64_t C, Handles* h, Layout* L, int orth = 0) {
+    // orth 0: the smaller Gram matrix; orth 1 / 2: the R x R / C x C one (see svd_gram_direct)
+    const int64_t n = orth == 1 ? R : orth == 2 ? C : (R < C ? R : C);
+    const int64_t m = orth ? (R < C ? R : C) : (R < C ? C : R);
     int lw_ev = 0, lw_qr = 0, lw_or = 0;
     if (La<T>::syevd_ws(h->sol, (int)n, &lw_ev) != CUSOLVER_STATUS_SUCCESS ||
-        La<T>::geqrf_ws(h->sol, (int)m, (int)n, &lw_qr) != CUSOLVER_STATUS_SUCCESS ||
-        La<T>::orgqr_ws(h->sol, (int)m, (int)n, &lw_or) != CUSOLVER_STATUS_SUCCESS) {
+        (!orth && (La<T>::geqrf_ws(h->sol, (int)m, (int)n, &lw_qr) != CUSOLVER_STATUS_SUCCESS ||
+                   La<T>::orgqr_ws(h->sol, (int)m, (int)n, &lw_or) !=
+                       CUSOLVER_STATUS_SUCCESS))) {
         tnk::set_error("svd_gram: cuSOLVER workspace query failed (R=%lld, C=%lld)",
                        (long long)R, (long long)C);
         return TNK_ERR_CUDA;
@@ -77,7 +81,7 @@ int sizes(int64_t R, int64_t C, Handles* h, Layout* L) {
     const size_t es = sizeof(T);
     size_t o = 0;
     L->G = o; o += up(es * n * n);
-    L->Y = o; o += up(es * m * n);
+    L->Y = o; o += up(es * (orth ? R * C : m * n));
     L->w = o; o += up(es * n);
     L->tau = o; o += up(es * n);
     L->sign = o; o += up(es * n);
@@ -222,8 +226,8 @@ template <> struct La<float> {
 namespace {
 
 template <typename T>
-int svd_gram_ws(int64_t R, int64_t C, int64_t* bytes) {
-    if (R < 1 || C < 1 || !bytes || R * C > (int64_t)1 << 30) {
+int svd_gram_ws(int64_t R, int64_t C, int64_t* bytes, int orth = 0) {
+    if (R < 1 || C < 1 || !bytes || R * C > (int64_t)1 << 30 || orth < 0 || orth > 2) {
         tnk::set_error("svd_gram_ws: bad argument");
         return TNK_ERR_ARG;
     }
@@ -231,16 +235,109 @@ int svd_gram_ws(int64_t R, int64_t C, int64_t* bytes) {
     int rc = handles_for_current_device(&h);
     if (rc) return rc;
     Layout L;
-    rc = sizes<T>(R, C, h, &L);
+    rc = sizes<T>(R, C, h, &L, orth);
     if (rc) return rc;
     *bytes = (int64_t)L.total;
     return TNK_OK;
 }
 
+// orth = 1: U orthonormal from the eigenvectors of M M^T, Vh = diag(1/S) U^T M; orth = 2: Vh
+// orthonormal from the eigenvectors of M^T M, U = M V diag(1/S); S = sqrt(max(lambda, 0)) in
+// descending order. No QR: the factor the sweep keeps canonical comes straight from its Gram
+// matrix, the other carries S and is the exact projection.
+template <typename T>
+int svd_gram_direct(const T* M, int64_t R, int64_t C, T* U, T* S, T* Vh, char* base,
+                    const Layout& L, Handles* h, int orth, double* S_host, cudaStream_t st) {
+    T* G = reinterpret_cast<T*>(base + L.G);
+    T* Y = reinterpret_cast<T*>(base + L.Y);
+    T* w = reinterpret_cast<T*>(base + L.w);
+    T* inv = reinterpret_cast<T*>(base + L.sign);
+    int* perm = reinterpret_cast<int*>(base + L.perm);
+    int* info = reinterpret_cast<int*>(base + L.info);
+    T* work = reinterpret_cast<T*>(base + L.work);
+    const int lwork = (int)((L.total - L.work) / sizeof(T));
+    const int g = orth == 1 ? (int)R : (int)C;          // Gram order
+    const int k = (int)(R < C ? R : C);                 // rank kept
+    // X = M^T is C x R column-major (ld C): M M^T = X^T X, M^T M = X X^T
+    int rc = check_blas(La<T>::syrk(h->blas, orth == 1 ? CUBLAS_OP_T : CUBLAS_OP_N, g,
+                                    orth == 1 ? (int)C : (int)R, M, (int)C, G, g), "syrk");
+    if (rc) return rc;
+    if ((rc = check_sol(La<T>::syevd(h->sol, g, G, w, work, lwork, info), "syevd"))) return rc;
+    const int threads = 256;
+    auto blocks = [&](int64_t e) {
+        int64_t b = (e + threads - 1) / threads;
+        return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+    };
+    flip_cols<T><<<blocks((int64_t)g * (g / 2)), threads, 0, st>>>(G, g);
+    if ((rc = tnk::check_launch("flip_cols"))) return rc;
+    // the other factor, unscaled: orth 1: Z = X U (C x k, ld C) = (U^T M)^T; orth 2: Y = X^T V
+    // (R x k, ld R) = M V
+    if (orth == 1)
+        rc = check_blas(La<T>::gemm(h->blas, CUBLAS_OP_N, (int)C, k, (int)R, M, (int)C, G, g, Y,
+                                    (int)C), "gemm");
+    else
+        rc = check_blas(La<T>::gemm(h->blas, CUBLAS_OP_T, (int)R, k, (int)C, M, (int)C, G, g, Y,
+                                    (int)R), "gemm");
+    if (rc) return rc;
+    std::vector<T> lam(g);
+    int hinfo = 0;
+    if (cudaMemcpyAsync(lam.data(), w, sizeof(T) * g, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        tnk::set_error("svd_gram: %s", cudaGetErrorString(cudaGetLastError()));
+        return TNK_ERR_CUDA;
+    }
+    if (hinfo) {
+        tnk::set_error("svd_gram: cuSOLVER info syevd=%d (R=%lld, C=%lld)", hinfo,
+                       (long long)R, (long long)C);
+        return TNK_ERR_CUDA;
+    }
+    std::vector<T> sv(k), iv(k);
+    std::vector<int> id(k);
+    for (int j = 0; j < k; ++j) {
+        const T l = lam[g - 1 - j];
+        sv[j] = l > 0 ? (T)std::sqrt((double)l) : (T)0;
+        iv[j] = sv[j] > 0 ? (T)1 / sv[j] : (T)0;
+        id[j] = j;
+    }
+    if (S_host)
+        for (int j = 0; j < k; ++j) S_host[j] = (double)sv[j];
+    if (cudaMemcpyAsync(perm, id.data(), sizeof(int) * k, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(inv, iv.data(), sizeof(T) * k, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(S, sv.data(), sizeof(T) * k, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess) {
+        tnk::set_error("svd_gram: upload of the scales failed");
+        return TNK_ERR_CUDA;
+    }
+    if (orth == 1) {
+        // U = eigenvectors (R x k row-major); Vh[j, c] = Z[c + j C] / S_j
+        gather_cols<T><<<blocks((int64_t)R * k), threads, 0, st>>>(G, g, R, perm, nullptr, k, U,
+                                                                   0);
+        gather_cols<T><<<blocks((int64_t)C * k), threads, 0, st>>>(Y, C, C, perm, inv, k, Vh,
+                                                                   1);
+    } else {
+        // U[r, j] = Y[r + j R] / S_j; Vh = V^T (k x C row-major)
+        gather_cols<T><<<blocks((int64_t)R * k), threads, 0, st>>>(Y, R, R, perm, inv, k, U, 0);
+        gather_cols<T><<<blocks((int64_t)C * k), threads, 0, st>>>(G, g, C, perm, nullptr, k,
+                                                                   Vh, 1);
+    }
+    rc = tnk::check_launch("gather_cols");
+    if (rc) return rc;
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        tnk::set_error("svd_gram: %s", cudaGetErrorString(cudaGetLastError()));
+        return TNK_ERR_CUDA;
+    }
+    return TNK_OK;
+}
+
 template <typename T>
 int svd_gram(const T* M, int64_t R, int64_t C, T* U, T* S, T* Vh, void* ws, int64_t ws_bytes,
-             double* S_host, cudaStream_t st) {
-    if (!M || !U || !S || !Vh || !ws || R < 1 || C < 1 || R * C > (int64_t)1 << 30) {
+             double* S_host, cudaStream_t st, int orth = 0) {
+    if (!M || !U || !S || !Vh || !ws || R < 1 || C < 1 || R * C > (int64_t)1 << 30 || orth < 0 ||
+        orth > 2) {
         tnk::set_error("svd_gram: bad argument");
         return TNK_ERR_ARG;
     }
@@ -257,7 +354,7 @@ int svd_gram(const T* M, int64_t R, int64_t C, T* U, T* S, T* Vh, void* ws, int6
     int rc = handles_for_current_device(&h);
     if (rc) return rc;
     Layout L;
-    rc = sizes<T>(R, C, h, &L);
+    rc = sizes<T>(R, C, h, &L, orth);
     if (rc) return rc;
     if (ws_bytes < (int64_t)L.total || ((uintptr_t)ws & 255)) {
         tnk::set_error("svd_gram: workspace of %lld bytes (256-aligned) needed, got %lld",
@@ -268,6 +365,8 @@ int svd_gram(const T* M, int64_t R, int64_t C, T* U, T* S, T* Vh, void* ws, int6
         (rc = check_sol(cusolverDnSetStream(h->sol, st), "cusolverDnSetStream")))
         return rc;
     char* base = static_cast<char*>(ws);
+    if (orth == 1 || orth == 2)
+        return svd_gram_direct<T>(M, R, C, U, S, Vh, base, L, h, orth, S_host, st);
     T* G = reinterpret_cast<T*>(base + L.G);
     T* Y = reinterpret_cast<T*>(base + L.Y);
     T* w = reinterpret_cast<T*>(base + L.w);
@@ -380,4 +479,14 @@ extern "C" int tnk_svd_gram_f32(const float* M, int64_t R, int64_t C, float* U, 
                                 float* Vh, void* ws, int64_t ws_bytes, double* S_host,
                                 void* stream) {
     return svd_gram<float>(M, R, C, U, S, Vh, ws, ws_bytes, S_host, (cudaStream_t)stream);
+}
+
+extern "C" int tnk_svd_gram_ws2_f64(int64_t R, int64_t C, int32_t orth, int64_t* bytes) {
+    return svd_gram_ws<double>(R, C, bytes, orth);
+}
+
+extern "C" int tnk_svd_gram2_f64(const double* M, int64_t R, int64_t C, int32_t orth, double* U,
+                                 double* S, double* Vh, void* ws, int64_t ws_bytes,
+                                 double* S_host, void* stream) {
+    return svd_gram<double>(M, R, C, U, S, Vh, ws, ws_bytes, S_host, (cudaStream_t)stream, orth);
 }

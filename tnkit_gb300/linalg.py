@@ -138,25 +138,31 @@ def _concurrent() -> _Concurrent:
     return _CONC
 
 
-def _svd_gram_native(M: torch.Tensor):
+def _svd_gram_native(M: torch.Tensor, orth: int = 0):
     """U, S, Vh (and S on the host) of one real CUDA block (FP64, or FP32) by
     tnk_svd_gram_f64 / _f32: the same factorisation as _svd_gram in one library call that holds
-    no interpreter lock."""
+    no interpreter lock. orth = 1 / 2 (FP64): the U / Vh side straight from its own Gram matrix,
+    no QR (tnk_svd_gram2_f64)."""
     R, Cc = M.shape
     k = min(R, Cc)
     lib = _lib.lib()
     f32 = M.dtype == torch.float32
-    ws_fn, fn = ((lib.tnk_svd_gram_ws_f32, lib.tnk_svd_gram_f32) if f32 else
-                 (lib.tnk_svd_gram_ws_f64, lib.tnk_svd_gram_f64))
     nb = C.c_int64()
-    _lib.check(ws_fn(R, Cc, C.byref(nb)), "svd_gram_ws")
+    if orth and not f32:
+        _lib.check(lib.tnk_svd_gram_ws2_f64(R, Cc, orth, C.byref(nb)), "svd_gram_ws")
+        call = lambda *a: lib.tnk_svd_gram2_f64(a[0], R, Cc, orth, *a[1:])
+    else:
+        ws_fn, fn = ((lib.tnk_svd_gram_ws_f32, lib.tnk_svd_gram_f32) if f32 else
+                     (lib.tnk_svd_gram_ws_f64, lib.tnk_svd_gram_f64))
+        _lib.check(ws_fn(R, Cc, C.byref(nb)), "svd_gram_ws")
+        call = lambda *a: fn(a[0], R, Cc, *a[1:])
     ws = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=M.device)
     U = torch.empty((R, k), dtype=M.dtype, device=M.device)
     S = torch.empty(k, dtype=M.dtype, device=M.device)
     Vh = torch.empty((k, Cc), dtype=M.dtype, device=M.device)
     s_host = np.empty(k, dtype=np.float64)
-    _lib.check(fn(M.data_ptr(), R, Cc, U.data_ptr(), S.data_ptr(), Vh.data_ptr(),
-                  ws.data_ptr(), ws.numel(), s_host.ctypes.data, _lib.stream_ptr()), "svd_gram")
+    _lib.check(call(M.data_ptr(), U.data_ptr(), S.data_ptr(), Vh.data_ptr(), ws.data_ptr(),
+                    ws.numel(), s_host.ctypes.data, _lib.stream_ptr()), "svd_gram")
     return U, S, Vh, s_host
 
 
@@ -213,11 +219,27 @@ def _assign_sectors(shapes, host_ok: bool):
     return out
 
 
-def _svd_gram_host(M: torch.Tensor):
+def _svd_gram_host(M: torch.Tensor, orth: int = 0):
     """The Gram factorisation of one block on the host (numpy / LAPACK), results back on the
-    device: the reference's numpy branch (tnkit/blocks.py:1345-1377)."""
+    device: the reference's numpy branch (tnkit/blocks.py:1345-1377), or with orth = 1 / 2 the
+    canonical side straight from its own Gram matrix (as _svd_gram_native)."""
     Mh = M.cpu().numpy()
     R, Cc = Mh.shape
+    dev = M.device
+    if orth:
+        k = min(R, Cc)
+        lam, E = np.linalg.eigh(Mh @ Mh.T if orth == 1 else Mh.T @ Mh)
+        lam, E = lam[::-1][:k], E[:, ::-1][:, :k]
+        S = np.sqrt(np.maximum(lam, 0.0))
+        inv = np.where(S > 0, 1.0 / np.where(S > 0, S, 1.0), 0.0)
+        if orth == 1:
+            U, Vh = E, (E.T @ Mh) * inv[:, None]
+        else:
+            U, Vh = (Mh @ E) * inv[None, :], E.T
+        # explicit copies: a (n, 1) view with a negative stride counts as contiguous
+        return (torch.as_tensor(U.copy(order="C"), device=dev),
+                torch.as_tensor(S.copy(), device=dev),
+                torch.as_tensor(Vh.copy(order="C"), device=dev), S.astype(np.float64))
     if R >= Cc:
         _, V = np.linalg.eigh(Mh.T @ Mh)
         V = V[:, ::-1]
@@ -235,10 +257,9 @@ def _svd_gram_host(M: torch.Tensor):
         U, Vh = Q, V[:, o].T
     else:
         U, Vh = Uh[:, o], Q.T
-    dev = M.device
-    return (torch.as_tensor(np.ascontiguousarray(U), device=dev),
-            torch.as_tensor(S, device=dev),
-            torch.as_tensor(np.ascontiguousarray(Vh), device=dev), S.astype(np.float64))
+    return (torch.as_tensor(U.copy(order="C"), device=dev),
+            torch.as_tensor(S.copy(), device=dev),
+            torch.as_tensor(Vh.copy(order="C"), device=dev), S.astype(np.float64))
 
 
 def _with_fp64_fallback(fn):
@@ -279,12 +300,16 @@ def _svd_gram(M: torch.Tensor):
 
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
                   method: str = "svd", normalize: bool = True, host: str = "auto",
-                  dtype=torch.float64):
+                  dtype=torch.float64, gram_qr: bool = False):
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
     With method='gram', `host` chooses where the sectors are factored: 'auto' (split between the
-    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only); dtype=float32
+    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only). For scale
+    'right' / 'left' the side the sweep keeps canonical (U / Vh) of a near-square sector comes
+    straight from its own Gram matrix and the other is the exact projection, with S the square
+    roots of the Gram eigenvalues; gram_qr=True keeps the reference's form (the smaller Gram
+    matrix, then a QR) everywhere. dtype=float32
     factors the blocks in FP32 (results returned in FP64; a sector whose FP32 eigensolver does
     not converge is redone in FP64). Inside a DMRG sweep near convergence the FP32 Gram matrix
     loses the small singular values and the environments built on its factors drift, so the
@@ -307,12 +332,21 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     else:
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
     mats = [M for _, _, M in blocks]
+    if method == "gram" and not gram_qr and not low and scale in ("right", "left"):
+        def pick(M, base):
+            R, Cc = M.shape
+            o = 1 if scale == "right" and R <= 1.25 * Cc else \
+                2 if scale == "left" and Cc <= 1.25 * R else 0
+            return (lambda X: base(X, o)) if o else base
+    else:
+        pick = lambda M, base: base
     if len(mats) > 1 and m.data.is_cuda:
         if method == "gram" and fn is _svd_gram_native and host != "never":
             blas = _host_blas()
             on_host = _assign_sectors([tuple(M.shape) for M in mats], blas is not None) \
                 if host == "auto" else [True] * len(mats)
-            fns = [_svd_gram_host if h else _svd_gram_native for h in on_host]
+            fns = [pick(M, _svd_gram_host if h else _svd_gram_native)
+                   for M, h in zip(mats, on_host)]
             if low:
                 fns = [_with_fp64_fallback(f) for f in fns]
             if any(on_host) and blas is not None:
@@ -327,10 +361,12 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
             else:
                 facs = _concurrent().map(fns, mats, m.data.device)
         else:
-            facs = _concurrent().map(_with_fp64_fallback(fn) if low else fn, mats,
-                                     m.data.device)
+            fn1 = _with_fp64_fallback(fn) if low else fn
+            facs = _concurrent().map([pick(M, fn1) if fn is _svd_gram_native else fn1
+                                      for M in mats], mats, m.data.device)
     else:
-        facs = [(_with_fp64_fallback(fn) if low else fn)(M) for M in mats]
+        fn1 = _with_fp64_fallback(fn) if low else fn
+        facs = [(pick(M, fn1) if fn is _svd_gram_native else fn1)(M) for M in mats]
     if low:
         facs = [(U.double(), S.double(), Vh.double(), h) for U, S, Vh, h in facs]
     parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
