@@ -182,6 +182,8 @@ def main():
     ap.add_argument("--mixed-schedule", default="bond", choices=["bond", "sweep"],
                     help="mixed modes: polish every bond, or tensor-core-only opening sweeps")
     ap.add_argument("--polish-sweeps", type=int, default=2)
+    ap.add_argument("--sweep-warmup-chi", type=int, default=256,
+                    help="untimed 2-sweep DMRG at this chi before each timed precision (0: none)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()
@@ -469,7 +471,7 @@ def sweep_leg(torch, args):
     reference's own FP64 result (tests/golden/c2_xxz_n64_chi1024.json) as the oracle at N=64
     chi=1024, or the half-filled Fermi-Hubbard chain (t=1, U=4) under U(1) x U(1) (N_up, N_dn)
     blocks, compared with the FP64 run."""
-    from tnkit_gb300 import workloads
+    from tnkit_gb300 import ops, workloads
     from tnkit_gb300.dmrg import dmrg
     from tnkit_gb300.mpo import to_block_mpo
     N, chi = args.sweep_n, args.sweep_chi
@@ -485,7 +487,11 @@ def sweep_leg(torch, args):
     out = {"workload": f"{name}, {args.sweeps} sweeps, seed 1, expand 0, "
                        f"truncation '{args.svd_method}', mixed schedule '{args.mixed_schedule}'"
                        + (f" ({args.polish_sweeps} polished sweeps)"
-                          if args.mixed_schedule == "sweep" else "")}
+                          if args.mixed_schedule == "sweep" else ""),
+           "warmup": (f"each precision after an untimed 2-sweep DMRG at chi="
+                      f"{min(chi, args.sweep_warmup_chi)} (first-use library and kernel loading), "
+                      if args.sweep_warmup_chi > 0 else "no warm-up DMRG, ")
+                     + "plan caches cleared before each timed run"}
     ref = None
     gp = os.path.join(HERE, "tests", "golden", "c2_xxz_n64_chi1024.json")
     if args.sweep_model == "xxz" and N == 64 and chi == 1024 and os.path.exists(gp):
@@ -494,6 +500,11 @@ def sweep_leg(torch, args):
         out["reference_sweep_s"] = ref["sweep_s"]
     precs = [p for p in args.sweep_precisions.split(",") if p]
     for prec in precs:
+        if args.sweep_warmup_chi > 0:
+            dmrg(make(), min(chi, args.sweep_warmup_chi), charge=charge, seed=2, n_sweeps=2,
+                 tol=0, rtol=0, expand=0, precision=prec, svd_method=args.svd_method,
+                 mixed_schedule=args.mixed_schedule, polish_sweeps=1)
+        ops._PLANS.clear()
         Wb = make()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

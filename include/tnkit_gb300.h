@@ -304,6 +304,12 @@ int tnk_cgs_pass_f32(const float* V, int64_t ldv, int32_t nv, const double* cin,
 /* y = x * (f / s[0]) on FP32 vectors, s on the device (double). */
 int tnk_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,
                       void* stream);
+/* Thick-restart rotation of an FP32 basis: out[q*ldo + k] = sum_r Y[r*kk + q] V[r*ldv + k] for
+ * q < kk, r < nv (nv, kk <= 64; Y row-major nv x kk doubles on the device, used in FP32; out must
+ * not overlap V). Replaces the (kk x cur)(cur x n) product U = Yk^T Vb[:cur] of the reference's
+ * restart, tnkit/eigensolver.py:626-636. */
+int tnk_rotate_f32(const float* V, int64_t ldv, int32_t nv, const double* Y, int32_t kk,
+                   float* out, int64_t ldo, int64_t n, void* stream);
 /* y = a*x + b*y with the scalars a = sa[0]*fa, b = sb[0]*fb read from device memory when
  * sa/sb are non-null (else 1): lets Lanczos use alpha/beta without a host round trip. */
 int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,

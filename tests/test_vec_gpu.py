@@ -195,3 +195,43 @@ def test_lanczos_fp32_basis_matches_eigvalsh():
     assert x.dtype == torch.float32 and info["converged"] and info["restarts"] > 0
     assert abs(e - ev[0]) <= 1e-5 * abs(ev[0])
     assert abs(abs(float(np.dot(x.double().cpu().numpy(), evec[:, 0]))) - 1.0) <= 1e-4
+
+
+@pytest.mark.parametrize("nv,kk,n,ld", [(40, 10, 808598, 808598), (64, 64, 1003, 1010),
+                                        (17, 33, 200003, 200003), (1, 1, 1, 1), (5, 3, 0, 0),
+                                        (0, 4, 100, 100)])
+def test_rotate_f32_matches_numpy(ctx, nv, kk, n, ld):
+    """The thick-restart rotation of an FP32 basis (tnk_rotate_f32): out = Y^T V[:nv], FP32
+    FMA chains in ascending row order, coefficients rounded to FP32 -- bar (nv + 2) FP32
+    roundings of the summed magnitudes; nv = 0 writes zeros."""
+    rng = np.random.default_rng(nv * 31 + kk + n)
+    V = rng.standard_normal((max(nv, 1), max(ld, 1))).astype(np.float32)
+    Y = rng.standard_normal((max(nv, 1), kk))
+    Vd = torch.as_tensor(V, device="cuda")
+    Yd = torch.as_tensor(Y[:nv].copy() if nv else Y, device="cuda")
+    out = torch.full((kk, max(ld, 1)), 7.0, dtype=torch.float32, device="cuda")
+    rc = ctx.lib.tnk_rotate_f32(Vd.data_ptr(), max(ld, 1), nv, Yd.data_ptr(), kk, out.data_ptr(),
+                                max(ld, 1), n, ctx.sp)
+    assert rc == 0
+    got = out[:, :n].double().cpu().numpy()
+    Vn = V[:nv, :n].astype(np.float64)
+    want = Y[:nv].T @ Vn
+    scale = np.abs(Y[:nv]).T @ np.abs(Vn)
+    assert np.all(np.abs(got - want) <= (nv + 2) * 1.2e-7 * scale + 1e-30)
+    if ld > n:                                       # columns past n untouched
+        assert bool((out[:, n:] == 7.0).all())
+
+
+def test_rotate_f32_rejects_bad_arguments(ctx):
+    V = torch.zeros((2, 8), dtype=torch.float32, device="cuda")
+    Y = torch.zeros((2, 2), dtype=torch.float64, device="cuda")
+    out = torch.zeros((2, 8), dtype=torch.float32, device="cuda")
+    lib = ctx.lib
+    args = lambda nv, kk, ldv, ldo, n: (V.data_ptr(), ldv, nv, Y.data_ptr(), kk, out.data_ptr(),
+                                       ldo, n, ctx.sp)
+    assert lib.tnk_rotate_f32(*args(65, 2, 8, 8, 8)) != 0       # nv above 64
+    assert lib.tnk_rotate_f32(*args(2, 0, 8, 8, 8)) != 0        # no kept vectors
+    assert lib.tnk_rotate_f32(*args(2, 65, 8, 8, 8)) != 0       # kk above 64
+    assert lib.tnk_rotate_f32(*args(2, 2, 4, 8, 8)) != 0        # ldv < n
+    assert lib.tnk_rotate_f32(*args(2, 2, 8, 4, 8)) != 0        # ldo < n
+    assert lib.tnk_rotate_f32(*args(2, 2, 8, 8, -1)) != 0       # negative length

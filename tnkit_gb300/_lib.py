@@ -94,6 +94,7 @@ _SIGS = {
     "tnk_cgs_pass_f64": ([_P, _I64, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P], C.c_int),
     "tnk_cgs_pass_f32": ([_P, _I64, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P], C.c_int),
     "tnk_scale_div_f32": ([_P, _P, _I64, _P, _D, _P], C.c_int),
+    "tnk_rotate_f32": ([_P, _I64, _I32, _P, _I32, _P, _I64, _I64, _P], C.c_int),
     "tnk_svd_gram_ws_f64": ([_I64, _I64, _P], C.c_int),
     "tnk_svd_gram_f64": ([_P, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P], C.c_int),
     "tnk_svd_gram_ws2_f64": ([_I64, _I64, _I32, _P], C.c_int),

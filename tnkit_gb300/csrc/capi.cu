@@ -27,6 +27,8 @@ int vec_cgs_pass(const double*, int64_t, int, const double*, double*, int64_t, d
 int vec_cgs_pass_f32(const float*, int64_t, int, const double*, float*, int64_t, double*, int,
                      double*, unsigned*, cudaStream_t);
 int vec_scale_div_f32(const float*, float*, int64_t, const double*, double, cudaStream_t);
+int vec_rotate_f32(const float*, int64_t, int, const double*, int, float*, int64_t, int64_t,
+                   cudaStream_t);
 
 // The three stages of a plan3 on the operand slots (x0, x1, x2, ws).
 static int run_plan3(const tnk_plan3* p, const double* x0, const double* x1, const double* x2,
@@ -172,6 +174,11 @@ int tnk_cgs_pass_f32(const float* V, int64_t ldv, int32_t nv, const double* cin,
 int tnk_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,
                       void* stream) {
     return vec_scale_div_f32(x, y, n, s, f, (cudaStream_t)stream);
+}
+
+int tnk_rotate_f32(const float* V, int64_t ldv, int32_t nv, const double* Y, int32_t kk,
+                   float* out, int64_t ldo, int64_t n, void* stream) {
+    return vec_rotate_f32(V, ldv, nv, Y, kk, out, ldo, n, (cudaStream_t)stream);
 }
 
 int tnk_axpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,

@@ -414,6 +414,50 @@ __global__ void __launch_bounds__(NT) scale_div_kernel(const double* __restrict_
         y[k] = x[k] * a;
 }
 
+// Thick-restart rotation of an FP32 Krylov basis: out[q*ldo + k] = sum_r Y[r*kk + q] V[r*ldv + k]
+// (q < kk kept Ritz vectors, r < nv basis rows, r ascending). One thread per column k: the
+// coefficients, converted to FP32 and padded with zeros to a multiple of RQ columns, sit in
+// shared memory and are read as broadcast float4; V is read once per chunk of RQ outputs (once
+// for kk <= RQ), coalesced along k.
+constexpr int RQ = 16;
+
+__global__ void __launch_bounds__(NT) rotate_f32_kernel(const float* __restrict__ V, int64_t ldv,
+                                                        int nv, const double* __restrict__ Y,
+                                                        int kk, float* __restrict__ out,
+                                                        int64_t ldo, int64_t n) {
+    __shared__ __align__(16) float ys[MAXNV * MAXNV];
+    const int kp = (kk + RQ - 1) / RQ * RQ;
+    for (int i = threadIdx.x; i < nv * kp; i += NT) {
+        const int r = i / kp, q = i - r * kp;
+        ys[i] = q < kk ? (float)Y[r * kk + q] : 0.0f;
+    }
+    __syncthreads();
+    for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * NT) {
+        for (int q0 = 0; q0 < kk; q0 += RQ) {
+            float acc[RQ];
+#pragma unroll
+            for (int q = 0; q < RQ; ++q) acc[q] = 0.0f;
+#pragma unroll 4
+            for (int r = 0; r < nv; ++r) {
+                const float v = V[r * ldv + k];
+                const float4* y4 = reinterpret_cast<const float4*>(ys + r * kp + q0);
+#pragma unroll
+                for (int c = 0; c < RQ / 4; ++c) {
+                    const float4 y = y4[c];
+                    acc[4 * c + 0] = fmaf(y.x, v, acc[4 * c + 0]);
+                    acc[4 * c + 1] = fmaf(y.y, v, acc[4 * c + 1]);
+                    acc[4 * c + 2] = fmaf(y.z, v, acc[4 * c + 2]);
+                    acc[4 * c + 3] = fmaf(y.w, v, acc[4 * c + 3]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < RQ; ++q)
+                if (q0 + q < kk) out[(q0 + q) * ldo + k] = acc[q];
+        }
+    }
+}
+
 }  // namespace
 
 int vec_dot(const double* x, const double* y, int64_t n, double* out, double* red,
@@ -522,6 +566,19 @@ int vec_scale_div_f32(const float* x, float* y, int64_t n, const double* s, doub
     if (n == 0) return TNK_OK;
     scale_div_f32_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(x, y, n, s, f);
     return check_launch("scale_div_f32_kernel");
+}
+
+int vec_rotate_f32(const float* V, int64_t ldv, int nv, const double* Y, int kk, float* out,
+                   int64_t ldo, int64_t n, cudaStream_t stream) {
+    if (n < 0 || nv < 0 || nv > MAXNV || kk < 1 || kk > MAXNV || ldv < n || ldo < n || !out ||
+        (nv > 0 && (!Y || (n > 0 && !V)))) {
+        set_error("rotate_f32: bad argument (nv=%d, kk=%d, n=%lld, ldv=%lld, ldo=%lld)", nv, kk,
+                  (long long)n, (long long)ldv, (long long)ldo);
+        return TNK_ERR_ARG;
+    }
+    if (n == 0) return TNK_OK;
+    rotate_f32_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(V, ldv, nv, Y, kk, out, ldo, n);
+    return check_launch("rotate_f32_kernel");
 }
 
 }  // namespace tnk

@@ -115,13 +115,15 @@ class _Dev:
 
     def rotate(self, Y: np.ndarray, V: torch.Tensor, out: torch.Tensor):
         """out (kk x n) = Y^T (kk x cur) @ V[:cur] as one grouped-GEMM launch (FP64), or one
-        library GEMM for an FP32 basis."""
+        tnk_rotate_f32 launch for an FP32 basis."""
         cur, kk = Y.shape
         n = V.shape[1]
         if V.dtype == torch.float32:
-            A = torch.as_tensor(np.ascontiguousarray(Y.T), dtype=torch.float32, device=V.device)
-            torch.mm(A, V, out=out)
-            return (A,)
+            Yd = torch.as_tensor(np.ascontiguousarray(Y, dtype=np.float64), device=V.device)
+            _lib.check(self.lib.tnk_rotate_f32(V.data_ptr(), V.stride(0), cur, Yd.data_ptr(), kk,
+                                               out.data_ptr(), out.stride(0), n, self.sp),
+                       "rotate")
+            return (Yd,)
         A = torch.as_tensor(np.ascontiguousarray(Y.T), dtype=torch.float64, device=V.device)
         task = np.array([(0, n, kk, n, 0, 1, 0)], dtype=GEMM_TASK)
         seg = np.array([(0, 0, cur, 1, V.stride(0), 1, cur, 0, 1, 0, 0, 1.0)], dtype=GEMM_SEG)

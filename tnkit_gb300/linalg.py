@@ -447,3 +447,18 @@ class Scalars:
         _lib.check(self.lib.tnk_nrm2_f64(x.data_ptr(), x.numel(), self.sc.data_ptr(),
                                          self.red.data_ptr(), sp), "nrm2")
         return float(self.sc[0].item())
+
+    def residual(self, v: torch.Tensor, w: torch.Tensor):
+        """(rayleigh quotient th, ||w - th v|| / ||v||) of real FP64 buffers with w = H v; w is
+        overwritten by w - th v."""
+        sp = _lib.stream_ptr()
+        n = v.numel()
+        _lib.check(self.lib.tnk_nrm2_f64(v.data_ptr(), n, self.sc.data_ptr(),
+                                         self.red.data_ptr(), sp), "nrm2")
+        _lib.check(self.lib.tnk_dot_f64(v.data_ptr(), w.data_ptr(), n, self.sc.data_ptr() + 8,
+                                        self.red.data_ptr(), sp), "dot")
+        nv, vw = (float(x) for x in self.sc[:2].tolist())
+        th = vw / (nv * nv)
+        _lib.check(self.lib.tnk_axpby_f64(v.data_ptr(), w.data_ptr(), n, None, -th, None, 1.0,
+                                          sp), "axpby")
+        return th, self.norm(w) / nv

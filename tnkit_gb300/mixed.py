@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import linalg as LA
 from . import plan as P
 from .lanczos import lanczos_ground_restart
 from .layout import Layout
@@ -109,13 +110,20 @@ class _F32Vectors:
         return out
 
 
+_SCAL = {}
+
+
+def _scalars(device) -> LA.Scalars:
+    key = str(device)
+    if key not in _SCAL:
+        _SCAL[key] = LA.Scalars(device)
+    return _SCAL[key]
+
+
 def _fp64_residual(op64, v: torch.Tensor):
-    """(rayleigh quotient, residual norm) of v in FP64: one FP64 matvec."""
-    w = op64(v)
-    nv = float(torch.linalg.vector_norm(v))
-    th = float(torch.dot(v, w)) / (nv * nv)
-    r = float(torch.linalg.vector_norm(w - th * v)) / nv
-    return th, r
+    """(rayleigh quotient, residual norm) of v in FP64: one FP64 matvec, then the library's
+    norm / dot / axpy kernels."""
+    return _scalars(v.device).residual(v, op64(v))
 
 
 def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
@@ -141,8 +149,7 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
         op_lo.check_device_error()
         if counts is not None:
             counts["lo"] = counts.get("lo", 0) + op_lo.calls
-        x = x32.double()
-        x = x / torch.linalg.vector_norm(x)
+        x = _scalars(x32.device).normalize_(x32.double())
         return e_lo, x, {"iters": info_lo["iters"], "converged": info_lo["converged"],
                          "e_lo": e_lo, "n_lo": op_lo.calls, "n_hi": 0, "matvecs": op_lo.calls}
     c0 = getattr(op64, "calls", 0)
@@ -152,8 +159,7 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
     x = v0
     if r0 < tol:
         e, info_hi = th0, {"iters": 0, "converged": True}
-        nrm = torch.linalg.vector_norm(v0)
-        x = v0 / nrm
+        x = _scalars(v0.device).normalize_(v0.clone())
     else:
         if r0 >= switch * tol_lo:
             op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
