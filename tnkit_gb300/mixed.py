@@ -25,7 +25,7 @@ from . import linalg as LA
 from . import plan as P
 from .lanczos import lanczos_ground_restart
 from .layout import Layout
-from .ops import _host_of, _pack, plan_two_site
+from .ops import _PLANS, _pack, _two_site_key, host_plan_two_site
 from .tensor import BlockTensor
 
 
@@ -39,8 +39,9 @@ class TwoSiteOperatorTC:
         dev = L.data.device
         self.device = dev
         self.passes = passes
-        p64 = plan_two_site(theta_layout, L, W1, W2, R, dev)
-        tc = P.HostPlanTC(p64.host, theta_layout, L.layout, R.layout)
+        key = _two_site_key(theta_layout, L, W1, W2, R)
+        tc = _PLANS.get_or(("tc",) + key, lambda: P.HostPlanTC(
+            host_plan_two_site(theta_layout, L, W1, W2, R), theta_layout, L.layout, R.layout))
         self.host = tc
         self.macs = tc.macs
         self.n = theta_layout.size

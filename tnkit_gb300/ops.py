@@ -43,16 +43,23 @@ def _cplx(hp):
 
 
 def _pack(arrays, device):
-    """Concatenate numpy arrays into one device byte buffer; return (buffer, byte offsets)."""
+    """Concatenate numpy arrays into one device byte buffer; return (buffer, byte offsets).
+    The bytes are staged in pinned host memory and copied without waiting for the stream, so
+    building a plan never drains the GPU's queue (the caching host allocator keeps the staging
+    block until the copy has run)."""
     offs, total = [], 0
     for a in arrays:
         offs.append(total)
         total += (a.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
-    host = np.zeros(max(total, _ALIGN), np.uint8)
+    total = max(total, _ALIGN)
+    dev = torch.device(device)
+    pinned = dev.type == "cuda"
+    host_t = torch.empty(total, dtype=torch.uint8, pin_memory=pinned)
+    host = host_t.numpy()
     for a, o in zip(arrays, offs):
         if a.nbytes:
-            host[o:o + a.nbytes] = np.frombuffer(a.tobytes(), np.uint8)
-    buf = torch.from_numpy(host).to(device)
+            host[o:o + a.nbytes] = np.frombuffer(np.ascontiguousarray(a).data, np.uint8)
+    buf = host_t.to(dev, non_blocking=pinned)
     return buf, offs
 
 
@@ -188,16 +195,26 @@ def _real_plan(key, build):
     return _PLANS.get_or(("host",) + key, build)
 
 
+def _two_site_key(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                  R: BlockTensor):
+    return ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout)
+
+
+def host_plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
+                       R: BlockTensor) -> P.HostPlan3:
+    """The host tables of the two-site plan (cached; no device copy)."""
+    return _real_plan(_two_site_key(theta, L, W1, W2, R),
+                      lambda: P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)),
+                                                             (W2.layout, _host_of(W2))],
+                                           R.layout))
+
+
 def plan_two_site(theta: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
                   R: BlockTensor, device, cplx: bool = False, ff: bool = False) -> DevicePlan3:
-    key = ("apply2", theta, L.layout, _mpo_key(W1), _mpo_key(W2), R.layout)
-
-    def host():
-        return P.plan_apply(theta, L.layout, [(W1.layout, _host_of(W1)),
-                                              (W2.layout, _host_of(W2))], R.layout)
+    key = _two_site_key(theta, L, W1, W2, R)
 
     def build():
-        hp = _real_plan(key, host)
+        hp = host_plan_two_site(theta, L, W1, W2, R)
         return DevicePlan3(_cplx(hp) if cplx else hp, device, ff=ff)
     return _PLANS.get_or(key + (str(device), cplx, ff), build)
 

@@ -101,12 +101,13 @@ class CombTable:
     def arrays(self):
         tasks = np.array(self.tasks, dtype=COMB_TASK) if self.tasks else np.zeros(0, COMB_TASK)
         terms = np.array(self.terms, dtype=COMB_TERM) if self.terms else np.zeros(0, COMB_TERM)
-        items = []
-        for t, (_, rows, cols, *_r) in enumerate(self.tasks):
-            step = max(1, COMB_CHUNK // max(1, cols))
-            for r0 in range(0, rows, step):
-                items.append((t, r0, min(rows, r0 + step), 0))
-        it = np.array(items, dtype=COMB_ITEM) if items else np.zeros(0, COMB_ITEM)
+        it = np.zeros(0, COMB_ITEM)
+        if len(tasks):
+            rows = tasks["rows"].astype(np.int64)
+            step = np.maximum(1, COMB_CHUNK // np.maximum(1, tasks["cols"].astype(np.int64)))
+            tid, r0, _ = _grid_items(rows, np.ones_like(rows), step, 1)
+            it = np.zeros(len(tid), COMB_ITEM)
+            it["task"], it["row0"], it["row1"] = tid, r0, np.minimum(rows[tid], r0 + step[tid])
         return tasks, terms, it
 
 
@@ -765,28 +766,43 @@ def _rup(x: int, a: int) -> int:
     return (int(x) + a - 1) // a * a
 
 
+def _grid_items(rows, cols, step_r, step_c):
+    """(task, r0, c0) of every step_r x step_c cell of each task's rows x cols, task-major, then
+    row-major: the enumeration of nested range() loops, vectorised."""
+    rows, cols = np.asarray(rows, np.int64), np.asarray(cols, np.int64)
+    step_r = np.broadcast_to(np.asarray(step_r, np.int64), rows.shape)
+    tr, tc = -(-rows // step_r), -(-cols // step_c)
+    cnt = tr * tc
+    tid = np.repeat(np.arange(len(rows)), cnt)
+    local = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+    return tid, (local // tc[tid]) * step_r[tid], (local % tc[tid]) * step_c
+
+
 def _tiles(tasks, segs, tile):
-    out, cost = [], []
-    for t, task in enumerate(tasks):
-        m, n = int(task["m"]), int(task["n"])
-        ktot = int(segs[int(task["seg_begin"]):int(task["seg_end"])]["k"].sum()) or 1
-        for m0 in range(0, m, tile):
-            for n0 in range(0, n, tile):
-                out.append((t, m0, n0, 0))
-                cost.append(ktot)
-    order = np.argsort(-np.asarray(cost, np.int64), kind="stable") if out else []
-    return (np.array([out[i] for i in order], dtype=GEMM_TILE) if out
-            else np.zeros(0, GEMM_TILE))
+    """Every (task, m0, n0) tile, ordered by decreasing K (stable)."""
+    if len(tasks) == 0:
+        return np.zeros(0, GEMM_TILE)
+    kcum = np.concatenate([[0], np.cumsum(segs["k"].astype(np.int64))]) if len(segs) else \
+        np.zeros(1, np.int64)
+    ktot = kcum[tasks["seg_end"]] - kcum[tasks["seg_begin"]]
+    ktot = np.where(ktot == 0, 1, ktot)
+    tid, m0, n0 = _grid_items(tasks["m"], tasks["n"], tile, tile)
+    order = np.argsort(-ktot[tid], kind="stable")
+    tl = np.zeros(len(tid), GEMM_TILE)
+    tl["task"], tl["m0"], tl["n0"] = tid[order], m0[order], n0[order]
+    return tl
 
 
 def _cvt_items(tasks):
+    """The 32 x 32 cells of every staging task (rows, cols at positions 2, 3)."""
     from ._lib import CVT_ITEM
-    items = []
-    for t, (src_off, dst_off, rows, cols, *_r) in enumerate(tasks):
-        for r0 in range(0, rows, 32):
-            for c0 in range(0, cols, 32):
-                items.append((t, r0, c0, 0))
-    return np.array(items, dtype=CVT_ITEM) if items else np.zeros(0, CVT_ITEM)
+    if not len(tasks):
+        return np.zeros(0, CVT_ITEM)
+    rc = np.array([(t[2], t[3]) for t in tasks], np.int64).reshape(-1, 2)
+    tid, r0, c0 = _grid_items(rc[:, 0], rc[:, 1], 32, 32)
+    it = np.zeros(len(tid), CVT_ITEM)
+    it["task"], it["r0"], it["c0"] = tid, r0, c0
+    return it
 
 
 class HostPlanTC:
