@@ -364,6 +364,58 @@ int tnk_svd_gram_ws_f32(int64_t R, int64_t C, int64_t* bytes);
 int tnk_svd_gram_f32(const float* M, int64_t R, int64_t C, float* U, float* S, float* Vh,
                      void* ws, int64_t ws_bytes, double* S_host, void* stream);
 
+/* ----------------------------------------------------------------------------------------
+ * Host planner: the block tables of the one- and two-site H_eff contraction (the stage-1 /
+ * stage-2 / stage-3 tables above) built natively from the layouts' sector keys, and their
+ * re-layout for the tensor-core path. It replaces the block pairing that the reference does in
+ * Python at every tensordot (tnkit/blocks.py:1089-1090, per pair of matching blocks) with one
+ * pass over the keys per local problem. Host memory only; no CUDA call.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct {
+    int32_t nlegs, nblocks;
+    const int64_t* keys;             /* nblocks x nlegs sector indices (canonical order) */
+    const int64_t* shapes;           /* nblocks x nlegs block extents */
+    const int64_t* offsets;          /* nblocks element offsets */
+} tnk_layout_desc;
+
+typedef struct {
+    int32_t n_sites, pad;            /* 1 or 2 */
+    tnk_layout_desc theta;           /* (a, s_1 .. s_n, b) */
+    tnk_layout_desc L;               /* (a', w, a) */
+    tnk_layout_desc R;               /* (b', r, b) */
+    tnk_layout_desc out;             /* (a', s'_1 .. s'_n, b') */
+    const double* S;                 /* combined MPO, dense C order over the axes
+                                        (w, in_1 .. in_n, out_1 .. out_n, r) */
+    int64_t s_dims[6];               /* its extents (2 n + 2 used) */
+    const int64_t* sec_start;        /* sector starts along the axes of S, axis by axis */
+    const int64_t* sec_dim;          /* and their extents */
+    int64_t sec_begin[7];            /* axis a's sectors at [sec_begin[a], sec_begin[a + 1]) */
+} tnk_apply_plan_in;
+
+/* Tables of a built plan, read back with tnk_planb_table(handle, id, &data, &count):
+ * 0 stage-1 tasks, 1 stage-1 segments, 2 stage-2 tasks, 3 stage-2 terms, 4 stage-3 tasks,
+ * 5 stage-3 segments (tnk_apply_plan_build); 10 stage-1 tasks, 11 stage-1 tensor-core segments,
+ * 12 stage-2 tasks, 13 stage-3 tasks, 14 stage-3 tensor-core segments, 15 tensor maps
+ * (int64 offset, rows, cols, ld each), 16 / 17 / 18 the staging tasks of L / R / theta
+ * (tnk_plan_tc_build). tnk_planb_scalars: ws1, ws2, stage-1 MACs, stage-3 MACs, staging
+ * elements. */
+int tnk_apply_plan_build(const tnk_apply_plan_in* in, void** handle);
+int tnk_plan_tc_build(const tnk_gemm_task* t1, int64_t nt1, const tnk_gemm_seg* s1,
+                      const tnk_comb_task* t2, int64_t nt2, const tnk_gemm_task* t3,
+                      int64_t nt3, const tnk_gemm_seg* s3, void** handle);
+/* Stage 3's long tasks cut along K so that one wave of tiles finishes together: a task whose
+ * tile work (K x min(tile_m, m) x min(tile_n, n)) exceeds the average work per resident CTA
+ * (slots) is split into at most max_chunks chunks writing compact partials at ws_base + ...
+ * (flags bit 4); tables 4 / 5 hold the new stage-3 tasks and segments, 2 / 3 the stage-4
+ * combination summing the partials in chunk order; scalars: 1 when anything was split (else
+ * the tables are empty and the input stands), then the workspace elements added. */
+int tnk_plan_split_k(const tnk_gemm_task* t, int64_t nt, const tnk_gemm_seg* s, int64_t ws_base,
+                     int32_t slots, int32_t max_chunks, int32_t tile_m, int32_t tile_n,
+                     void** handle);
+int tnk_planb_table(const void* handle, int32_t id, const void** data, int64_t* count);
+int tnk_planb_scalars(const void* handle, int64_t* out5);
+void tnk_planb_free(void* handle);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,14 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: takes more than a few seconds on the CPU")
 
 
+@pytest.fixture(scope="session", autouse=True)
+def _native_library():
+    """The library (host planner and kernels) built in-tree before any test: nvcc cross-compiles
+    it without a GPU, and the build is skipped when it is up to date."""
+    from tnkit_gb300 import build
+    build.build()
+
+
 @pytest.fixture(scope="session")
 def golden():
     import json

@@ -48,6 +48,18 @@ CVT_TASK = np.dtype([("src_off", "<i8"), ("dst_off", "<i8"), ("rows", "<i4"), ("
 CVT_ITEM = np.dtype([("task", "<i4"), ("r0", "<i4"), ("c0", "<i4"), ("pad", "<i4")])
 
 
+class LayoutDesc(C.Structure):
+    _fields_ = [("nlegs", C.c_int32), ("nblocks", C.c_int32), ("keys", C.c_void_p),
+                ("shapes", C.c_void_p), ("offsets", C.c_void_p)]
+
+
+class ApplyPlanIn(C.Structure):
+    _fields_ = [("n_sites", C.c_int32), ("pad", C.c_int32), ("theta", LayoutDesc),
+                ("L", LayoutDesc), ("R", LayoutDesc), ("out", LayoutDesc), ("S", C.c_void_p),
+                ("s_dims", C.c_int64 * 6), ("sec_start", C.c_void_p), ("sec_dim", C.c_void_p),
+                ("sec_begin", C.c_int64 * 7)]
+
+
 class Plan3(C.Structure):
     _fields_ = [("t1", C.c_void_p), ("s1", C.c_void_p), ("tiles1", C.c_void_p),
                 ("n_tiles1", C.c_int64),
@@ -116,6 +128,12 @@ _SIGS = {
     "tnk_zmultidot_f64": ([_P, _I64, _I32, _P, _I64, _P, _P, _P], C.c_int),
     "tnk_zgemv_sub_f64": ([_P, _I64, _I32, _P, _P, _I64, _P], C.c_int),
     "tnk_zaxpby_f64": ([_P, _P, _I64, _P, _D, _P, _D, _P], C.c_int),
+    "tnk_apply_plan_build": ([_P, _P], C.c_int),
+    "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
+    "tnk_plan_split_k": ([_P, _I64, _P, _I64, _I32, _I32, _I32, _I32, _P], C.c_int),
+    "tnk_planb_table": ([_P, _I32, _P, _P], C.c_int),
+    "tnk_planb_scalars": ([_P, _P], C.c_int),
+    "tnk_planb_free": ([_P], None),
 }
 
 _lib = None

@@ -115,12 +115,17 @@ class _Concurrent:
             s.wait_stream(main)
         fns = fn if isinstance(fn, (list, tuple)) else [fn] * len(mats)
 
+        def keep(out):
+            for t in out:
+                if isinstance(t, torch.Tensor):
+                    t.record_stream(main)
+                elif isinstance(t, (list, tuple)):
+                    keep(t)
+
         def run(i):
             with torch.cuda.stream(streams[i]):
                 out = fns[i](mats[i])
-                for t in out:
-                    if isinstance(t, torch.Tensor):
-                        t.record_stream(main)
+                keep(out)
                 return out
         res = list(self.pool.map(run, range(len(mats))))
         for s in streams:
@@ -176,6 +181,8 @@ def _svd_gram_native(M: torch.Tensor, orth: int = 0):
 # each other down).
 _GPU_MS_PER_ROW = 14.0 / 522          # cuSOLVER path: ~linear in n (latency-bound)
 _HOST_MS_522 = 28.6                   # numpy path with a quarter of the cores: ~n^2.1
+_HOST_MODE = "parallel"               # host sectors: 'parallel' (a worker each) or 'queue'
+_HOST_THREADS_DIV = 4                 # host library threads during the truncation: cores / this
 _HOST_BLAS = {"lib": None, "tried": False}
 
 
@@ -198,6 +205,24 @@ def _host_blas():
             _HOST_BLAS["lib"] = (set_, get_)
             break
     return _HOST_BLAS["lib"]
+
+
+def _map_hybrid(fns, mats, on_host, device):
+    """fns[i](mats[i]) for every sector: the GPU sectors one stream and worker each, the host
+    sectors (_HOST_MODE 'queue') one after another, largest first, in a single worker whose
+    LAPACK calls use the host library's threads; 'parallel' gives them a worker each too."""
+    if _HOST_MODE != "queue":
+        return _concurrent().map(fns, mats, device)
+    gpu = [i for i, h in enumerate(on_host) if not h]
+    host = sorted((i for i, h in enumerate(on_host) if h), key=lambda i: -min(mats[i].shape))
+    items = [fns[i] for i in gpu] + [lambda _: [fns[i](mats[i]) for i in host]]
+    res = _concurrent().map(items, [mats[i] for i in gpu] + [None], device)
+    out = [None] * len(mats)
+    for i, r in zip(gpu, res[:len(gpu)]):
+        out[i] = r
+    for i, r in zip(host, res[-1]):
+        out[i] = r
+    return out
 
 
 def _assign_sectors(shapes, host_ok: bool):
@@ -351,11 +376,9 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
                 fns = [_with_fp64_fallback(f) for f in fns]
             if any(on_host) and blas is not None:
                 prev = blas[1]()
-                # a quarter of the cores: with more, the truncation of a chi=1024 mid bond is
-                # no faster than on the GPU alone (46 ms); with 4 of 16 it takes 32 ms
-                blas[0](max(1, prev // 4))
+                blas[0](max(1, prev // _HOST_THREADS_DIV))
                 try:
-                    facs = _concurrent().map(fns, mats, m.data.device)
+                    facs = _map_hybrid(fns, mats, on_host, m.data.device)
                 finally:
                     blas[0](prev)
             else:

@@ -21,6 +21,7 @@ tnkit/blocks.py:_sym_plan does, from the same canonical layouts.
 """
 from __future__ import annotations
 
+import ctypes as C
 import itertools
 import math
 from collections import defaultdict
@@ -28,6 +29,7 @@ from typing import Dict, List, Sequence, Tuple
 
 import numpy as np
 
+from . import _lib
 from ._lib import (COMB_ITEM, COMB_TASK, COMB_TERM, GEMM_SEG, GEMM_TASK, GEMM_TILE)
 from .layout import Layout, Leg, canonical
 
@@ -101,14 +103,20 @@ class CombTable:
     def arrays(self):
         tasks = np.array(self.tasks, dtype=COMB_TASK) if self.tasks else np.zeros(0, COMB_TASK)
         terms = np.array(self.terms, dtype=COMB_TERM) if self.terms else np.zeros(0, COMB_TERM)
-        it = np.zeros(0, COMB_ITEM)
-        if len(tasks):
-            rows = tasks["rows"].astype(np.int64)
-            step = np.maximum(1, COMB_CHUNK // np.maximum(1, tasks["cols"].astype(np.int64)))
-            tid, r0, _ = _grid_items(rows, np.ones_like(rows), step, 1)
-            it = np.zeros(len(tid), COMB_ITEM)
-            it["task"], it["row0"], it["row1"] = tid, r0, np.minimum(rows[tid], r0 + step[tid])
-        return tasks, terms, it
+        return tasks, terms, _comb_items(tasks)
+
+
+def _comb_items(tasks) -> np.ndarray:
+    """The launch grid of a combination stage: chunks of about COMB_CHUNK elements (at least one
+    row) of every task."""
+    if not len(tasks):
+        return np.zeros(0, COMB_ITEM)
+    rows = tasks["rows"].astype(np.int64)
+    step = np.maximum(1, COMB_CHUNK // np.maximum(1, tasks["cols"].astype(np.int64)))
+    tid, r0, _ = _grid_items(rows, np.ones_like(rows), step, 1)
+    it = np.zeros(len(tid), COMB_ITEM)
+    it["task"], it["row0"], it["row1"] = tid, r0, np.minimum(rows[tid], r0 + step[tid])
+    return it
 
 
 def term(src_off, src_ld, src_cs, coef):
@@ -130,7 +138,29 @@ def split_long_tiles(g3, ws_base: int, slots: int = SLOTS, max_chunks: int = 8):
     resident CTA, so one wave of tiles finishes together. Each chunk becomes a task that writes
     its partial product to the workspace (flags bit 4, compact rows at ws_base + ...); stage 4
     sums a split task's partials into its output block in a fixed order. Returns (tables,
-    stage-4 tables, workspace elements added)."""
+    stage-4 tables, workspace elements added). Built by tnk_plan_split_k;
+    _split_long_tiles_py states the same in Python."""
+    tasks, segs, tiles = g3
+    if len(tasks) == 0:
+        return g3, _empty_comb(), 0
+    tasks, segs = np.ascontiguousarray(tasks), np.ascontiguousarray(segs)
+    lib = _lib.lib()
+    h = C.c_void_p()
+    _lib.check(lib.tnk_plan_split_k(tasks.ctypes.data, len(tasks), segs.ctypes.data,
+                                    int(ws_base), slots, max_chunks, TILE_M, TILE_N,
+                                    C.byref(h)), "tnk_plan_split_k")
+    try:
+        (ta, sa, t4, c4), sc = _planb_read(h, [(4, GEMM_TASK), (5, GEMM_SEG), (2, COMB_TASK),
+                                               (3, COMB_TERM)])
+    finally:
+        lib.tnk_planb_free(h)
+    if not sc[0]:
+        return g3, _empty_comb(), 0
+    return (ta, sa, _tiles_cost(ta, sa, TILE_M)), (t4, c4, _comb_items(t4)), sc[1]
+
+
+def _split_long_tiles_py(g3, ws_base: int, slots: int = SLOTS, max_chunks: int = 8):
+    """split_long_tiles in Python (the statement the native planner is tested against)."""
     tasks, segs, tiles = g3
     if len(tasks) == 0:
         return g3, _empty_comb(), 0
@@ -222,10 +252,38 @@ def _dense_sector_order(layout: Layout, data: np.ndarray) -> np.ndarray:
 # --------------------------------------------------------------------------- #
 # H_eff matvec (one or two sites)
 # --------------------------------------------------------------------------- #
-def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]],
-               R: Layout) -> HostPlan3:
-    """Plan of (H_eff theta) for n = len(Ws) in {1, 2} sites. `Ws` holds (layout, flat host
-    data) of each MPO tensor, legs (wl, wr, s, s')."""
+_S_CACHE: "OrderedDict" = None
+
+
+def _combined_mpo(Ws) -> np.ndarray:
+    """Dense combined MPO S[w, i.., s.., r] over sector-ordered indices (S = W1 W2 contracted
+    over the middle channel for two sites), cached per pair of MPO tensors: the same site
+    tensors recur at every bond of every sweep."""
+    global _S_CACHE
+    from collections import OrderedDict
+    if _S_CACHE is None:
+        _S_CACHE = OrderedDict()
+    key = tuple((id(l), id(d)) for l, d in Ws)
+    hit = _S_CACHE.get(key)
+    if hit is not None and all(a is l and b is d for (a, b), (l, d) in zip(hit[0], Ws)):
+        _S_CACHE.move_to_end(key)
+        return hit[1]
+    Wd = [_dense_sector_order(l, d) for l, d in Ws]
+    if len(Ws) == 1:
+        S = np.einsum("wrsi->wisr", Wd[0])
+    else:
+        S = np.einsum("wmsi,mrtj->wijstr", Wd[0], Wd[1])
+    S = np.ascontiguousarray(S, np.float64)
+    _S_CACHE[key] = (tuple(Ws), S)
+    while len(_S_CACHE) > 256:
+        _S_CACHE.popitem(last=False)
+    return S
+
+
+def _apply_setup(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]],
+                 R: Layout):
+    """Checks, the dense combined MPO S[w, in.., out.., r] and the output layout of an H_eff
+    plan (shared by the native and the Python planner)."""
     n = len(Ws)
     if n not in (1, 2) or len(theta.legs) != n + 2:
         raise ValueError("plan_apply: one or two sites")
@@ -238,12 +296,7 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
         _check_contract(theta.legs[1 + a], WL[a].legs[3], "theta.phys/W.in")
     if n == 2:
         _check_contract(WL[0].legs[1], WL[1].legs[0], "W1.right/W2.left")
-    # dense combined MPO S[w, i.., s.., r] over sector-ordered indices
-    Wd = [_dense_sector_order(l, d) for l, d in Ws]
-    if n == 1:
-        S = np.einsum("wrsi->wisr", Wd[0])
-    else:
-        S = np.einsum("wmsi,mrtj->wijstr", Wd[0], Wd[1])
+    S = _combined_mpo(Ws)
     wleg, rleg = WL[0].legs[0], WL[-1].legs[1]
     ins = [WL[a].legs[3] for a in range(n)]
     outs = [WL[a].legs[2] for a in range(n)]
@@ -252,6 +305,94 @@ def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]]
 
     out_legs = (L.legs[0],) + tuple(outs) + (R.legs[0],)
     out = canonical(out_legs, theta.charge)
+    return n, S, wleg, rleg, ins, outs, wst, rst, ist, ost, out
+
+
+def _desc(lay: Layout, keep: list) -> _lib.LayoutDesc:
+    k = np.ascontiguousarray(lay.blocks, np.int64)
+    sh = np.ascontiguousarray(lay.shapes, np.int64)
+    o = np.ascontiguousarray(lay.offsets, np.int64)
+    keep.extend((k, sh, o))
+    return _lib.LayoutDesc(len(lay.legs), lay.nblocks, k.ctypes.data, sh.ctypes.data,
+                           o.ctypes.data)
+
+
+def _planb_read(h, specs):
+    """Copies of the built tables `specs` = [(id, dtype)], then the scalars."""
+    lib = _lib.lib()
+    out = []
+    for tid, dt in specs:
+        ptr, cnt = C.c_void_p(), C.c_int64()
+        _lib.check(lib.tnk_planb_table(h, tid, C.byref(ptr), C.byref(cnt)), "tnk_planb_table")
+        n = int(cnt.value)
+        out.append(np.frombuffer((C.c_char * (n * dt.itemsize)).from_address(ptr.value), dt).copy()
+                   if n else np.zeros(0, dt))
+    sc = (C.c_int64 * 5)()
+    _lib.check(lib.tnk_planb_scalars(h, C.cast(sc, C.c_void_p)), "tnk_planb_scalars")
+    return out, [int(x) for x in sc]
+
+
+class _GemmArrays:
+    """Ready tables of one grouped-GEMM stage (the native planner's output)."""
+
+    def __init__(self, tasks, segs, macs):
+        self.tasks, self.segs, self.macs = tasks, segs, int(macs)
+
+    def arrays(self):
+        return self.tasks, self.segs, _tiles_cost(self.tasks, self.segs, TILE_M)
+
+
+class _CombArrays:
+    def __init__(self, tasks, terms):
+        self.tasks, self.terms = tasks, terms
+
+    def arrays(self):
+        return self.tasks, self.terms, _comb_items(self.tasks)
+
+
+def plan_apply(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]],
+               R: Layout) -> HostPlan3:
+    """Plan of (H_eff theta) for n = len(Ws) in {1, 2} sites. `Ws` holds (layout, flat host
+    data) of each MPO tensor, legs (wl, wr, s, s'). Built by the native planner
+    (tnk_apply_plan_build); _plan_apply_py states the same construction in Python and the tests
+    require identical tables."""
+    n, S, wleg, rleg, ins, outs, wst, rst, ist, ost, out = _apply_setup(theta, L, Ws, R)
+    keep: list = []
+    S = np.ascontiguousarray(S, np.float64)
+    axes = [wleg] + list(ins) + list(outs) + [rleg]
+    starts = np.ascontiguousarray(np.concatenate([l.starts() for l in axes]), np.int64)
+    dims = np.ascontiguousarray(np.concatenate([np.asarray(l.dims, np.int64) for l in axes]),
+                                np.int64)
+    begin = np.concatenate([[0], np.cumsum([len(l.dims) for l in axes])]).astype(np.int64)
+    a = _lib.ApplyPlanIn()
+    a.n_sites = n
+    a.theta, a.L, a.R, a.out = (_desc(theta, keep), _desc(L, keep), _desc(R, keep),
+                                _desc(out, keep))
+    a.S = S.ctypes.data
+    for i, d in enumerate(S.shape):
+        a.s_dims[i] = int(d)
+    a.sec_start, a.sec_dim = starts.ctypes.data, dims.ctypes.data
+    for i, b in enumerate(begin):
+        a.sec_begin[i] = int(b)
+    lib = _lib.lib()
+    h = C.c_void_p()
+    _lib.check(lib.tnk_apply_plan_build(C.byref(a), C.byref(h)), "tnk_apply_plan_build")
+    try:
+        (t1, s1, t2, c2, t3, s3), sc = _planb_read(h, [(0, GEMM_TASK), (1, GEMM_SEG),
+                                                       (2, COMB_TASK), (3, COMB_TERM),
+                                                       (4, GEMM_TASK), (5, GEMM_SEG)])
+    finally:
+        lib.tnk_planb_free(h)
+    ws1, ws2, macs1, macs3, _ = sc
+    return HostPlan3(_GemmArrays(t1, s1, macs1), _CombArrays(t2, c2), _GemmArrays(t3, s3, macs3),
+                     ws1, ws2, out, kind=f"apply{n}")
+
+
+def _plan_apply_py(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarray]],
+                   R: Layout) -> HostPlan3:
+    """The construction of plan_apply in Python (the statement the native planner is tested
+    against)."""
+    n, S, wleg, rleg, ins, outs, wst, rst, ist, ost, out = _apply_setup(theta, L, Ws, R)
 
     # stage 1 candidates: Y[(p, w, phys.., b)] <- (L block, theta block)
     th_by_q: Dict[int, List[int]] = defaultdict(list)
@@ -812,9 +953,47 @@ class HostPlanTC:
     blocks, and the FP64 -> FP32 staging tasks of L, R (once per local problem) and theta (every
     matvec). Derived from the FP64 plan `hp`, whose block structure it keeps."""
 
-    def __init__(self, hp: HostPlan3, theta: Layout, L: Layout, R: Layout):
+    def __init__(self, hp: HostPlan3, theta: Layout, L: Layout, R: Layout, native: bool = True):
         from ._lib import CVT_TASK, TC_SEG
         (t1, s1, _), (t2, c2, i2), (t3, s3, _) = hp.g1, hp.c2, hp.g3_unsplit
+        if native:
+            self._native(t1, s1, t2, t3, s3)
+        else:
+            self._python(t1, s1, t2, t3, s3)
+        self.tiles1 = _tiles(self.t1, self.s1, TC_TILE)
+        self.tiles3 = _tiles(self.t3, self.s3, TC_TILE)
+        self.c2, self.items2 = c2, i2
+        self.cvt_items = {k: _cvt_items(v) for k, v in self.cvt.items()}
+        self.stage_elems = _rup(self.cursor, TC_ALIGN)    # hi region; lo at +stage_elems
+        self.y32_elems = hp.ws1
+        self.out_layout = hp.out_layout
+        self.macs = hp.macs
+
+    def _native(self, t1, s1, t2, t3, s3):
+        """The tables by tnk_plan_tc_build."""
+        from ._lib import CVT_TASK, TC_SEG
+        c = lambda a: np.ascontiguousarray(a)
+        t1, s1, t2, t3, s3 = c(t1), c(s1), c(t2), c(t3), c(s3)
+        lib = _lib.lib()
+        h = C.c_void_p()
+        _lib.check(lib.tnk_plan_tc_build(t1.ctypes.data, len(t1), s1.ctypes.data, t2.ctypes.data,
+                                         len(t2), t3.ctypes.data, len(t3), s3.ctypes.data,
+                                         C.byref(h)), "tnk_plan_tc_build")
+        maps_dt = np.dtype([("off", "<i8"), ("rows", "<i8"), ("cols", "<i8"), ("ld", "<i8")])
+        try:
+            (self.t1, self.s1, self.t2, self.t3, self.s3, maps, cl, cr, ct), sc = _planb_read(
+                h, [(10, GEMM_TASK), (11, TC_SEG), (12, COMB_TASK), (13, GEMM_TASK),
+                    (14, TC_SEG), (15, maps_dt), (16, CVT_TASK), (17, CVT_TASK),
+                    (18, CVT_TASK)])
+        finally:
+            lib.tnk_planb_free(h)
+        self.maps = maps.view(np.int64).reshape(-1, 4)
+        self.cvt = {"L": cl, "R": cr, "T": ct}
+        self.cursor = sc[4]
+
+    def _python(self, t1, s1, t2, t3, s3):
+        """The same tables in Python (the statement the native planner is tested against)."""
+        from ._lib import CVT_TASK, TC_SEG
         self.cursor = 0
         self.maps: List[tuple] = []
         map_of: Dict[tuple, int] = {}
@@ -892,23 +1071,17 @@ class HostPlanTC:
         mk = lambda rows, dt: np.array(rows, dtype=dt) if rows else np.zeros(0, dt)
         self.t1, self.s1 = mk(T1, GEMM_TASK), mk(S1, TC_SEG)
         self.t3, self.s3 = mk(T3, GEMM_TASK), mk(S3, TC_SEG)
-        self.tiles1 = _tiles(self.t1, self.s1, TC_TILE)
-        self.tiles3 = _tiles(self.t3, self.s3, TC_TILE)
         self.t2 = mk(T2, COMB_TASK)
-        self.c2, self.items2 = c2, i2
         self.cvt = {k: mk(v, CVT_TASK) for k, v in cvt.items()}
-        self.cvt_items = {k: _cvt_items(v) for k, v in cvt.items()}
-        self.stage_elems = _rup(self.cursor, TC_ALIGN)    # hi region; lo at +stage_elems
-        self.y32_elems = hp.ws1
-        self.out_layout = hp.out_layout
-        self.macs = hp.macs
+        self.maps = np.array(self.maps, np.int64).reshape(-1, 4)
 
     def map_desc(self) -> np.ndarray:
         """(offset, rows, cols, ld) of every tensor map, hi and lo interleaved."""
-        d = np.zeros((2 * len(self.maps), 4), np.int64)
-        for i, (off, r, c, ld) in enumerate(self.maps):
-            d[2 * i] = (off, r, c, ld)
-            d[2 * i + 1] = (off + self.stage_elems, r, c, ld)
+        m = np.asarray(self.maps, np.int64).reshape(-1, 4)
+        d = np.zeros((2 * len(m), 4), np.int64)
+        d[0::2] = m
+        d[1::2] = m
+        d[1::2, 0] += self.stage_elems
         return d
 
 
