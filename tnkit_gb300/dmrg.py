@@ -62,8 +62,10 @@ class DMRGOptions:
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
     svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
-    env_precision: str = "f64"            # 'f64' or 'ff': environment updates in float-float
-                                          # (~2x faster; ~10x larger energy error, ~1e-13)
+    env_precision: str = "auto"           # 'f64', 'ff' (environment updates in float-float:
+                                          # ~2x faster, ~10x larger energy error, ~1e-13) or
+                                          # 'auto': float-float in the tensor-core-only sweeps
+                                          # of the 'sweep' schedule, FP64 everywhere else
 
 
 def _resolve(options, kw) -> DMRGOptions:
@@ -161,9 +163,13 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     for i in range(N - 1, 0, -1):
         R[i] = ops.update_right_env(R[i + 1], M[i], W[i])
 
-    if o.env_precision not in ("f64", "ff"):
-        raise ValueError("env_precision must be 'f64' or 'ff'")
-    env_prec = o.env_precision
+    if o.env_precision not in ("f64", "ff", "auto"):
+        raise ValueError("env_precision must be 'f64', 'ff' or 'auto'")
+
+    def env_prec():
+        if o.env_precision == "auto":
+            return "ff" if tc_only_sweep() else "f64"
+        return o.env_precision
     energies, sweep_s, alphas = [], [], []
     phase = {"eig": 0.0, "trunc": 0.0, "env": 0.0}
     counts = {"lo": 0, "hi": 0}
@@ -173,11 +179,14 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     def sync():
         torch.cuda.current_stream().synchronize()
 
+    def tc_only_sweep():
+        return (o.precision in ("mixed", "mixed-ff") and o.mixed_schedule == "sweep"
+                and sweep_no["n"] < o.n_sweeps - max(0, o.polish_sweeps))
+
     def eigsolve(theta: BlockTensor, i: int):
         nonlocal mv_calls
         hi = "ff" if o.precision in ("ff", "mixed-ff") else "f64"
-        tc_only = (o.precision in ("mixed", "mixed-ff") and o.mixed_schedule == "sweep"
-                   and sweep_no["n"] < o.n_sweeps - max(0, o.polish_sweeps))
+        tc_only = tc_only_sweep()
         op = None if tc_only else ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1],
                                                       R[i + 2], precision=hi)
         n = theta.layout.size
@@ -219,9 +228,10 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         phase["trunc"] += time.perf_counter() - t0
         t0 = time.perf_counter()
         if right:
-            L[i + 1] = ops.update_left_env(L[i], M[i], W[i], precision=env_prec)
+            L[i + 1] = ops.update_left_env(L[i], M[i], W[i], precision=env_prec())
         else:
-            R[i + 1] = ops.update_right_env(R[i + 2], M[i + 1], W[i + 1], precision=env_prec)
+            R[i + 1] = ops.update_right_env(R[i + 2], M[i + 1], W[i + 1],
+                                            precision=env_prec())
         sync()
         phase["env"] += time.perf_counter() - t0
         return e
