@@ -173,6 +173,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--sweep", action="store_true",
                     help="also run the whole chi=1024 DMRG (6 sweeps, FP64 and mixed): minutes")
+    ap.add_argument("--batch", action="store_true",
+                    help="also time the 64-chain batched local problems (sequential, batched, "
+                         "graph-captured)")
     ap.add_argument("--sweep-chi", type=int, default=1024)
     ap.add_argument("--sweep-n", type=int, default=64)
     ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
@@ -360,6 +363,8 @@ def main():
                                      "float_float": per_step + 1}
     if args.sweep:
         line["sweep"] = sweep_leg(torch, args)
+    if args.batch:
+        line["batch"] = batch_leg(torch, dev, flush, max(args.steps, 5))
     if not args.no_cpu:
         dt, reps = cpu_matvec_baseline(th, L, W1, W2, R)
         line["cpu_baseline"] = {"value": flops_ref / dt / 1e9, "unit": "GFLOP/s",
@@ -464,6 +469,76 @@ def ff_leg(torch, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps, ms64, d
     return {"value": gf, "unit": "GFLOP/s", "ms_per_step": mms, "speedup_vs_fp64": ms64 / mms,
             "max_rel_err_vs_fp64": err, "dtype": "f32x2 (float-float, 48-bit)",
             "vs_measured_dgemm_peak": gf / 1e3 / dgemm}
+
+
+def batch_leg(torch, dev, flush, steps):
+    """The batched-solve workload: the mid-bond local problems of 64 chains (half dense
+    transverse-field Ising, half U(1) XXZ; N in {16, ..., 64}, chi in {64, 128, 256}; seed 2)
+    applied one operator per chain (a launch sequence each), as one batched operator (one
+    launch per stage for all 64), and as that operator captured in a CUDA graph, FP64 and
+    float-float. L2 flushed before every timed step; CUDA events on the launching stream."""
+    from tnkit_gb300 import batch as B, ops
+    probs = B.batch_problems(64, seed=2, device=dev)
+    singles = [ops.TwoSiteOperator(th, L, W1, W2, R) for th, L, W1, W2, R in probs]
+    op = B.BatchedTwoSiteOperator(probs)
+    opf = B.BatchedTwoSiteOperator(probs, precision="ff")
+    flops = 2 * op.ref_macs
+    x = torch.randn(op.n, dtype=torch.float64, device=dev)
+    y, yf, yg = (torch.empty_like(x) for _ in range(3))
+    xs, ys = op.split(x), [torch.empty_like(v) for v in op.split(x)]
+    stream = torch.cuda.current_stream()
+
+    def run_seq():
+        for o, a, b in zip(singles, xs, ys):
+            o(a, b)
+    for _ in range(3):
+        run_seq()
+        op(x, y)
+        opf(x, yf)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        op(x, yg)
+    graph.replay()
+    torch.cuda.synchronize()
+    ref = torch.cat(ys)
+    err = float((y - ref).abs().max() / ref.abs().max())
+    errf = float((yf - ref).abs().max() / ref.abs().max())
+    errg = float((yg - y).abs().max())
+
+    def timed(fn):
+        t = 0.0
+        for i in range(steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t += a.elapsed_time(b) / 1e3
+        ms = t / steps * 1e3
+        return {"ms_per_step": ms, "value": flops / (ms / 1e3) / 1e9, "unit": "GFLOP/s"}
+    seq = timed(run_seq)
+    bat = timed(lambda: op(x, y))
+    gra = timed(graph.replay)
+    bff = timed(lambda: opf(x, yf))
+    draws = B.chain_draws(64, 2)
+
+    def launches(hp):      # stages with work (an empty stage launches nothing)
+        return sum(len(t) > 0 for t in (hp.g1[2], hp.c2[2], hp.g3[2], hp.c4[2]))
+    n_seq, n_bat = sum(launches(o.plan.host) for o in singles), launches(op.host)
+    return {"workload": "mid-bond two-site H_eff of 64 chains: 32 dense transverse-field Ising "
+                        "(g in [0.5, 1.5]), 32 U(1) XXZ (Delta in [0, 2]), N in {16, 24, 32, 48, "
+                        "64}, chi in {64, 128, 256}, seed 2; random environments",
+            "chains": len(probs), "entries": op.n,
+            "chi_counts": {str(c): sum(1 for *_, ch in draws if ch == c) for c in (64, 128, 256)},
+            "gflop_per_step": flops / 1e9,
+            "sequential_f64": dict(seq, launches=n_seq),
+            "batched_f64": dict(bat, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
+                                bat["ms_per_step"], max_rel_err_vs_sequential=err),
+            "graph_f64": dict(gra, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
+                              gra["ms_per_step"], max_abs_diff_vs_batched=errg),
+            "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf)}
 
 
 def sweep_leg(torch, args):

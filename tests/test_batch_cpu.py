@@ -1,0 +1,53 @@
+"""Batched local problems on the CPU: the concatenated tables of K independent two-site problems
+(dense Ising and U(1) XXZ chains of different sizes), run through the table interpreter, give
+each problem's own matvec; the batched-solve workload's draws are reproducible."""
+import numpy as np
+import pytest
+
+from tnkit_gb300 import batch as B
+from tnkit_gb300 import plan as P
+from tnkit_gb300.ops import _host_of
+from table_interp import run_plan3
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_batched_tables_match_each_problem():
+    specs = [("tfim", 0.7, 16, 16), ("xxz", 0.3, 16, 32), ("tfim", 1.3, 24, 32),
+             ("xxz", 1.7, 24, 16), ("xxz", 1.0, 32, 24), ("tfim", 1.0, 8, 8)]
+    probs = [B.chain_problem(*s, seed=50 + k, device="cpu") for k, s in enumerate(specs)]
+    plans = [P.plan_apply(th, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
+                          R.layout) for th, L, W1, W2, R in probs]
+    sizes = np.array([[L.host.size, th.size, R.host.size, hp.ws1 + hp.ws2_unsplit]
+                      for (th, L, _, _, R), hp in zip(probs, plans)], np.int64)
+    starts = np.vstack([np.zeros(4, np.int64), np.cumsum(sizes, 0)])
+    hb = B.batch_plan(plans, [tuple(int(v) for v in starts[k]) for k in range(len(plans))],
+                      [int(starts[k, 1]) for k in range(len(plans))], int(starts[-1, 3]),
+                      int(starts[-1, 1]))
+    rng = np.random.default_rng(3)
+    thetas = [rng.standard_normal(th.size) for th, *_ in probs]
+    Lcat = np.concatenate([p[1].host for p in probs])
+    Rcat = np.concatenate([p[4].host for p in probs])
+    got = run_plan3(hb, Lcat, np.concatenate(thetas), Rcat)
+    assert hb.macs == sum(hp.macs for hp in plans)
+    for k, ((th, L, W1, W2, R), hp) in enumerate(zip(probs, plans)):
+        want = run_plan3(hp, L.host, thetas[k], R.host)
+        assert _rel(got[starts[k, 1]:starts[k + 1, 1]], want) <= 1e-13
+
+
+def test_chain_draws_reproducible():
+    d = B.chain_draws(64, 2)
+    assert d == B.chain_draws(64, 2) and len(d) == 64
+    assert sum(m == "tfim" for m, *_ in d) == 32
+    for m, g, N, chi in d:
+        assert N in (16, 24, 32, 48, 64) and chi in (64, 128, 256)
+        assert (0.5 <= g <= 1.5) if m == "tfim" else (0.0 <= g <= 2.0)
+
+
+@pytest.mark.parametrize("N,chi", [(16, 64), (16, 256), (64, 256), (8, 1024)])
+def test_mid_bond_sectors(N, chi):
+    ch, dims = B._mid_bond_sectors(N, chi)
+    assert sum(dims) == min(chi, 2 ** (N // 2)) and all(d >= 1 for d in dims)
+    assert ch == sorted(ch) and ch == [-c for c in reversed(ch)]
