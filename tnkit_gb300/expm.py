@@ -24,6 +24,26 @@ from . import _lib
 _MAXNV = 64
 
 
+def _expm_col(tau, alphas, betas, route: str = "eigh") -> np.ndarray:
+    """The first column of exp(tau T) for the real symmetric tridiagonal T of the Lanczos
+    coefficients. 'eigh' (default): T = Z diag(lam) Z^T by LAPACK's tridiagonal solver, then
+    exp(tau T) e_1 = Z (exp(tau lam) * Z[0, :]) -- exact to eigensolver accuracy, O(j^2) after
+    the O(j^2) eigensolve, the route the reference offers as `expm_sym_tridiag_eigh`
+    (tnkit/backend.py:643-661); 'pade': scipy's scaling and squaring on the complex j x j
+    matrix, the reference's per-iteration host call (tnkit/eigensolver.py:260)."""
+    j = len(alphas)
+    if route == "pade":
+        return scipy.linalg.expm(tau * _tridiag(alphas, betas))[:, 0]
+    if route != "eigh":
+        raise ValueError("route must be 'eigh' or 'pade'")
+    d = np.asarray(alphas, np.float64)
+    if j == 1:
+        return np.exp(tau * d).astype(complex)
+    lam, Z = scipy.linalg.eigh_tridiagonal(d, np.asarray(betas[:j - 1], np.float64),
+                                           check_finite=False)
+    return Z @ (np.exp(tau * lam) * Z[0, :])
+
+
 def _tridiag(alphas, betas) -> np.ndarray:
     j = len(alphas)
     T = np.diag(np.asarray(alphas, np.float64)).astype(complex)
@@ -36,8 +56,9 @@ def _tridiag(alphas, betas) -> np.ndarray:
 class ExpmMonitor:
     """Breakdown test, Saad's estimate, adaptive stop and the final coefficients."""
 
-    def __init__(self, tau, beta0, tol, adaptive, info, est_ref_j=2):
+    def __init__(self, tau, beta0, tol, adaptive, info, est_ref_j=2, route="eigh"):
         self.tau, self.beta0, self.tol, self.adaptive = tau, beta0, tol, adaptive
+        self.route = route
         self.info, self.est_ref_j = info, est_ref_j
         self.est = float("inf")
         self.est_ref, self.est_ref_at, self.beta1 = float("nan"), 0, float("nan")
@@ -52,8 +73,8 @@ class ExpmMonitor:
         jj = len(alphas)
         want_ref = self.info is not None and self.est_ref_at == 0 and jj >= self.est_ref_j
         if (self.adaptive and jj >= 2) or want_ref:
-            Et = scipy.linalg.expm(self.tau * _tridiag(alphas, betas))
-            self.est = abs(beta) * abs(self.tau) * abs(Et[jj - 1, 0]) * self.beta0
+            e1 = _expm_col(self.tau, alphas, betas, self.route)
+            self.est = abs(beta) * abs(self.tau) * abs(e1[jj - 1]) * self.beta0
             if want_ref:
                 self.est_ref, self.est_ref_at = self.est, jj
             if self.adaptive and jj >= 2 and self.est < self.tol:
@@ -61,7 +82,7 @@ class ExpmMonitor:
         return None
 
     def finish(self, alphas, betas, capped):
-        c = self.beta0 * scipy.linalg.expm(self.tau * _tridiag(alphas, betas))[:, 0]
+        c = self.beta0 * _expm_col(self.tau, alphas, betas, self.route)
         if self.info is not None:
             self.info.update(krylov_dim=len(alphas), err_est=self.est, beta1=self.beta1,
                              est_ref=self.est_ref, est_ref_j=self.est_ref_at, capped=capped)
@@ -74,8 +95,10 @@ def _real(x: torch.Tensor) -> torch.Tensor:
 
 def lanczos_expm(matvec: Callable, v: torch.Tensor, tau: complex, m: int = 30,
                  tol: float = 1e-12, adaptive: bool = True, info: Optional[dict] = None,
-                 est_ref_j: int = 2) -> torch.Tensor:
-    """exp(tau H) v for Hermitian H given as `matvec(x, out)` on complex128 CUDA vectors."""
+                 est_ref_j: int = 2, route: str = "eigh") -> torch.Tensor:
+    """exp(tau H) v for Hermitian H given as `matvec(x, out)` on complex128 CUDA vectors. The
+    per-iteration Saad estimate and the final coefficients take exp(tau T) e_1 by `route`
+    ('eigh': the tridiagonal eigendecomposition; 'pade': scipy's expm of the j x j matrix)."""
     if not (v.is_cuda and v.dtype == torch.complex128):
         raise TypeError("lanczos_expm needs a complex128 CUDA vector")
     if m + 1 > _MAXNV:
@@ -101,7 +124,7 @@ def lanczos_expm(matvec: Callable, v: torch.Tensor, tau: complex, m: int = 30,
     beta0 = float(read()[0])
     if not math.isfinite(beta0) or beta0 < 1e-300:
         return v.clone()
-    mon = ExpmMonitor(tau, beta0, tol, adaptive, info, est_ref_j)
+    mon = ExpmMonitor(tau, beta0, tol, adaptive, info, est_ref_j, route)
     V = torch.empty((m + 1, n), dtype=torch.complex128, device=dev)
     _lib.check(lib.tnk_scale_div_f64(_real(v).data_ptr(), _real(V[0]).data_ptr(), 2 * n, a(0),
                                      1.0, sp), "scale_div")
