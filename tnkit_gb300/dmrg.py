@@ -66,6 +66,9 @@ class DMRGOptions:
                                           # ~2x faster, ~10x larger energy error, ~1e-13) or
                                           # 'auto': float-float in the tensor-core-only sweeps
                                           # of the 'sweep' schedule, FP64 everywhere else
+    graph: bool = False                   # replay each local problem's FP64 / float-float
+                                          # matvec from a CUDA graph after one eager call
+                                          # (as the reference's MatvecGraph)
 
 
 def _resolve(options, kw) -> DMRGOptions:
@@ -189,6 +192,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         tc_only = tc_only_sweep()
         op = None if tc_only else ops.TwoSiteOperator(theta.layout, L[i], W[i], W[i + 1],
                                                       R[i + 2], precision=hi)
+        if o.graph and op is not None:
+            op = ops.GraphedOperator(op, theta.layout.size, device=device)
         n = theta.layout.size
         mi = o.max_iter if o.max_iter is not None else min(n, max(200, 4 * chi))
         need = (o.restart_m + 1) * n
