@@ -99,6 +99,7 @@ class _Concurrent:
         self.pool = cf.ThreadPoolExecutor(workers, thread_name_prefix="tnk-svd")
         self.streams = {}
         self.lock = threading.Lock()
+        self.warmed = set()
 
     def stream(self, device, i):
         with self.lock:
@@ -107,8 +108,22 @@ class _Concurrent:
                 self.streams[key] = torch.cuda.Stream(device=device)
             return self.streams[key]
 
+    def _warm(self, device):
+        """torch.linalg's CUDA libraries are loaded lazily, and the first call must not come
+        from several threads at once (torch raises "lazy wrapper should be called at most
+        once"): make the first calls here, on the calling thread, once per device."""
+        key = str(device)
+        if key in self.warmed:
+            return
+        a = torch.eye(2, dtype=torch.float64, device=device)
+        torch.linalg.qr(a)
+        torch.linalg.eigh(a)
+        torch.linalg.svd(a, full_matrices=False)
+        self.warmed.add(key)
+
     def map(self, fn, mats, device):
         """fn(M) for each M (or fn[i](M_i) when fn is a list), one stream per item."""
+        self._warm(device)
         main = torch.cuda.current_stream(device)
         streams = [self.stream(device, i) for i in range(len(mats))]
         for s in streams:
