@@ -112,6 +112,38 @@ def right_canonicalize(M: List[BlockTensor], scal: LA.Scalars) -> List[BlockTens
     return M
 
 
+def setup_chain(mpo, chi: int, o: DMRGOptions, device):
+    """MPO tensors on the device, the initial MPS (o.init_mps, or the seeded random one),
+    right-canonicalised, and the environments of a sweep's start: (W, M, L, R, block)."""
+    block = isinstance(mpo[0], BlockTensor)
+    if block and (o.charge is None) == (o.init_mps is None):
+        raise ValueError("a block MPO needs exactly one of charge= and a block init_mps")
+    if not block and o.charge is not None:
+        raise ValueError("charge= needs a block MPO (convert it with to_block_mpo first)")
+    N = len(mpo)
+    if block:
+        W = list(mpo)
+        for w in W:
+            if w.data.device != device:
+                w.data = w.data.to(device)
+    else:
+        W = dense_mpo([np.asarray(w) for w in mpo], device=device)
+    if o.init_mps is not None:
+        M = [BlockTensor(m.layout, m.data.to(device).clone()) for m in o.init_mps]
+    elif block:
+        M = random_block_mps(W, chi, o.charge, np.random.default_rng(o.seed), device=device)
+    else:
+        d = W[0].legs[2].size
+        M = random_dense_mps(N, chi, d, np.random.default_rng(o.seed), device=device)
+    M = right_canonicalize(M, LA.Scalars(device))
+    L: List[Optional[BlockTensor]] = [None] * (N + 1)
+    R: List[Optional[BlockTensor]] = [None] * (N + 1)
+    L[0], R[N] = edge_envs(M, W, device)
+    for i in range(N - 1, 0, -1):
+        R[i] = ops.update_right_env(R[i + 1], M[i], W[i])
+    return W, M, L, R, block
+
+
 def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
     """Ground state of an MPO by two-site DMRG on the GPU. See the module docstring."""
     if chi is None:
@@ -137,34 +169,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         raise ValueError("n_sweeps must be >= 1")
     device = torch.device(o.device) if o.device is not None else torch.device(
         "cuda", torch.cuda.current_device())
-    block = isinstance(mpo[0], BlockTensor)
-    if block and (o.charge is None) == (o.init_mps is None):
-        raise ValueError("a block MPO needs exactly one of charge= and a block init_mps")
-    if not block and o.charge is not None:
-        raise ValueError("charge= needs a block MPO (convert it with to_block_mpo first)")
-    N = len(mpo)
-    if block:
-        W = list(mpo)
-        for w in W:
-            if w.data.device != device:
-                w.data = w.data.to(device)
-    else:
-        W = dense_mpo([np.asarray(w) for w in mpo], device=device)
-    if o.init_mps is not None:
-        M = [BlockTensor(m.layout, m.data.to(device).clone()) for m in o.init_mps]
-    elif block:
-        M = random_block_mps(W, chi, o.charge, np.random.default_rng(o.seed), device=device)
-    else:
-        d = W[0].legs[2].size
-        M = random_dense_mps(N, chi, d, np.random.default_rng(o.seed), device=device)
-    scal = LA.Scalars(device)
-    M = right_canonicalize(M, scal)
-
-    L: List[Optional[BlockTensor]] = [None] * (N + 1)
-    R: List[Optional[BlockTensor]] = [None] * (N + 1)
-    L[0], R[N] = edge_envs(M, W, device)
-    for i in range(N - 1, 0, -1):
-        R[i] = ops.update_right_env(R[i + 1], M[i], W[i])
+    W, M, L, R, block = setup_chain(mpo, chi, o, device)
+    N = len(W)
 
     if o.env_precision not in ("f64", "ff", "auto"):
         raise ValueError("env_precision must be 'f64', 'ff' or 'auto'")
