@@ -51,3 +51,34 @@ def test_mid_bond_sectors(N, chi):
     ch, dims = B._mid_bond_sectors(N, chi)
     assert sum(dims) == min(chi, 2 ** (N // 2)) and all(d >= 1 for d in dims)
     assert ch == sorted(ch) and ch == [-c for c in reversed(ch)]
+
+
+def test_launch_units_owned_by_their_problem():
+    """Every tile and combination item of a batched plan maps to the problem whose buffers it
+    touches (the basis of dropping converged problems' launch grids)."""
+    specs = [("xxz", 1.0, 32, 64), ("tfim", 0.9, 16, 48), ("xxz", 0.4, 24, 32)]
+    probs = [B.chain_problem(*s, seed=70 + k, device="cpu") for k, s in enumerate(specs)]
+    plans = [P.plan_apply(th, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
+                          R.layout) for th, L, W1, W2, R in probs]
+    sizes = np.array([[L.host.size, th.size, R.host.size, hp.ws1 + hp.ws2_unsplit]
+                      for (th, L, _, _, R), hp in zip(probs, plans)], np.int64)
+    starts = np.vstack([np.zeros(4, np.int64), np.cumsum(sizes, 0)])
+    hb = B.batch_plan(plans, [tuple(int(v) for v in starts[k]) for k in range(3)],
+                      [int(starts[k, 1]) for k in range(3)], int(starts[-1, 3]),
+                      int(starts[-1, 1]))
+    op = B.BatchedTwoSiteOperator.__new__(B.BatchedTwoSiteOperator)
+    op.host = hb
+    op._owners(plans, starts)
+    own1, own2, own3, own4 = op._own
+    t1, s1, tl1 = hb.g1
+    assert np.array_equal(own1, np.searchsorted(starts[:, 3], t1["c_off"][tl1["task"]],
+                                                side="right") - 1)
+    t3, s3, tl3 = hb.g3
+    for o, t in zip(own3, tl3["task"]):
+        sb, se = int(t3["seg_begin"][t]), int(t3["seg_end"][t])
+        assert ((s3["b_off"][sb:se] >= starts[o, 2]) & (s3["b_off"][sb:se] < starts[o + 1, 2])).all()
+    t4 = hb.c4[0]
+    if len(t4):
+        assert np.array_equal(own4, np.searchsorted(starts[:, 1], t4["dst_off"][hb.c4[2]["task"]],
+                                                    side="right") - 1)
+    assert len(own2) == len(hb.c2[2]) and own2.max() == 2

@@ -63,3 +63,23 @@ def test_batched_rejects_wrong_length(problems):
     op = B.BatchedTwoSiteOperator(problems[:3])
     with pytest.raises(ValueError):
         op(torch.zeros(op.n + 1, dtype=torch.float64, device="cuda"))
+
+
+def test_set_active_skips_only_the_masked_problems(problems):
+    """Dropping problems' launch grids leaves the others' results bit-identical and the
+    dropped problems' output untouched; restoring the mask restores the full result."""
+    from tnkit_gb300 import batch as B
+    op = B.BatchedTwoSiteOperator(problems[:10])
+    x = torch.randn(op.n, dtype=torch.float64, device="cuda")
+    full = op(x)
+    mask = np.array([k % 3 != 1 for k in range(10)])
+    op.set_active(mask)
+    y = torch.full_like(x, 7.0)
+    op(x, y)
+    for k, (a, b) in enumerate(zip(op.split(y), op.split(full))):
+        if mask[k]:
+            assert torch.equal(a, b), k
+        else:
+            assert bool((a == 7.0).all()), k
+    op.set_active(np.ones(10, bool))
+    assert torch.equal(op(x), full)

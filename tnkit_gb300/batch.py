@@ -120,6 +120,10 @@ class BatchedTwoSiteOperator:
                         self.n)
         self.host = hp
         self.plan = ops.DevicePlan3(hp, dev, ff=precision == "ff")
+        self.K = len(plans)
+        self._owners(plans, starts)
+        self.active = np.ones(self.K, bool)
+        self._mask_buf = None
         self.macs = hp.macs
         self.ref_macs = sum(P.two_site_ref_macs(th, L.layout, W1.layout, W2.layout, R.layout)
                             for th, L, W1, W2, R in problems)
@@ -136,6 +140,47 @@ class BatchedTwoSiteOperator:
                 _lib.check(lib.tnk_ff_split(src.data_ptr(), dst.data_ptr(), src.numel(), sp),
                            "ff split")
         self.calls = 0
+
+    def _owners(self, plans, starts):
+        """The problem each launch unit (GEMM tile, combination item) belongs to."""
+        hp = self.host
+        K = len(plans)
+        task1 = np.repeat(np.arange(K), [len(p.g1[0]) for p in plans])
+        task2 = np.repeat(np.arange(K), [len(p.c2[0]) for p in plans])
+        t3, s3, _ = hp.g3
+        # an output task by where it writes; a split-K partial (flags bit 4, written to the
+        # shared partial region) by where its first K segment reads its Z block
+        task3 = np.searchsorted(starts[:, 1], t3["c_off"], side="right") - 1
+        part = np.nonzero(t3["flags"] & 16)[0]
+        if len(part):
+            task3[part] = np.searchsorted(starts[:, 3], s3["a_off"][t3["seg_begin"][part]],
+                                          side="right") - 1
+        task4 = (np.searchsorted(starts[:, 1], hp.c4[0]["dst_off"], side="right") - 1
+                 if len(hp.c4[0]) else np.zeros(0, np.int64))
+        self._own = (task1[hp.g1[2]["task"]], task2[hp.c2[2]["task"]],
+                     task3[hp.g3[2]["task"]], task4[hp.c4[2]["task"]])
+
+    def set_active(self, mask) -> None:
+        """Apply only the problems where `mask` is true from now on: the launch grids (tiles
+        and combination items) of the others are dropped; tables and buffers stay. A skipped
+        problem's part of the output is left as it was."""
+        mask = np.asarray(mask, bool)
+        if mask.shape != (self.K,):
+            raise ValueError(f"need one flag per problem ({self.K})")
+        if np.array_equal(mask, self.active):
+            return
+        hp = self.host
+        units = [hp.g1[2], hp.c2[2], hp.g3[2], hp.c4[2]]
+        kept = [u[mask[o]] for u, o in zip(units, self._own)]
+        buf, offs = ops._pack(kept, self.device)
+        base = buf.data_ptr()
+        c = self.plan.c
+        c.tiles1, c.n_tiles1 = base + offs[0], len(kept[0])
+        c.items2, c.n_items2 = base + offs[1], len(kept[1])
+        c.tiles3, c.n_tiles3 = base + offs[2], len(kept[2])
+        c.items4, c.n_items4 = base + offs[3], len(kept[3])
+        self._mask_buf = buf
+        self.active = mask.copy()
 
     def __call__(self, x: torch.Tensor, out: torch.Tensor = None) -> torch.Tensor:
         if x.numel() != self.n:

@@ -144,6 +144,8 @@ def lanczos_ground_batched(op, x0: torch.Tensor, offsets: Sequence[int], tol: fl
         keep = np.nonzero(~done)[0]
         if len(keep) == 0:
             break
+        if done.any() and hasattr(op, "set_active"):
+            op.set_active(active)                     # converged chains leave the launches
         if cur >= m:                                  # thick restart, all chains in step
             kk = min(k, cur - 1)
             for q in keep:
@@ -224,30 +226,36 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
         matvecs += info["matvecs"]
         sync()
         phase["eig"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        fused = []
         for q, c in enumerate(act):
-            ch = chains[c]
-            i, right = ch["sched"][r]
-            t0 = time.perf_counter()
             x = BlockTensor(thetas[q].layout, X[int(op.offsets[q]):int(op.offsets[q + 1])])
-            mat, finfo = LA.fuse_matrix(x, 2)
-            U, S, Vh, disc = LA.truncated_svd(mat, ch["chi"], scale="right" if right else "left",
-                                              driver=o.svd_driver, method=o.svd_method)
+            fused.append(LA.fuse_matrix(x, 2))
+        facs = LA.truncated_svd_many(
+            [(mat, chains[c]["chi"], "right" if chains[c]["sched"][r][1] else "left")
+             for (mat, _), c in zip(fused, act)], driver=o.svd_driver, method=o.svd_method)
+        for (U, S, Vh, disc), (_, finfo), c in zip(facs, fused, act):
+            ch = chains[c]
+            i, _ = ch["sched"][r]
             ch["M"][i] = LA.split_rows(U, finfo)
             ch["M"][i + 1] = LA.split_cols(Vh, finfo)
             ch["disc"] += disc
-            sync()
-            phase["trunc"] += time.perf_counter() - t0
-            t0 = time.perf_counter()
+        sync()
+        phase["trunc"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for q, c in enumerate(act):
+            ch = chains[c]
+            i, right = ch["sched"][r]
             if right:
                 ch["L"][i + 1] = ops.update_left_env(ch["L"][i], ch["M"][i], ch["W"][i])
             else:
                 ch["R"][i + 1] = ops.update_right_env(ch["R"][i + 2], ch["M"][i + 1],
                                                       ch["W"][i + 1])
-            sync()
-            phase["env"] += time.perf_counter() - t0
             E_last[c] = E[q]
             if (r + 1) % ch["per_sweep"] == 0:
                 ch["energies"].append(float(E[q]))
+        sync()
+        phase["env"] += time.perf_counter() - t0
     energies = [float(e) for e in E_last]
     return energies, [ch["M"] for ch in chains], {
         "energies": [ch["energies"] for ch in chains], "rounds": rounds,

@@ -407,6 +407,73 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
         facs = [(pick(M, fn1) if fn is _svd_gram_native else fn1)(M) for M in mats]
     if low:
         facs = [(U.double(), S.double(), Vh.double(), h) for U, S, Vh, h in facs]
+    return _trunc_finish(m, blocks, facs, chi, scale, normalize)
+
+
+def _gram_pick(scale: str):
+    """The Gram factorisation per sector shape: the side the sweep keeps canonical straight from
+    its own Gram matrix for near-square sectors (orth 1 / 2), else the reference's QR form."""
+    def pick(M, base):
+        R, Cc = M.shape
+        o = 1 if scale == "right" and R <= 1.25 * Cc else \
+            2 if scale == "left" and Cc <= 1.25 * R else 0
+        return (lambda X: base(X, o)) if o else base
+    return pick
+
+
+def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool = True,
+                       host: str = "auto"):
+    """truncated_svd of several FP64 CUDA block matrices -- e.g. one bond of each of many
+    chains -- given as [(m, chi, scale)], with the sectors of all of them factored in one
+    concurrent pass (GPU sectors a stream each, with method='gram' the host LAPACK share
+    assigned over all sectors together). Returns the list of (U, S, Vh, disc)."""
+    if host not in ("auto", "never", "always"):
+        raise ValueError("host must be 'auto', 'never' or 'always'")
+    if method not in ("svd", "gram"):
+        raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
+    per, fns, mats, shapes = [], [], [], []
+    for m, chi, scale in items:
+        if chi < 1:
+            raise ValueError(f"chi must be at least 1, got {chi}")
+        if not (m.data.is_cuda and m.data.dtype == torch.float64):
+            raise TypeError("truncated_svd_many takes FP64 CUDA block matrices")
+        blocks = list(_blocks(m))
+        per.append((m, chi, scale, blocks, len(mats)))
+        for _, _, M in blocks:
+            mats.append(M)
+            shapes.append((tuple(M.shape), scale))
+    if method == "svd":
+        fn = lambda M: tuple(torch.linalg.svd(M, full_matrices=False, driver=driver)) + (None,)
+        facs = _concurrent().map([fn] * len(mats), mats, mats[0].device) if len(mats) > 1 \
+            else [fn(M) for M in mats]
+    else:
+        blas = _host_blas() if host != "never" else None
+        on_host = ([False] * len(mats) if blas is None else
+                   [True] * len(mats) if host == "always" else
+                   _assign_sectors([sh for sh, _ in shapes], True))
+        fns = [_gram_pick(sc)(M, _svd_gram_host if h else _svd_gram_native)
+               if sc in ("right", "left") else (_svd_gram_host if h else _svd_gram_native)
+               for M, (_, sc), h in zip(mats, shapes, on_host)]
+        if any(on_host):
+            prev = blas[1]()
+            blas[0](max(1, prev // _HOST_THREADS_DIV))
+            try:
+                facs = _map_hybrid(fns, mats, on_host, mats[0].device)
+            finally:
+                blas[0](prev)
+        elif len(mats) > 1:
+            facs = _concurrent().map(fns, mats, mats[0].device)
+        else:
+            facs = [f(M) for f, M in zip(fns, mats)]
+    return [_trunc_finish(m, blocks, facs[b:b + len(blocks)], chi, scale, normalize)
+            for m, chi, scale, blocks, b in per]
+
+
+def _trunc_finish(m: BlockTensor, blocks, facs, chi: int, scale: str, normalize: bool):
+    """The global cut over all sectors' singular values (descending, stable: the reference's
+    order, tnkit/blocks.py:1427), the new bond leg, S normalised and folded into the kept
+    factor."""
+    lr, lc = m.layout.legs
     parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
     if not parts:
         raise ValueError("the matrix has no allowed blocks")
