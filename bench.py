@@ -176,6 +176,10 @@ def main():
     ap.add_argument("--batch", action="store_true",
                     help="also time the 64-chain batched local problems (sequential, batched, "
                          "graph-captured)")
+    ap.add_argument("--batch-dmrg", action="store_true",
+                    help="also run the 16-chain batched DMRG against one chain after another: "
+                         "minutes")
+    ap.add_argument("--batch-sweeps", type=int, default=2)
     ap.add_argument("--sweep-chi", type=int, default=1024)
     ap.add_argument("--sweep-n", type=int, default=64)
     ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
@@ -365,6 +369,8 @@ def main():
         line["sweep"] = sweep_leg(torch, args)
     if args.batch:
         line["batch"] = batch_leg(torch, dev, flush, max(args.steps, 5))
+    if args.batch_dmrg:
+        line["batch_dmrg"] = batch_dmrg_leg(torch, args)
     if not args.no_cpu:
         dt, reps = cpu_matvec_baseline(th, L, W1, W2, R)
         line["cpu_baseline"] = {"value": flops_ref / dt / 1e9, "unit": "GFLOP/s",
@@ -539,6 +545,58 @@ def batch_leg(torch, dev, flush, steps):
             "graph_f64": dict(gra, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
                               gra["ms_per_step"], max_abs_diff_vs_batched=errg),
             "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf)}
+
+
+def batch_dmrg_leg(torch, args):
+    """Whole DMRG of a sample of the 64-chain workload -- the first 8 Ising and first 8 XXZ
+    chains of the seed-2 draws, `--batch-sweeps` sweeps each, seeds 0..15 -- run one chain after
+    another with `dmrg` (FP64) and as one lockstep batch (`dmrg_batch`, FP64 and float-float);
+    after an untimed warm-up of both drivers. Wall-clock seconds and the largest energy
+    difference between the batched and the one-by-one runs."""
+    from tnkit_gb300 import batch as B, workloads
+    from tnkit_gb300.batch_dmrg import dmrg_batch
+    from tnkit_gb300.dmrg import dmrg
+    from tnkit_gb300.mpo import to_block_mpo
+    draws = B.chain_draws(64, 2)
+    sel = [d for d in draws if d[0] == "tfim"][:8] + [d for d in draws if d[0] == "xxz"][:8]
+
+    def mk(m, g, N):
+        return workloads.tfim_mpo(N, g) if m == "tfim" else \
+            to_block_mpo(workloads.xxz_mpo(N, g), [[1, -1]] * N)[0]
+    kw = dict(n_sweeps=args.batch_sweeps, tol=0, rtol=0, expand=0)
+    dmrg_batch([mk("tfim", 1.0, 8), mk("xxz", 1.0, 8)], [16, 16], charges=[None, 0],
+               **dict(kw, n_sweeps=1))
+    dmrg(mk("xxz", 1.0, 8), 16, charge=0, **dict(kw, n_sweeps=1))
+    torch.cuda.synchronize()
+    out = {"workload": "DMRG of 16 chains (the first 8 transverse-field Ising and first 8 U(1) "
+                       "XXZ chains of the 64-chain seed-2 draws), "
+                       f"{args.batch_sweeps} sweeps each, seeds 0..15",
+           "chains": [list(d) for d in sel]}
+    for prec in ("f64", "ff"):
+        t0 = time.perf_counter()
+        Eb, _, info = dmrg_batch([mk(m, g, N) for m, g, N, _ in sel],
+                                 [chi for *_, chi in sel],
+                                 charges=[None if m == "tfim" else 0 for m, *_ in sel],
+                                 seeds=list(range(len(sel))), precision=prec, **kw)
+        torch.cuda.synchronize()
+        out[f"batched_{prec}"] = {"s": time.perf_counter() - t0, "phase_time": info["phase_time"],
+                                  "rounds": info["rounds"], "batched_iterations": info["matvecs"],
+                                  "E": Eb}
+    t0 = time.perf_counter()
+    Es, ph = [], {"eig": 0.0, "trunc": 0.0, "env": 0.0}
+    for q, (m, g, N, chi) in enumerate(sel):
+        ckw = dict(kw, seed=q, **({"charge": 0} if m == "xxz" else {}))
+        E, _, inf = dmrg(mk(m, g, N), chi, **ckw)
+        Es.append(E)
+        for k in ph:
+            ph[k] += inf["phase_time"][k]
+    torch.cuda.synchronize()
+    out["sequential_f64"] = {"s": time.perf_counter() - t0, "phase_time": ph, "E": Es}
+    for prec in ("f64", "ff"):
+        b = out[f"batched_{prec}"]
+        b["speedup_vs_sequential_f64"] = out["sequential_f64"]["s"] / b["s"]
+        b["max_abs_dE_vs_sequential"] = float(np.max(np.abs(np.array(b["E"]) - np.array(Es))))
+    return out
 
 
 def sweep_leg(torch, args):
