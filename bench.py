@@ -180,6 +180,8 @@ def main():
                     help="also run the 16-chain batched DMRG against one chain after another: "
                          "minutes")
     ap.add_argument("--batch-sweeps", type=int, default=2)
+    ap.add_argument("--batch-pipeline", action="store_true",
+                    help="batched DMRG with the two chain groups' phases overlapped")
     ap.add_argument("--sweep-chi", type=int, default=1024)
     ap.add_argument("--sweep-n", type=int, default=64)
     ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
@@ -577,11 +579,12 @@ def batch_dmrg_leg(torch, args):
         Eb, _, info = dmrg_batch([mk(m, g, N) for m, g, N, _ in sel],
                                  [chi for *_, chi in sel],
                                  charges=[None if m == "tfim" else 0 for m, *_ in sel],
-                                 seeds=list(range(len(sel))), precision=prec, **kw)
+                                 seeds=list(range(len(sel))), precision=prec,
+                                 pipeline=args.batch_pipeline, **kw)
         torch.cuda.synchronize()
         out[f"batched_{prec}"] = {"s": time.perf_counter() - t0, "phase_time": info["phase_time"],
                                   "rounds": info["rounds"], "batched_iterations": info["matvecs"],
-                                  "E": Eb}
+                                  "pipeline": info["pipeline"], "E": Eb}
     t0 = time.perf_counter()
     Es, ph = [], {"eig": 0.0, "trunc": 0.0, "env": 0.0}
     for q, (m, g, N, chi) in enumerate(sel):

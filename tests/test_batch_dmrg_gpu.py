@@ -49,8 +49,8 @@ def test_batched_lanczos_matches_eigvalsh():
         assert abs(abs(x @ evec[:, 0]) - 1.0) <= 1e-8
 
 
-@pytest.mark.parametrize("precision", ["f64", "ff"])
-def test_dmrg_batch_matches_independent_runs(precision):
+@pytest.mark.parametrize("precision,pipeline", [("f64", True), ("ff", True), ("f64", False)])
+def test_dmrg_batch_matches_independent_runs(precision, pipeline):
     from tnkit_gb300 import workloads
     from tnkit_gb300.batch_dmrg import dmrg_batch
     from tnkit_gb300.dmrg import dmrg
@@ -64,7 +64,7 @@ def test_dmrg_batch_matches_independent_runs(precision):
                               [chi for _, _, chi, _, _ in specs],
                               charges=[None if m == "tfim" else 0 for m, *_ in specs],
                               seeds=[s for *_, s in specs], n_sweeps=sweeps, tol=0, rtol=0,
-                              expand=0, precision=precision)
+                              expand=0, precision=precision, pipeline=pipeline)
     assert info["rounds"] == sweeps * 2 * (16 - 1)
     for (m, N, chi, g, seed), e, es in zip(specs, Eb, info["energies"]):
         assert len(es) == sweeps

@@ -9,6 +9,7 @@ raise.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 from collections import OrderedDict
 from typing import Dict, Optional
 
@@ -147,33 +148,45 @@ class DeviceCombPlan:
 # --------------------------------------------------------------------------- #
 # workspace and plan caches
 # --------------------------------------------------------------------------- #
-_WS: Dict[torch.device, torch.Tensor] = {}
+_WS: Dict[tuple, torch.Tensor] = {}
 
 
 def workspace(n: int, device) -> torch.Tensor:
-    """A grow-only float64 workspace per device (the caller's stream orders its reuse)."""
+    """A grow-only float64 workspace per device and current stream (that stream orders its
+    reuse; work on another stream, e.g. another thread's, gets its own)."""
     device = torch.device(device)
-    w = _WS.get(device)
+    key = (device, torch.cuda.current_stream(device).cuda_stream if device.type == "cuda"
+           else 0)
+    w = _WS.get(key)
     if w is None or w.numel() < n:
         w = torch.empty(max(n, 1 << 16), dtype=torch.float64, device=device)
-        _WS[device] = w
+        _WS[key] = w
     return w
 
 
 class _LRU(OrderedDict):
+    """Bounded cache of plans; safe to share between host threads (a plan may be built twice
+    when two threads miss at once, and the first stored wins)."""
+
     def __init__(self, cap):
         super().__init__()
         self.cap = cap
+        self._lock = threading.Lock()
 
     def get_or(self, key, build):
-        v = self.get(key)
-        if v is not None:
-            self.move_to_end(key)
-            return v
+        with self._lock:
+            v = self.get(key)
+            if v is not None:
+                self.move_to_end(key)
+                return v
         v = build()
-        self[key] = v
-        while len(self) > self.cap:
-            self.popitem(last=False)
+        with self._lock:
+            old = self.get(key)
+            if old is not None:
+                return old
+            self[key] = v
+            while len(self) > self.cap:
+                self.popitem(last=False)
         return v
 
 

@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import ctypes as C
 import itertools
+import threading
 import math
 from collections import defaultdict
 from typing import Dict, List, Sequence, Tuple
@@ -253,6 +254,7 @@ def _dense_sector_order(layout: Layout, data: np.ndarray) -> np.ndarray:
 # H_eff matvec (one or two sites)
 # --------------------------------------------------------------------------- #
 _S_CACHE: "OrderedDict" = None
+_S_LOCK = threading.Lock()
 
 
 def _combined_mpo(Ws) -> np.ndarray:
@@ -261,22 +263,24 @@ def _combined_mpo(Ws) -> np.ndarray:
     tensors recur at every bond of every sweep."""
     global _S_CACHE
     from collections import OrderedDict
-    if _S_CACHE is None:
-        _S_CACHE = OrderedDict()
     key = tuple((id(l), id(d)) for l, d in Ws)
-    hit = _S_CACHE.get(key)
-    if hit is not None and all(a is l and b is d for (a, b), (l, d) in zip(hit[0], Ws)):
-        _S_CACHE.move_to_end(key)
-        return hit[1]
+    with _S_LOCK:
+        if _S_CACHE is None:
+            _S_CACHE = OrderedDict()
+        hit = _S_CACHE.get(key)
+        if hit is not None and all(a is l and b is d for (a, b), (l, d) in zip(hit[0], Ws)):
+            _S_CACHE.move_to_end(key)
+            return hit[1]
     Wd = [_dense_sector_order(l, d) for l, d in Ws]
     if len(Ws) == 1:
         S = np.einsum("wrsi->wisr", Wd[0])
     else:
         S = np.einsum("wmsi,mrtj->wijstr", Wd[0], Wd[1])
     S = np.ascontiguousarray(S, np.float64)
-    _S_CACHE[key] = (tuple(Ws), S)
-    while len(_S_CACHE) > 256:
-        _S_CACHE.popitem(last=False)
+    with _S_LOCK:
+        _S_CACHE[key] = (tuple(Ws), S)
+        while len(_S_CACHE) > 256:
+            _S_CACHE.popitem(last=False)
     return S
 
 
