@@ -16,7 +16,6 @@ The reference has no batched solve; its oracle is a loop of independent calls, o
 """
 from __future__ import annotations
 
-import ctypes as C
 from typing import List, Sequence, Tuple
 
 import numpy as np

@@ -19,7 +19,7 @@ chain (tnkit/_dmrg.py:439-522).
 from __future__ import annotations
 
 import time
-from typing import List, Optional, Sequence
+from typing import Optional, Sequence
 
 import numpy as np
 import torch
@@ -28,7 +28,7 @@ from . import _lib
 from . import linalg as LA
 from . import ops
 from .batch import BatchedTwoSiteOperator
-from .dmrg import DMRGOptions, _resolve, setup_chain
+from .dmrg import _resolve, setup_chain
 from .tensor import BlockTensor
 
 _MAXNV = 64

@@ -19,7 +19,7 @@ from __future__ import annotations
 
 import dataclasses
 import time
-from typing import Any, Dict, List, Optional
+from typing import Any, List, Optional
 
 import numpy as np
 import torch
@@ -27,7 +27,7 @@ import torch
 from . import linalg as LA
 from . import ops
 from .lanczos import lanczos_ground_restart
-from .layout import Leg, canonical
+from .layout import canonical
 from .mpo import dense_mpo, random_block_mps, random_dense_mps
 from .tensor import BlockTensor
 
