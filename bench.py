@@ -12,6 +12,10 @@ and block. One step = one H_eff matvec (the call Lanczos makes hundreds of times
   roofline  the dominant kernel (gemm_f64_kernel, the two grouped-GEMM stages) against the
           FP64 peak measured in this run (cuBLAS DGEMM 8192^3 through torch)
   cpu_baseline  the oracle's numpy restatement of the reference's block matvec on the host
+  sweep   the whole DMRG the matvec serves -- XXZ N=64 chi=1024, 6 sweeps, seed 1 -- in FP64 and
+          in the mixed mode (tensor-core opening sweeps, one float-float polished sweep): sweep
+          seconds, phase times and |dE| against the reference's own energy (run by default at
+          N=1; --no-sweep skips it)
 
 L2 is flushed (a 256 MiB write) before every timed step, outside the step's CUDA events.
 --impl reference times the oracle port (the reference's algorithm, numpy) on the host cores.
@@ -172,7 +176,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--sweep", action="store_true",
-                    help="also run the whole chi=1024 DMRG (6 sweeps, FP64 and mixed): minutes")
+                    help="run the whole chi=1024 DMRG leg even under torchrun (it runs by default "
+                         "at N=1)")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the whole chi=1024 DMRG leg (FP64 against mixed-ff, ~2 minutes)")
     ap.add_argument("--batch", action="store_true",
                     help="also time the 64-chain batched local problems (sequential, batched, "
                          "graph-captured)")
@@ -187,10 +194,11 @@ def main():
     ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
-    ap.add_argument("--sweep-precisions", default="f64,ff,mixed,mixed-ff")
-    ap.add_argument("--mixed-schedule", default="bond", choices=["bond", "sweep"],
+    ap.add_argument("--sweep-precisions", default="f64,mixed-ff",
+                    help="comma-separated among f64, ff, mixed, mixed-ff")
+    ap.add_argument("--mixed-schedule", default="sweep", choices=["bond", "sweep"],
                     help="mixed modes: polish every bond, or tensor-core-only opening sweeps")
-    ap.add_argument("--polish-sweeps", type=int, default=2)
+    ap.add_argument("--polish-sweeps", type=int, default=1)
     ap.add_argument("--sweep-warmup-chi", type=int, default=256,
                     help="untimed 2-sweep DMRG at this chi before each timed precision (0: none)")
     args = ap.parse_args()
@@ -367,7 +375,7 @@ def main():
     # the float-float leg: theta split, two GEMMs, combination, split-K sum when present
     line["gpu_launches_per_step"] = {"fp64": per_step, "e2e": per_step, "mixed": 4,
                                      "float_float": per_step + 1}
-    if args.sweep:
+    if args.sweep or (world == 1 and not args.no_sweep):
         line["sweep"] = sweep_leg(torch, args)
     if args.batch:
         line["batch"] = batch_leg(torch, dev, flush, max(args.steps, 5))
