@@ -168,3 +168,60 @@ def energy_gradient_xxz(mps: Sequence[BlockTensor], delta: float = 1.0) -> np.nd
     dev = mps[0].data.device
     Wb, _ = to_block_mpo(xxz_bond_operator(delta), [[1, -1]] * 2, device=dev)
     return bond_expectations(mps, Wb)
+
+
+# --------------------------------------------------------------------------------------------
+# gradients with respect to the MPS tensors, by environment recomputation
+# --------------------------------------------------------------------------------------------
+
+
+def _identity_mpo(W: Sequence[BlockTensor]) -> List[BlockTensor]:
+    """The identity MPO with the physical legs of `W` (channel legs one-dimensional)."""
+    dense = [np.eye(w.legs[2].size)[None, None] for w in W]
+    if all(len(w.legs[2].charges) == 1 for w in W) and all(len(w.legs[0].charges) == 1
+                                                           for w in W):
+        from .mpo import dense_mpo
+        return dense_mpo(dense, device=W[0].data.device)
+    labels = [[c for c, d in zip(w.legs[2].charges, w.legs[2].dims) for _ in range(d)]
+              for w in W]
+    return to_block_mpo(dense, labels, device=W[0].data.device)[0]
+
+
+def _network(M, W):
+    """All left environments L[0..N] and right environments R[0..N] of <psi|W|psi>."""
+    from .dmrg import edge_envs
+    N = len(M)
+    dev = M[0].data.device
+    L: list = [None] * (N + 1)
+    R: list = [None] * (N + 1)
+    L[0], R[N] = edge_envs(M, W, dev)
+    for i in range(N):
+        L[i + 1] = ops.update_left_env(L[i], M[i], W[i])
+    for i in range(N - 1, -1, -1):
+        R[i] = ops.update_right_env(R[i + 1], M[i], W[i])
+    return L, R
+
+
+def mps_energy_gradient(mps: Sequence[BlockTensor], mpo: Sequence[BlockTensor]):
+    """E = <psi|H|psi> / <psi|psi> of a real MPS and dE/dA_i for every site tensor, by
+    environment recomputation: the derivative of the network <psi|H|psi> with respect to A_i
+    is the network with A_i taken out, i.e. 2 H_eff^(i) A_i -- the one-site effective operator
+    (L_i, W_i, R_i+1) applied to A_i by the one-site matvec kernel -- and likewise for the norm
+    with the identity MPO; dE/dA_i = (2 H_eff A_i - 2 E N_eff A_i) / <psi|psi>. No canonical
+    form is assumed. Returns (E, [dE/dA_i as BlockTensors with the layouts of the A_i])."""
+    M = list(mps)
+    W = list(mpo)
+    if any(m.data.is_complex() for m in M):
+        raise TypeError("mps_energy_gradient takes a real MPS")
+    Wn = _identity_mpo(W)
+    Lh, Rh = _network(M, W)
+    Ln, Rn = _network(M, Wn)
+    f = float(Lh[len(M)].data.sum())
+    nrm = float(Ln[len(M)].data.sum())
+    E = f / nrm
+    grads = []
+    for i, A in enumerate(M):
+        h = ops.apply_one_site(A, Lh[i], W[i], Rh[i + 1]).data
+        n = ops.apply_one_site(A, Ln[i], Wn[i], Rn[i + 1]).data
+        grads.append(BlockTensor(A.layout, (2.0 / nrm) * (h - E * n)))
+    return E, grads
