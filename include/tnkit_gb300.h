@@ -392,6 +392,25 @@ typedef struct {
     int64_t sec_begin[7];            /* axis a's sectors at [sec_begin[a], sec_begin[a + 1]) */
 } tnk_apply_plan_in;
 
+/* Environment-update plan: side 0 builds L'[d,r,e] = sum L[p,w,q] conj(A[p,s,d]) W[w,r,s,y]
+ * A[q,y,e] (env = L, site = A), side 1 builds R'[u,w,v] = sum R[x,r,y] conj(B[u,s,x])
+ * W[w,r,s,p] B[v,p,y] (env = R, site = B); W is the dense MPO tensor over its sector-ordered
+ * indices with the sector starts / extents of its four legs. Tables 0 .. 5 as for the H_eff
+ * plan (stage-1 GEMMs: conj(site) x env; stage 2: MPO coefficients; stage 3: x site). */
+typedef struct {
+    int32_t side, pad;
+    tnk_layout_desc env;
+    tnk_layout_desc site;
+    tnk_layout_desc out;
+    const double* W;
+    int64_t w_dims[4];
+    const int64_t* sec_start;
+    const int64_t* sec_dim;
+    int64_t sec_begin[5];
+} tnk_env_plan_in;
+
+int tnk_env_plan_build(const tnk_env_plan_in* in, void** handle);
+
 /* Tables of a built plan, read back with tnk_planb_table(handle, id, &data, &count):
  * 0 stage-1 tasks, 1 stage-1 segments, 2 stage-2 tasks, 3 stage-2 terms, 4 stage-3 tasks,
  * 5 stage-3 segments (tnk_apply_plan_build); 10 stage-1 tasks, 11 stage-1 tensor-core segments,

@@ -148,3 +148,60 @@ def test_native_split_k_random_tables(seed):
     ta, sa = np.array(tasks, GEMM_TASK), np.array(segs, GEMM_SEG)
     g3 = (ta, sa, P._tiles_cost(ta, sa, P.TILE_M))
     _same_split(g3, 5, slots=int(rng.integers(1, 400)), max_chunks=int(rng.integers(1, 9)))
+
+
+def _both_env(L, A, WA, R, B, WB):
+    _same_plan(P.plan_left_env(L, A, WA), P._plan_left_env_py(L, A, WA))
+    _same_plan(P.plan_right_env(R, B, WB), P._plan_right_env_py(R, B, WB))
+
+
+@pytest.mark.parametrize("tag", ["xxz12_b0", "xxz12_b5"])
+def test_native_env_planner_golden_problems(golden, tag):
+    meta, A = golden
+    g = lambda k: (_lay(meta[f"{tag}_{k}"]), A[f"{tag}_{k}"])
+    (Ll, _), (Al, _), (W1l, W1d), (Rl, _), (Bl, _), (W2l, W2d) = (
+        g(k) for k in ("L", "A", "W1", "R", "B", "W2"))
+    _both_env(Ll, Al, (W1l, W1d), Rl, Bl, (W2l, W2d))
+
+
+def test_native_env_planner_chi1024_mid_bond():
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=3, device="cpu")
+    bond, phys = th.layout.legs[0], th.layout.legs[1]
+    A = layout_of((bond, phys, bond.flip()), 0)
+    _both_env(L.layout, A, (W1.layout, _host_of(W1)), R.layout, A, (W2.layout, _host_of(W2)))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_native_env_planner_ragged_u1_layouts(seed):
+    rng = np.random.default_rng(200 + seed)
+    Wb, _ = to_block_mpo(workloads.xxz_mpo(6), [[1, -1]] * 6, device="cpu")
+    W1 = Wb[2]
+    left = _random_bond(rng, list(range(-6, 7, 2)))
+    right = _random_bond(rng, list(range(-5, 6, 2)))
+    phys = W1.legs[2]
+    A = layout_of((left, phys, right.flip()), 0)
+    if A.nblocks == 0:
+        pytest.skip("no allowed block for this draw")
+    L = layout_of((left, W1.legs[0].flip(), left.flip()), 0)
+    R = layout_of((right.flip(), W1.legs[1].flip(), right), 0)
+    Ws = (W1.layout, _host_of(W1))
+    _both_env(L, A, Ws, R, A, Ws)
+
+
+def test_native_env_planner_hubbard():
+    rng = np.random.default_rng(6)
+    N = 6
+    Wb, _ = to_block_mpo(workloads.hubbard_mpo(N, 1.0, 4.0),
+                         [workloads.HUBBARD_SITE_CHARGES] * N, device="cpu")
+    W1 = Wb[2]
+    phys = W1.legs[2]
+    ch = [(a, b) for a in range(0, 4) for b in range(0, 4)]
+    left = Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))), 1)
+    ch2 = [(a, b) for a in range(0, 5) for b in range(0, 5)]
+    right = Leg(tuple(ch2), tuple(int(x) for x in rng.integers(1, 9, len(ch2))), 1)
+    A = layout_of((left, phys, right.flip()), (0, 0))
+    L = layout_of((left, W1.legs[0].flip(), left.flip()), (0, 0))
+    R = layout_of((right.flip(), W1.legs[1].flip(), right), (0, 0))
+    assert A.nblocks > 0
+    Ws = (W1.layout, _host_of(W1))
+    _both_env(L, A, Ws, R, A, Ws)

@@ -60,6 +60,13 @@ class ApplyPlanIn(C.Structure):
                 ("sec_begin", C.c_int64 * 7)]
 
 
+class EnvPlanIn(C.Structure):
+    _fields_ = [("side", C.c_int32), ("pad", C.c_int32), ("env", LayoutDesc),
+                ("site", LayoutDesc), ("out", LayoutDesc), ("W", C.c_void_p),
+                ("w_dims", C.c_int64 * 4), ("sec_start", C.c_void_p), ("sec_dim", C.c_void_p),
+                ("sec_begin", C.c_int64 * 5)]
+
+
 class Plan3(C.Structure):
     _fields_ = [("t1", C.c_void_p), ("s1", C.c_void_p), ("tiles1", C.c_void_p),
                 ("n_tiles1", C.c_int64),
@@ -130,6 +137,7 @@ _SIGS = {
     "tnk_zaxpby_f64": ([_P, _P, _I64, _P, _D, _P, _D, _P], C.c_int),
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
+    "tnk_env_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_split_k": ([_P, _I64, _P, _I64, _I32, _I32, _I32, _I32, _P], C.c_int),
     "tnk_planb_table": ([_P, _I32, _P, _P], C.c_int),
     "tnk_planb_scalars": ([_P, _P], C.c_int),

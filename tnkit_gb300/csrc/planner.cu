@@ -17,6 +17,7 @@
 #include <climits>
 #include <cmath>
 #include <map>
+#include <stdexcept>
 #include <unordered_map>
 #include <utility>
 #include <vector>
@@ -478,6 +479,223 @@ int split_build(const tnk_gemm_task* t, int64_t nt, const tnk_gemm_seg* s, int64
     return TNK_OK;
 }
 
+// Environment updates (tnkit/_dmrg.py:216-231) as three stages:
+//   left   T[(s,d),(w,q)] = conj(A)[p,(s,d)]^T L[p,(w,q)]          stage 1, per (A, L) block pair
+//          U[d, (r, q, y)] = sum_{w,s} W[w,r,s,y] T[(s,d),(w,q)]     stage 2, MPO coefficients
+//          L'[(d,r), e] = sum_{q,y} U[(d,r),(q,y)] A[(q,y), e]        stage 3
+//   right  T[(u,s),(r,y)] = conj(B)[(u,s),x] R[x,(r,y)]
+//          V[u, (w, p, y)] = sum_{r,s} W[w,r,s,p] T[(u,s),(r,y)]
+//          R'[(u,w), v] = sum_{p,y} V[(u,w),(p,y)] B[v,(p,y)]^T
+// The iteration orders and offsets follow plan.py's plan_left_env / plan_right_env exactly.
+int env_build(const tnk_env_plan_in* in, PlanBuild* pb) {
+    const bool left = in->side == 0;
+    if ((in->side != 0 && in->side != 1) || in->env.nlegs != 3 || in->site.nlegs != 3 ||
+        in->out.nlegs != 3 || !in->W || !in->sec_start || !in->sec_dim) {
+        tnk::set_error("plan_env: bad arguments");
+        return TNK_ERR_ARG;
+    }
+    const Lay E{&in->env}, S{&in->site}, O{&in->out};
+    int64_t st[4];
+    st[3] = 1;
+    for (int a = 2; a >= 0; --a) st[a] = st[a + 1] * in->w_dims[a + 1];
+    auto nsec = [&](int a) { return in->sec_begin[a + 1] - in->sec_begin[a]; };
+    auto sstart = [&](int a, int64_t s) { return in->sec_start[in->sec_begin[a] + s]; };
+    auto sdim = [&](int a, int64_t s) { return in->sec_dim[in->sec_begin[a] + s]; };
+    // W entry at the sectors (w, r, s, t) and offsets (ww, rr, ss, tt) inside them
+    auto wval = [&](const int64_t* sec, int64_t ww, int64_t rr, int64_t ss, int64_t tt) {
+        return in->W[(sstart(0, sec[0]) + ww) * st[0] + (sstart(1, sec[1]) + rr) * st[1] +
+                     (sstart(2, sec[2]) + ss) * st[2] + (sstart(3, sec[3]) + tt) * st[3]];
+    };
+    auto any_nonzero = [&](const int64_t* sec) {
+        for (int a = 0; a < 4; ++a)
+            if (sec[a] < 0 || sec[a] >= nsec(a)) throw std::out_of_range("MPO sector");
+        for (int64_t a = 0; a < sdim(0, sec[0]); ++a)
+            for (int64_t b = 0; b < sdim(1, sec[1]); ++b)
+                for (int64_t c = 0; c < sdim(2, sec[2]); ++c)
+                    for (int64_t d = 0; d < sdim(3, sec[3]); ++d)
+                        if (wval(sec, a, b, c, d) != 0.0) return true;
+        return false;
+    };
+    using TK = std::array<int64_t, 4>;
+    std::unordered_map<int64_t, std::vector<int64_t>> env_by0, site_by;
+    for (int64_t k = 0; k < E.nb(); ++k) env_by0[E.key(k, 0)].push_back(k);
+    for (int64_t k = 0; k < S.nb(); ++k) site_by[S.key(k, left ? 2 : 0)].push_back(k);
+    std::map<TK, std::pair<int64_t, int64_t>> tcand;
+    std::map<std::pair<int64_t, int64_t>, std::vector<TK>> t_by;
+    for (int64_t ks = 0; ks < S.nb(); ++ks) {
+        const int64_t s0 = S.key(ks, 0), s1 = S.key(ks, 1), s2 = S.key(ks, 2);
+        auto it = env_by0.find(left ? s0 : s2);
+        if (it == env_by0.end()) continue;
+        for (int64_t ke : it->second) {
+            const int64_t e1 = E.key(ke, 1), e2 = E.key(ke, 2);
+            // left: (s, d, w, q); right: (u, s, r, y)
+            const TK tk = left ? TK{s1, s2, e1, e2} : TK{s0, s1, e1, e2};
+            tcand[tk] = {ks, ke};
+            t_by[left ? std::make_pair(s2, e2) : std::make_pair(s0, e2)].push_back(tk);
+        }
+    }
+    struct Contrib {
+        TK tk;
+        int64_t sec[4];
+    };
+    struct Def {
+        int64_t a, b, c, d, ks2;     // left: D, Rd, Q, Yd; right: U, Wd, Pd, Yd
+        std::vector<Contrib> contrib;
+    };
+    std::vector<Def> defs;
+    std::vector<std::pair<int64_t, std::vector<int64_t>>> tasks3;
+    for (int64_t ko = 0; ko < O.nb(); ++ko) {
+        const int64_t o0 = O.key(ko, 0), o1 = O.key(ko, 1), o2 = O.key(ko, 2);
+        std::vector<int64_t> segs3;
+        auto sit = site_by.find(left ? o2 : o2);
+        if (sit != site_by.end()) {
+            for (int64_t ks2 : sit->second) {
+                Def df{};
+                df.ks2 = ks2;
+                const int64_t k0 = S.key(ks2, 0), k1 = S.key(ks2, 1);
+                auto tit = t_by.find({o0, left ? k0 : S.key(ks2, 2)});
+                if (tit != t_by.end()) {
+                    for (const TK& tk : tit->second) {
+                        Contrib cb{};
+                        cb.tk = tk;
+                        if (left) {   // W[w, r, s, y]: w = tk[2], r = o1, s = tk[0], y = k1
+                            cb.sec[0] = tk[2]; cb.sec[1] = o1; cb.sec[2] = tk[0]; cb.sec[3] = k1;
+                        } else {      // W[w, r, s, p]: w = o1, r = tk[2], s = tk[1], p = k1
+                            cb.sec[0] = o1; cb.sec[1] = tk[2]; cb.sec[2] = tk[1]; cb.sec[3] = k1;
+                        }
+                        if (any_nonzero(cb.sec)) df.contrib.push_back(cb);
+                    }
+                }
+                if (df.contrib.empty()) continue;
+                if (left) {
+                    df.a = O.shape(ko, 0); df.b = O.shape(ko, 1);
+                    df.c = S.shape(ks2, 0); df.d = S.shape(ks2, 1);
+                } else {
+                    df.a = O.shape(ko, 0); df.b = O.shape(ko, 1);
+                    df.c = S.shape(ks2, 1); df.d = S.shape(ks2, 2);
+                }
+                defs.push_back(std::move(df));
+                segs3.push_back((int64_t)defs.size() - 1);
+            }
+        }
+        tasks3.emplace_back(ko, std::move(segs3));
+    }
+    // stage 1: the T blocks some U / V block uses, in order of first use
+    std::map<TK, int64_t> t_off;
+    for (const Def& df : defs)
+        for (const Contrib& cb : df.contrib) {
+            if (t_off.count(cb.tk)) continue;
+            const auto [ks, ke] = tcand.at(cb.tk);
+            const int64_t b = (int64_t)pb->g1s.size();
+            t_off[cb.tk] = pb->ws1;
+            int64_t m, n, k;
+            if (left) {   // A (P, S, D) x L (P, Wd, Q)
+                const int64_t P = S.shape(ks, 0), Sd = S.shape(ks, 1), D = S.shape(ks, 2);
+                const int64_t Wd = E.shape(ke, 1), Q = E.shape(ke, 2);
+                m = Sd * D; n = Wd * Q; k = P;
+                pb->g1s.push_back(make_seg(S.off(ks), 1, Sd * D, SLOT_X0, E.off(ke), Wd * Q, 1,
+                                           SLOT_X1, P));
+            } else {      // B (U, S, X) x R (X, Rd, Yd)
+                const int64_t U = S.shape(ks, 0), Sd = S.shape(ks, 1), X = S.shape(ks, 2);
+                const int64_t Rd = E.shape(ke, 1), Yd = E.shape(ke, 2);
+                m = U * Sd; n = Rd * Yd; k = X;
+                pb->g1s.push_back(make_seg(S.off(ks), X, 1, SLOT_X0, E.off(ke), Rd * Yd, 1,
+                                           SLOT_X1, X));
+            }
+            pb->g1s.back().conj = 1;
+            pb->g1t.push_back(make_task(pb->ws1, n, m, n, b, b + 1, 0));
+            pb->macs1 += m * n * k;
+            pb->ws1 += m * n;
+        }
+    // stage 2
+    std::vector<int64_t> d_off;
+    for (const Def& df : defs) {
+        const int64_t base = pb->ws1 + pb->ws2;
+        d_off.push_back(base);
+        pb->ws2 += df.a * df.b * df.c * df.d;
+        if (left) {   // rows D, cols Q, for each (rr, yy)
+            const int64_t D = df.a, Rd = df.b, Q = df.c, Yd = df.d;
+            for (int64_t rr = 0; rr < Rd; ++rr)
+                for (int64_t yy = 0; yy < Yd; ++yy) {
+                    const int64_t tb = (int64_t)pb->c2c.size();
+                    for (const Contrib& cb : df.contrib) {
+                        const auto [ks, ke] = tcand.at(cb.tk);
+                        const int64_t Sd = S.shape(ks, 1), Dd = S.shape(ks, 2);
+                        const int64_t Wd = E.shape(ke, 1), Qd = E.shape(ke, 2);
+                        for (int64_t ww = 0; ww < Wd; ++ww)
+                            for (int64_t ss = 0; ss < Sd; ++ss) {
+                                const double c = wval(cb.sec, ww, rr, ss, yy);
+                                if (c == 0.0) continue;
+                                tnk_comb_term t{};
+                                t.src_off = t_off.at(cb.tk) + ss * Dd * Wd * Qd + ww * Qd;
+                                t.src_ld = i32(Wd * Qd);
+                                t.src_cs = 1;
+                                t.coef = c;
+                                pb->c2c.push_back(t);
+                            }
+                    }
+                    tnk_comb_task c{};
+                    c.dst_off = base + rr * Q * Yd + yy;
+                    c.rows = i32(D);
+                    c.cols = i32(Q);
+                    c.dst_ld = i32(Rd * Q * Yd);
+                    c.dst_cs = i32(Yd);
+                    c.term_begin = i32(tb);
+                    c.term_end = i32((int64_t)pb->c2c.size());
+                    pb->c2t.push_back(c);
+                }
+        } else {      // rows U, cols Yd, for each (ww, pp)
+            const int64_t U = df.a, Wd = df.b, Pd = df.c, Yd = df.d;
+            for (int64_t ww = 0; ww < Wd; ++ww)
+                for (int64_t pp = 0; pp < Pd; ++pp) {
+                    const int64_t tb = (int64_t)pb->c2c.size();
+                    for (const Contrib& cb : df.contrib) {
+                        const auto [ks, ke] = tcand.at(cb.tk);
+                        const int64_t Sd = S.shape(ks, 1), Rd = E.shape(ke, 1);
+                        for (int64_t ss = 0; ss < Sd; ++ss)
+                            for (int64_t rr = 0; rr < Rd; ++rr) {
+                                const double c = wval(cb.sec, ww, rr, ss, pp);
+                                if (c == 0.0) continue;
+                                tnk_comb_term t{};
+                                t.src_off = t_off.at(cb.tk) + (ss * Rd + rr) * Yd;
+                                t.src_ld = i32(Sd * Rd * Yd);
+                                t.src_cs = 1;
+                                t.coef = c;
+                                pb->c2c.push_back(t);
+                            }
+                    }
+                    tnk_comb_task c{};
+                    c.dst_off = base + (ww * Pd + pp) * Yd;
+                    c.rows = i32(U);
+                    c.cols = i32(Yd);
+                    c.dst_ld = i32(Wd * Pd * Yd);
+                    c.dst_cs = 1;
+                    c.term_begin = i32(tb);
+                    c.term_end = i32((int64_t)pb->c2c.size());
+                    pb->c2t.push_back(c);
+                }
+        }
+    }
+    // stage 3
+    for (const auto& [ko, segs3] : tasks3) {
+        const int64_t b = (int64_t)pb->g3s.size();
+        const int64_t o0 = O.shape(ko, 0), o1 = O.shape(ko, 1), o2 = O.shape(ko, 2);
+        for (int64_t di : segs3) {
+            const Def& df = defs[di];
+            const int64_t K = df.c * df.d;
+            if (left)
+                pb->g3s.push_back(make_seg(d_off[di], K, 1, SLOT_WS, S.off(df.ks2), o2, 1,
+                                           SLOT_X2, K));
+            else
+                pb->g3s.push_back(make_seg(d_off[di], K, 1, SLOT_WS, S.off(df.ks2), 1, K,
+                                           SLOT_X2, K));
+            pb->macs3 += o0 * o1 * o2 * K;
+        }
+        pb->g3t.push_back(make_task(O.off(ko), o2, o0 * o1, o2, b, (int64_t)pb->g3s.size(), 0));
+    }
+    return TNK_OK;
+}
+
 template <typename T>
 void table(const std::vector<T>& v, const void** data, int64_t* count) {
     *data = v.empty() ? nullptr : (const void*)v.data();
@@ -501,6 +719,31 @@ extern "C" int tnk_apply_plan_build(const tnk_apply_plan_in* in, void** handle) 
         rc = TNK_ERR_SIZE;
     } catch (const std::exception& e) {
         tnk::set_error("plan_apply: %s", e.what());
+        rc = TNK_ERR_ARG;
+    }
+    if (rc) {
+        delete pb;
+        return rc;
+    }
+    *handle = pb;
+    return TNK_OK;
+}
+
+extern "C" int tnk_env_plan_build(const tnk_env_plan_in* in, void** handle) {
+    if (!in || !handle) {
+        tnk::set_error("tnk_env_plan_build: null argument");
+        return TNK_ERR_ARG;
+    }
+    *handle = nullptr;
+    PlanBuild* pb = new PlanBuild();
+    int rc;
+    try {
+        rc = env_build(in, pb);
+    } catch (const Overflow&) {
+        tnk::set_error("plan_env: a table entry exceeds 32 bits");
+        rc = TNK_ERR_SIZE;
+    } catch (const std::exception& e) {
+        tnk::set_error("plan_env: %s", e.what());
         rc = TNK_ERR_ARG;
     }
     if (rc) {

@@ -513,9 +513,7 @@ def _plan_apply_py(theta: Layout, L: Layout, Ws: Sequence[Tuple[Layout, np.ndarr
 # --------------------------------------------------------------------------- #
 # environment updates
 # --------------------------------------------------------------------------- #
-def plan_left_env(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
-    """Plan of L'[d,r,e] = sum L[p,w,q] conj(A[p,s,d]) W[w,r,s,y] A[q,y,e]
-    (tnkit/_dmrg.py:216-222). Slots: x0 = A (conjugated), x1 = L, x2 = A."""
+def _left_env_setup(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]):
     WL, wdata = W
     # conj(A) legs carry flipped signs: its left leg meets L's bra leg (same signs as A's)
     _check_contract(A.legs[0].flip(), L.legs[0], "conj(A).left/L.bra")
@@ -524,9 +522,73 @@ def plan_left_env(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPla
     _check_contract(A.legs[1].flip(), WL.legs[2], "conj(A).phys/W.out")
     _check_contract(WL.legs[3], A.legs[1], "W.in/A.phys")
     Wd = _dense_sector_order(WL, wdata)          # [w, r, s, y]
+    return Wd, canonical((A.legs[2].flip(), WL.legs[1], A.legs[2]), L.charge)
+
+
+def _right_env_setup(R: Layout, B: Layout, W: Tuple[Layout, np.ndarray]):
+    WL, wdata = W
+    _check_contract(B.legs[2].flip(), R.legs[0], "conj(B).right/R.bra")
+    _check_contract(B.legs[2], R.legs[2], "B.right/R.ket")
+    _check_contract(WL.legs[1], R.legs[1], "W.right/R.mpo")
+    _check_contract(B.legs[1].flip(), WL.legs[2], "conj(B).phys/W.out")
+    _check_contract(WL.legs[3], B.legs[1], "W.in/B.phys")
+    Wd = _dense_sector_order(WL, wdata)          # [w, r, s, p]
+    return Wd, canonical((B.legs[0].flip(), WL.legs[0], B.legs[0]), R.charge)
+
+
+def _env_native(side: int, env: Layout, site: Layout, W: Tuple[Layout, np.ndarray],
+                kind: str) -> HostPlan3:
+    """plan_left_env / plan_right_env by tnk_env_plan_build."""
+    Wd, out = (_left_env_setup if side == 0 else _right_env_setup)(env, site, W)
+    Wd = np.ascontiguousarray(Wd, np.float64)
+    legs = W[0].legs
+    keep: list = []
+    starts = np.ascontiguousarray(np.concatenate([l.starts() for l in legs]), np.int64)
+    dims = np.ascontiguousarray(np.concatenate([np.asarray(l.dims, np.int64) for l in legs]))
+    begin = np.concatenate([[0], np.cumsum([len(l.dims) for l in legs])]).astype(np.int64)
+    a = _lib.EnvPlanIn()
+    a.side = side
+    a.env, a.site, a.out = _desc(env, keep), _desc(site, keep), _desc(out, keep)
+    a.W = Wd.ctypes.data
+    for i, d in enumerate(Wd.shape):
+        a.w_dims[i] = int(d)
+    a.sec_start, a.sec_dim = starts.ctypes.data, dims.ctypes.data
+    for i, b in enumerate(begin):
+        a.sec_begin[i] = int(b)
+    lib = _lib.lib()
+    h = C.c_void_p()
+    _lib.check(lib.tnk_env_plan_build(C.byref(a), C.byref(h)), "tnk_env_plan_build")
+    try:
+        (t1, s1, t2, c2, t3, s3), sc = _planb_read(h, [(0, GEMM_TASK), (1, GEMM_SEG),
+                                                       (2, COMB_TASK), (3, COMB_TERM),
+                                                       (4, GEMM_TASK), (5, GEMM_SEG)])
+    finally:
+        lib.tnk_planb_free(h)
+    ws1, ws2, macs1, macs3, _ = sc
+    return HostPlan3(_GemmArrays(t1, s1, macs1), _CombArrays(t2, c2), _GemmArrays(t3, s3, macs3),
+                     ws1, ws2, out, kind=kind)
+
+
+def plan_left_env(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """Plan of L'[d,r,e] = sum L[p,w,q] conj(A[p,s,d]) W[w,r,s,y] A[q,y,e]
+    (tnkit/_dmrg.py:216-222). Slots: x0 = A (conjugated), x1 = L, x2 = A. Built by the native
+    planner; _plan_left_env_py states the same construction."""
+    return _env_native(0, L, A, W, "left_env")
+
+
+def plan_right_env(R: Layout, B: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """Plan of R'[u,w,v] = sum R[x,r,y] conj(B[u,s,x]) W[w,r,s,p] B[v,p,y]
+    (tnkit/_dmrg.py:225-231). Slots: x0 = B (conjugated), x1 = R, x2 = B. Built by the native
+    planner; _plan_right_env_py states the same construction."""
+    return _env_native(1, R, B, W, "right_env")
+
+
+def _plan_left_env_py(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """plan_left_env in Python (the statement the native planner is tested against)."""
+    WL, wdata = W
+    Wd, out = _left_env_setup(L, A, W)
     wleg, rleg, sleg, yleg = WL.legs
     wst, rst, sst, yst = (l.starts() for l in WL.legs)
-    out = canonical((A.legs[2].flip(), rleg, A.legs[2]), L.charge)
 
     # stage 1: T[(s,d),(w,q)] per (A block (p,s,d), L block (p,w,q))
     L_by_p: Dict[int, List[int]] = defaultdict(list)
@@ -616,19 +678,12 @@ def plan_left_env(L: Layout, A: Layout, W: Tuple[Layout, np.ndarray]) -> HostPla
     return HostPlan3(g1, c2, g3, ws1, ws2, out, kind="left_env")
 
 
-def plan_right_env(R: Layout, B: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
-    """Plan of R'[u,w,v] = sum R[x,r,y] conj(B[u,s,x]) W[w,r,s,p] B[v,p,y]
-    (tnkit/_dmrg.py:225-231). Slots: x0 = B (conjugated), x1 = R, x2 = B."""
+def _plan_right_env_py(R: Layout, B: Layout, W: Tuple[Layout, np.ndarray]) -> HostPlan3:
+    """plan_right_env in Python (the statement the native planner is tested against)."""
     WL, wdata = W
-    _check_contract(B.legs[2].flip(), R.legs[0], "conj(B).right/R.bra")
-    _check_contract(B.legs[2], R.legs[2], "B.right/R.ket")
-    _check_contract(WL.legs[1], R.legs[1], "W.right/R.mpo")
-    _check_contract(B.legs[1].flip(), WL.legs[2], "conj(B).phys/W.out")
-    _check_contract(WL.legs[3], B.legs[1], "W.in/B.phys")
-    Wd = _dense_sector_order(WL, wdata)          # [w, r, s, p]
+    Wd, out = _right_env_setup(R, B, W)
     wleg, rleg, sleg, pleg = WL.legs
     wst, rst, sst, pst = (l.starts() for l in WL.legs)
-    out = canonical((B.legs[0].flip(), wleg, B.legs[0]), R.charge)
 
     R_by_x: Dict[int, List[int]] = defaultdict(list)
     for k in range(R.nblocks):
