@@ -410,6 +410,11 @@ typedef struct {
 } tnk_env_plan_in;
 
 int tnk_env_plan_build(const tnk_env_plan_in* in, void** handle);
+/* Block tensordot plan: out = a . b contracting the last nc legs of a with the first nc legs
+ * of b (out's layout given: the free legs of a, then those of b); tables 0 / 1 hold one GEMM task
+ * per output block and one K segment per matching block pair (slots x0 = a, x1 = b). */
+int tnk_tensordot_plan_build(const tnk_layout_desc* a, const tnk_layout_desc* b,
+                             const tnk_layout_desc* out, int32_t nc, void** handle);
 
 /* Tables of a built plan, read back with tnk_planb_table(handle, id, &data, &count):
  * 0 stage-1 tasks, 1 stage-1 segments, 2 stage-2 tasks, 3 stage-2 terms, 4 stage-3 tasks,

@@ -205,3 +205,42 @@ def test_native_env_planner_hubbard():
     assert A.nblocks > 0
     Ws = (W1.layout, _host_of(W1))
     _both_env(L, A, Ws, R, A, Ws)
+
+
+def _same_gemm(a, b):
+    for x, y in zip(a.g, b.g):
+        assert x.dtype == y.dtype and np.array_equal(x, y)
+    assert a.macs == b.macs and a.out_layout.legs == b.out_layout.legs
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_native_tensordot_planner(seed):
+    """MPS-site products (one contracted leg) and theta-environment contractions (two legs) on
+    ragged U(1) layouts, and a U(1)xU(1) Hubbard pair: identical tables to the Python planner."""
+    rng = np.random.default_rng(300 + seed)
+    Wb, _ = to_block_mpo(workloads.xxz_mpo(6), [[1, -1]] * 6, device="cpu")
+    phys = Wb[2].legs[2]
+    a = _random_bond(rng, list(range(-6, 7, 2)))
+    b = _random_bond(rng, list(range(-5, 6, 2)))
+    c = _random_bond(rng, list(range(-6, 7, 2)))
+    A = layout_of((a, phys, b.flip()), 0)
+    B2 = layout_of((b, phys, c.flip()), 0)
+    if A.nblocks and B2.nblocks:
+        _same_gemm(P.plan_tensordot(A, B2, 1), P._plan_tensordot_py(A, B2, 1))
+        th = P.plan_tensordot(A, B2, 1).out_layout
+        X = layout_of((phys.flip(), c, b.flip()), 0)       # contracts theta's last two legs
+        if th.nblocks and X.nblocks:
+            _same_gemm(P.plan_tensordot(th, X, 2), P._plan_tensordot_py(th, X, 2))
+
+
+def test_native_tensordot_planner_hubbard():
+    rng = np.random.default_rng(9)
+    Wb, _ = to_block_mpo(workloads.hubbard_mpo(6, 1.0, 4.0),
+                         [workloads.HUBBARD_SITE_CHARGES] * 6, device="cpu")
+    phys = Wb[2].legs[2]
+    ch = [(a, b) for a in range(0, 5) for b in range(0, 5)]
+    left = Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))), 1)
+    mid = Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))), 1)
+    A1 = layout_of((left, phys, mid.flip()), (0, 0))
+    A2 = layout_of((mid, phys, left.flip()), (0, 0))
+    _same_gemm(P.plan_tensordot(A1, A2, 1), P._plan_tensordot_py(A1, A2, 1))

@@ -138,6 +138,7 @@ _SIGS = {
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
     "tnk_env_plan_build": ([_P, _P], C.c_int),
+    "tnk_tensordot_plan_build": ([_P, _P, _P, _I32, _P], C.c_int),
     "tnk_plan_split_k": ([_P, _I64, _P, _I64, _I32, _I32, _I32, _I32, _P], C.c_int),
     "tnk_planb_table": ([_P, _I32, _P, _P], C.c_int),
     "tnk_planb_scalars": ([_P, _P], C.c_int),

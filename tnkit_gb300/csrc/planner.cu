@@ -696,6 +696,52 @@ int env_build(const tnk_env_plan_in* in, PlanBuild* pb) {
     return TNK_OK;
 }
 
+// Block tensordot (tnkit/blocks.py:1156-1192): out = a . b over the last nc legs of a and the
+// first nc legs of b; one GEMM task per output block with one K segment per matching (a, b)
+// block pair, in plan.py's plan_tensordot order.
+int tensordot_build(const tnk_layout_desc* ad, const tnk_layout_desc* bd,
+                    const tnk_layout_desc* od, int nc, PlanBuild* pb) {
+    const Lay a{ad}, b{bd}, o{od};
+    const int na = ad->nlegs, nb = bd->nlegs;
+    if (nc < 0 || nc > na || nc > nb || od->nlegs != na + nb - 2 * nc) {
+        tnk::set_error("plan_tensordot: bad leg counts");
+        return TNK_ERR_ARG;
+    }
+    using Key = std::vector<int64_t>;
+    auto key = [](const Lay& t, int64_t k, int l0, int l1) {
+        Key v;
+        for (int l = l0; l < l1; ++l) v.push_back(t.key(k, l));
+        return v;
+    };
+    std::map<Key, std::vector<int64_t>> b_by_k, a_by_free;
+    for (int64_t k = 0; k < b.nb(); ++k) b_by_k[key(b, k, 0, nc)].push_back(k);
+    for (int64_t k = 0; k < a.nb(); ++k) a_by_free[key(a, k, 0, na - nc)].push_back(k);
+    for (int64_t ko = 0; ko < o.nb(); ++ko) {
+        const Key fa = key(o, ko, 0, na - nc), fb = key(o, ko, na - nc, od->nlegs);
+        int64_t M = 1, N = 1;
+        for (int l = 0; l < na - nc; ++l) M *= o.shape(ko, l);
+        for (int l = na - nc; l < od->nlegs; ++l) N *= o.shape(ko, l);
+        const int64_t s0 = (int64_t)pb->g1s.size();
+        auto ait = a_by_free.find(fa);
+        if (ait != a_by_free.end()) {
+            for (int64_t ka : ait->second) {
+                auto bit = b_by_k.find(key(a, ka, na - nc, na));
+                if (bit == b_by_k.end()) continue;
+                for (int64_t kb : bit->second) {
+                    if (key(b, kb, nc, nb) != fb) continue;
+                    int64_t K = 1;
+                    for (int l = na - nc; l < na; ++l) K *= a.shape(ka, l);
+                    pb->g1s.push_back(make_seg(a.off(ka), K, 1, SLOT_X0, b.off(kb), N, 1,
+                                               SLOT_X1, K));
+                    pb->macs1 += M * N * K;
+                }
+            }
+        }
+        pb->g1t.push_back(make_task(o.off(ko), N, M, N, s0, (int64_t)pb->g1s.size(), 0));
+    }
+    return TNK_OK;
+}
+
 template <typename T>
 void table(const std::vector<T>& v, const void** data, int64_t* count) {
     *data = v.empty() ? nullptr : (const void*)v.data();
@@ -745,6 +791,30 @@ extern "C" int tnk_env_plan_build(const tnk_env_plan_in* in, void** handle) {
     } catch (const std::exception& e) {
         tnk::set_error("plan_env: %s", e.what());
         rc = TNK_ERR_ARG;
+    }
+    if (rc) {
+        delete pb;
+        return rc;
+    }
+    *handle = pb;
+    return TNK_OK;
+}
+
+extern "C" int tnk_tensordot_plan_build(const tnk_layout_desc* a, const tnk_layout_desc* b,
+                                        const tnk_layout_desc* out, int32_t nc,
+                                        void** handle) {
+    if (!a || !b || !out || !handle) {
+        tnk::set_error("tnk_tensordot_plan_build: null argument");
+        return TNK_ERR_ARG;
+    }
+    *handle = nullptr;
+    PlanBuild* pb = new PlanBuild();
+    int rc;
+    try {
+        rc = tensordot_build(a, b, out, nc, pb);
+    } catch (const Overflow&) {
+        tnk::set_error("plan_tensordot: a table entry exceeds 32 bits");
+        rc = TNK_ERR_SIZE;
     }
     if (rc) {
         delete pb;

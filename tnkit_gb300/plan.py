@@ -784,7 +784,30 @@ class HostGemmPlan:
 def plan_tensordot(a: Layout, b: Layout, nc: int) -> HostGemmPlan:
     """out = a . b contracting the last `nc` legs of a with the first `nc` legs of b; output legs
     = free legs of a then free legs of b (tnkit/blocks.py:1156-1192 for this leg order).
-    Slots: x0 = a, x1 = b."""
+    Slots: x0 = a, x1 = b. Built by tnk_tensordot_plan_build; _plan_tensordot_py states the same
+    construction."""
+    na, nb = len(a.legs), len(b.legs)
+    for i in range(nc):
+        _check_contract(a.legs[na - nc + i], b.legs[i], "tensordot")
+    out = canonical(a.legs[:na - nc] + b.legs[nc:], _add_charge(a.charge, b.charge))
+    keep: list = []
+    da, db, do = _desc(a, keep), _desc(b, keep), _desc(out, keep)
+    lib = _lib.lib()
+    h = C.c_void_p()
+    _lib.check(lib.tnk_tensordot_plan_build(C.byref(da), C.byref(db), C.byref(do), int(nc),
+                                            C.byref(h)), "tnk_tensordot_plan_build")
+    try:
+        (t, sg), sc = _planb_read(h, [(0, GEMM_TASK), (1, GEMM_SEG)])
+    finally:
+        lib.tnk_planb_free(h)
+    hp = HostGemmPlan.__new__(HostGemmPlan)
+    hp.g = (t, sg, _tiles_cost(t, sg, TILE_M))
+    hp.macs, hp.out_layout = sc[2], out
+    return hp
+
+
+def _plan_tensordot_py(a: Layout, b: Layout, nc: int) -> HostGemmPlan:
+    """plan_tensordot in Python (the statement the native planner is tested against)."""
     na, nb = len(a.legs), len(b.legs)
     for i in range(nc):
         _check_contract(a.legs[na - nc + i], b.legs[i], "tensordot")
