@@ -244,3 +244,23 @@ def test_native_tensordot_planner_hubbard():
     A1 = layout_of((left, phys, mid.flip()), (0, 0))
     A2 = layout_of((mid, phys, left.flip()), (0, 0))
     _same_gemm(P.plan_tensordot(A1, A2, 1), P._plan_tensordot_py(A1, A2, 1))
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_fuse_group_matches_loops(seed):
+    """The fused legs of one, two and three consecutive legs (U(1) and U(1)xU(1) charges, signs
+    of both kinds): the same charges, sub-sector offsets and dims as the per-tuple loops."""
+    rng = np.random.default_rng(400 + seed)
+
+    def leg(tuple_charges):
+        k = int(rng.integers(1, 6))
+        if tuple_charges:
+            ch = sorted({(int(a), int(b)) for a, b in rng.integers(-3, 4, (k, 2))})
+        else:
+            ch = sorted({int(a) for a in rng.integers(-6, 7, k)})
+        return Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))),
+                   int(rng.choice([1, -1])))
+    for tup in (False, True):
+        for nl in (1, 2, 3):
+            legs = [leg(tup) for _ in range(nl)]
+            assert P._fuse_group(legs) == P._fuse_group_py(legs)

@@ -862,28 +862,63 @@ class FuseInfo:
         self.groups = groups
         self.fused, self.subs = [], []
         for g in groups:
-            by_q: Dict = defaultdict(list)
-            import itertools
-            for t in itertools.product(*(range(len(legs[a].charges)) for a in g)):
-                qs = [np.asarray(legs[a].charges[s]) * legs[a].sign for a, s in zip(g, t)]
-                tot = sum(qs[1:], qs[0])
-                key = tuple(int(v) for v in np.ravel(tot)) if np.ndim(tot) else int(tot)
-                by_q[key].append(t)
-            qs = sorted(by_q)
-            subs, dims = [], []
-            for q in qs:
-                off, items = 0, {}
-                for t in by_q[q]:
-                    nn = int(np.prod([legs[a].dims[s] for a, s in zip(g, t)]))
-                    items[t] = (off, nn)
-                    off += nn
-                subs.append(items)
-                dims.append(off)
+            qs, subs, dims = _fuse_group([legs[a] for a in g])
             self.fused.append(Leg(tuple(qs), tuple(dims), 1))
             self.subs.append(subs)
         self.sector_of = [{t: (k, o, nn) for k, items in enumerate(subs)
                            for t, (o, nn) in items.items()} for subs in self.subs]
         self.matrix = canonical(tuple(self.fused), layout.charge)
+
+
+def _fuse_group(legs):
+    """The fused leg of consecutive legs: its charges (the signed totals of every sector tuple,
+    sorted), per fused sector the sub-sector tuples in product order with their (offset, size),
+    and the fused dims. The charge sums and sizes of all tuples are computed at once."""
+    n = [len(l.charges) for l in legs]
+    if not legs:
+        return [0], [{(): (0, 1)}], [1]
+    idx = np.indices(n).reshape(len(legs), -1)          # product order (C order)
+    q = [l.q * l.sign for l in legs]                      # (sectors, factors)
+    tot = sum(qa[ia] for qa, ia in zip(q, idx))           # (tuples, factors)
+    size = np.prod([np.asarray(l.dims, np.int64)[ia] for l, ia in zip(legs, idx)], axis=0)
+    scalar = not isinstance(legs[0].charges[0], tuple)
+    keys = [int(r[0]) for r in tot.tolist()] if scalar else [tuple(r) for r in tot.tolist()]
+    by_q: Dict = defaultdict(list)
+    tuples = list(map(tuple, idx.T.tolist()))
+    for t, k, nn in zip(tuples, keys, size.tolist()):
+        by_q[k].append((t, nn))
+    qs = sorted(by_q)
+    subs, dims = [], []
+    for k in qs:
+        off, items = 0, {}
+        for t, nn in by_q[k]:
+            items[t] = (off, nn)
+            off += nn
+        subs.append(items)
+        dims.append(off)
+    return qs, subs, dims
+
+
+def _fuse_group_py(legs):
+    """_fuse_group as per-tuple loops (the statement it is tested against)."""
+    import itertools
+    by_q: Dict = defaultdict(list)
+    for t in itertools.product(*(range(len(l.charges)) for l in legs)):
+        qv = [np.asarray(l.charges[s]) * l.sign for l, s in zip(legs, t)]
+        tot = sum(qv[1:], qv[0])
+        key = tuple(int(v) for v in np.ravel(tot)) if np.ndim(tot) else int(tot)
+        by_q[key].append(t)
+    qs = sorted(by_q)
+    subs, dims = [], []
+    for q in qs:
+        off, items = 0, {}
+        for t in by_q[q]:
+            nn = int(np.prod([l.dims[s] for l, s in zip(legs, t)]))
+            items[t] = (off, nn)
+            off += nn
+        subs.append(items)
+        dims.append(off)
+    return qs, subs, dims
 
 
 def plan_fuse(info: FuseInfo) -> HostCombPlan:
