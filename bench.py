@@ -356,7 +356,7 @@ def main():
                          # DRAM bytes read + written by the two gemm_f64_kernel launches of
                          # one matvec, from `ncu --set full --clock-control none -k
                          # regex:gemm_f64 -s 2 -c 3 python bench.py --steps 2 --warmup 1
-                         # --no-cpu` (14.73 MB + 34.15 MB): the operands L, theta, R once; the
+                         # --no-cpu --no-sweep` (14.73 MB + 34.15 MB): the operands L, theta, R once; the
                          # intermediates stay in the 129 MB L2
                          "traffic": 48.88e6,
                          "traffic_unit": "bytes per matvec (stages 1+3)",
