@@ -264,3 +264,41 @@ def test_fuse_group_matches_loops(seed):
         for nl in (1, 2, 3):
             legs = [leg(tup) for _ in range(nl)]
             assert P._fuse_group(legs) == P._fuse_group_py(legs)
+
+
+def _same_comb(a, b):
+    for x, y in zip(a.c, b.c):
+        assert x.dtype == y.dtype and np.array_equal(x, y)
+    assert a.out_layout.legs == b.out_layout.legs
+
+
+def _fuse_cases():
+    th, *_ = workloads.mid_bond_problem(seed=3, device="cpu")
+    yield th.layout, 0
+    rng = np.random.default_rng(10)
+    Wb, _ = to_block_mpo(workloads.hubbard_mpo(6, 1.0, 4.0),
+                         [workloads.HUBBARD_SITE_CHARGES] * 6, device="cpu")
+    phys = Wb[2].legs[2]
+    ch = [(a, b) for a in range(0, 5) for b in range(0, 5)]
+    left = Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))), 1)
+    right = Leg(tuple(ch), tuple(int(x) for x in rng.integers(1, 9, len(ch))), 1)
+    yield layout_of((left, phys, phys, right.flip()), (0, 0)), (0, 0)
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_vectorised_fuse_and_split_plans(case):
+    """The fused matrix copy and both splits back (row side with a truncated bond that keeps
+    only some row sectors, column side likewise): identical tables to the block-by-block
+    statements."""
+    lay, zero = list(_fuse_cases())[case]
+    info = P.FuseInfo(lay, 2)
+    _same_comb(P.plan_fuse(info), P._plan_fuse_py(info))
+    rows, cols = info.matrix.legs
+    rng = np.random.default_rng(case)
+    keep = sorted(rng.choice(len(rows.charges), max(1, len(rows.charges) // 2), replace=False))
+    bond = Leg(tuple(rows.charges[k] for k in keep),
+               tuple(int(rng.integers(1, 6)) for _ in keep), 1)
+    U = layout_of((rows, bond.flip()), zero)
+    Vh = layout_of((bond, cols), lay.charge)
+    _same_comb(P.plan_split_rows(info, U), P._plan_split_rows_py(info, U))
+    _same_comb(P.plan_split_cols(info, Vh), P._plan_split_cols_py(info, Vh))

@@ -868,6 +868,21 @@ class FuseInfo:
         self.sector_of = [{t: (k, o, nn) for k, items in enumerate(subs)
                            for t, (o, nn) in items.items()} for subs in self.subs]
         self.matrix = canonical(tuple(self.fused), layout.charge)
+        # the same maps as arrays over the flat index of a sector tuple (C order)
+        self.nsec = [tuple(len(legs[a].charges) for a in g) for g in groups]
+        self.lut = []
+        for ns, so in zip(self.nsec, self.sector_of):
+            lut = np.zeros((3, int(np.prod(ns)) if ns else 1), np.int64)
+            for t, v in so.items():
+                lut[:, np.ravel_multi_index(t, ns) if ns else 0] = v
+            self.lut.append(lut)
+
+    def lookup(self, g: int, keys: np.ndarray):
+        """(fused sector, offset, size) of the sector tuples `keys` (rows) of group g."""
+        ns = self.nsec[g]
+        flat = np.ravel_multi_index(tuple(np.asarray(keys, np.int64).T), ns) if ns else \
+            np.zeros(len(keys), np.int64)
+        return self.lut[g][:, flat]
 
 
 def _fuse_group(legs):
@@ -921,8 +936,54 @@ def _fuse_group_py(legs):
     return qs, subs, dims
 
 
+def _block_map2(lay: Layout) -> np.ndarray:
+    """Block index of every (row sector, column sector) of a two-leg layout, -1 where absent."""
+    m = np.full((len(lay.legs[0].charges), len(lay.legs[1].charges)), -1, np.int64)
+    if lay.nblocks:
+        m[lay.blocks[:, 0], lay.blocks[:, 1]] = np.arange(lay.nblocks)
+    return m
+
+
+def _lookup2(bmap: np.ndarray, i: np.ndarray, j: np.ndarray) -> np.ndarray:
+    """bmap[i, j], -1 where (i, j) lies outside it."""
+    ok = (i >= 0) & (i < bmap.shape[0]) & (j >= 0) & (j < bmap.shape[1])
+    out = np.full(len(i), -1, np.int64)
+    out[ok] = bmap[i[ok], j[ok]]
+    return out
+
+
+def _comb_tables(dst, rows, cols, ld, cs, src, src_ld, has):
+    """One combination task per entry (with one unit term where `has`, else none)."""
+    n = len(dst)
+    t = np.zeros(n, COMB_TASK)
+    t["dst_off"], t["rows"], t["cols"], t["dst_ld"], t["dst_cs"] = dst, rows, cols, ld, cs
+    cnt = np.asarray(has, np.int64)
+    end = np.cumsum(cnt)
+    t["term_begin"], t["term_end"] = end - cnt, end
+    u = np.zeros(int(cnt.sum()), COMB_TERM)
+    sel = np.nonzero(cnt)[0]
+    u["src_off"], u["src_ld"], u["src_cs"], u["coef"] = src[sel], src_ld[sel], 1, 1.0
+    return _CombArrays(t, u)
+
+
 def plan_fuse(info: FuseInfo) -> HostCombPlan:
-    """Copy every block of `info.layout` into its place in the fused matrix."""
+    """Copy every block of `info.layout` into its place in the fused matrix (one strided copy
+    per block, vectorised; _plan_fuse_py states it block by block)."""
+    lay, mat = info.layout, info.matrix
+    nr = info.nrow
+    if lay.nblocks == 0:
+        return HostCombPlan(CombTable(), mat)
+    rs, ro, rn = info.lookup(0, lay.blocks[:, :nr])
+    cs_, co, cn = info.lookup(1, lay.blocks[:, nr:])
+    km = _block_map2(mat)[rs, cs_]
+    ncols = mat.shapes[km, 1]
+    dst = mat.offsets[km] + ro * ncols + co
+    return HostCombPlan(_comb_tables(dst, rn, cn, ncols, 1, lay.offsets, cn,
+                                     np.ones(lay.nblocks, bool)), mat)
+
+
+def _plan_fuse_py(info: FuseInfo) -> HostCombPlan:
+    """plan_fuse block by block (the statement the vectorised form is tested against)."""
     lay, mat = info.layout, info.matrix
     c = CombTable()
     nr = info.nrow
@@ -939,7 +1000,22 @@ def plan_fuse(info: FuseInfo) -> HostCombPlan:
 
 def plan_split_rows(info: FuseInfo, m: Layout) -> HostCombPlan:
     """Split the fused row leg of a matrix layout `m` (legs (F0, k)) back into info's row legs:
-    result legs = row legs + (k,)."""
+    result legs = row legs + (k,). Vectorised; _plan_split_rows_py states it block by block."""
+    nr = info.nrow
+    rows = info.layout.legs[:nr]
+    out = canonical(tuple(rows) + (m.legs[1],), _charge_of_rows(info, m))
+    if out.nblocks == 0:
+        return HostCombPlan(CombTable(), out)
+    rs, ro, rn = info.lookup(0, out.blocks[:, :nr])
+    km = _lookup2(_block_map2(m), rs, out.blocks[:, nr])
+    ncols = out.shapes[:, -1]
+    has = km >= 0
+    src = np.where(has, m.offsets[np.maximum(km, 0)] + ro * ncols, 0)
+    return HostCombPlan(_comb_tables(out.offsets, rn, ncols, ncols, 1, src, ncols, has), out)
+
+
+def _plan_split_rows_py(info: FuseInfo, m: Layout) -> HostCombPlan:
+    """plan_split_rows block by block (the statement the vectorised form is tested against)."""
     nr = info.nrow
     rows = info.layout.legs[:nr]
     out = canonical(tuple(rows) + (m.legs[1],), _charge_of_rows(info, m))
@@ -963,7 +1039,25 @@ def _charge_of_rows(info, m):
 
 def plan_split_cols(info: FuseInfo, m: Layout) -> HostCombPlan:
     """Split the fused column leg of a matrix layout `m` (legs (k, F1)) back into info's column
-    legs: result legs = (k,) + col legs."""
+    legs: result legs = (k,) + col legs. Vectorised; _plan_split_cols_py states it block by
+    block."""
+    nr = info.nrow
+    cols = info.layout.legs[nr:]
+    out = canonical((m.legs[0],) + tuple(cols), m.charge)
+    if out.nblocks == 0:
+        return HostCombPlan(CombTable(), out)
+    cs_, co, cn = info.lookup(1, out.blocks[:, 1:])
+    km = _lookup2(_block_map2(m), out.blocks[:, 0], cs_)
+    nrows = out.shapes[:, 0]
+    has = km >= 0
+    kk = np.maximum(km, 0)
+    src = np.where(has, m.offsets[kk] + co, 0)
+    ld = np.where(has, m.shapes[kk, 1], 0)
+    return HostCombPlan(_comb_tables(out.offsets, nrows, cn, cn, 1, src, ld, has), out)
+
+
+def _plan_split_cols_py(info: FuseInfo, m: Layout) -> HostCombPlan:
+    """plan_split_cols block by block (the statement the vectorised form is tested against)."""
     nr = info.nrow
     cols = info.layout.legs[nr:]
     out = canonical((m.legs[0],) + tuple(cols), m.charge)
