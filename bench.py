@@ -28,6 +28,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -239,8 +240,7 @@ def main():
     torch.cuda.synchronize()
 
     # --- device-resident timed region: K matvecs, L2 flushed before each ---
-    clk_path = os.path.join(HERE, "gpurun_out", f"clocks_rank{rank}.csv")
-    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    clk_path = os.path.join(tempfile.gettempdir(), f"tnk_bench_clocks_rank{rank}.csv")
     sampler, fh = _clock_sampler(clk_path)
     if world > 1:
         dist.barrier()
