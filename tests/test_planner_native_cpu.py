@@ -302,3 +302,25 @@ def test_vectorised_fuse_and_split_plans(case):
     Vh = layout_of((bond, cols), lay.charge)
     _same_comb(P.plan_split_rows(info, U), P._plan_split_rows_py(info, U))
     _same_comb(P.plan_split_cols(info, Vh), P._plan_split_cols_py(info, Vh))
+
+
+def test_native_planners_on_layouts_without_blocks():
+    """A theta with no allowed block (bond charges that cannot meet the total charge): every
+    planner returns empty tables, identical between the native and Python forms."""
+    Wb, _ = to_block_mpo(workloads.xxz_mpo(6), [[1, -1]] * 6, device="cpu")
+    W1, W2 = Wb[2], Wb[3]
+    phys = W1.legs[2]
+    left, right = Leg((-4,), (3,), 1), Leg((4,), (2,), 1)
+    th = layout_of((left, phys, phys, right.flip()), 0)
+    L = layout_of((left, W1.legs[0].flip(), left.flip()), 0)
+    R = layout_of((right.flip(), W2.legs[1].flip(), right), 0)
+    assert th.nblocks == 0
+    hp = _both(th, L, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))], R)
+    assert hp.macs == 0 and len(hp.g1[0]) == 0
+    A = layout_of((left, phys, right.flip()), 0)
+    _same_plan(P.plan_left_env(L, A, (W1.layout, _host_of(W1))),
+               P._plan_left_env_py(L, A, (W1.layout, _host_of(W1))))
+    B = layout_of((right, phys, left.flip()), 0)
+    _same_gemm(P.plan_tensordot(A, B, 1), P._plan_tensordot_py(A, B, 1))
+    info = P.FuseInfo(th, 2)
+    _same_comb(P.plan_fuse(info), P._plan_fuse_py(info))
