@@ -82,3 +82,22 @@ def test_launch_units_owned_by_their_problem():
         assert np.array_equal(own4, np.searchsorted(starts[:, 1], t4["dst_off"][hb.c4[2]["task"]],
                                                     side="right") - 1)
     assert len(own2) == len(hb.c2[2]) and own2.max() == 2
+
+
+def test_full_64_chain_workload_plans():
+    """Every local problem of the 64-chain batch workload plans, and the concatenated plan of all
+    64 has every problem's tasks, segments, combination terms and MAC count."""
+    probs = B.batch_problems(64, seed=2, device="cpu")
+    plans = [P.plan_apply(th, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
+                          R.layout) for th, L, W1, W2, R in probs]
+    sizes = np.array([[L.host.size, th.size, R.host.size, hp.ws1 + hp.ws2_unsplit]
+                      for (th, L, _, _, R), hp in zip(probs, plans)], np.int64)
+    starts = np.vstack([np.zeros(4, np.int64), np.cumsum(sizes, 0)])
+    hb = B.batch_plan(plans, [tuple(int(v) for v in starts[k]) for k in range(64)],
+                      [int(starts[k, 1]) for k in range(64)], int(starts[-1, 3]),
+                      int(starts[-1, 1]))
+    assert len(hb.g1[0]) == sum(len(p.g1[0]) for p in plans)
+    assert len(hb.c2[1]) == sum(len(p.c2[1]) for p in plans)
+    assert len(hb.g3_unsplit[1]) == sum(len(p.g3_unsplit[1]) for p in plans)
+    assert hb.macs == sum(p.macs for p in plans)
+    assert int(starts[-1, 1]) == sum(th.size for th, *_ in probs)
