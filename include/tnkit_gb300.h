@@ -156,8 +156,10 @@ int tnk_update_right_env_f64(const tnk_plan3* plan, const double* R, const doubl
  * (64 MiB, enough for the chi=1024 U(1) XXZ mid bond, which needs 7.9 M), held on every GPU that
  * loads the library until the process exits. Plans needing more scratch get TNK_ERR_SIZE. The
  * first call on each device looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture. All calls share the array, so
- * calls that overlap on the GPU race; order them on one stream. Allocates nothing. */
+ * device current; make that first call before any stream capture. The address is cached for the
+ * process: after a cudaDeviceReset of that device it is stale, so do not call this entry point on
+ * a device that was reset. All calls share the array, so calls that overlap on the GPU race;
+ * order them on one stream. Allocates nothing. */
 #define TNK_NOALLOC_SCRATCH_ELEMS 8388608
 int tnk_apply_two_site_f64_noalloc(const tnk_plan3* plan, const double* L, const double* theta,
                                    const double* R, double* out, void* stream);

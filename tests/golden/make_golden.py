@@ -1,13 +1,15 @@
 """Generate the golden fixtures of this directory by running the reference tnkit itself.
 
-This script is test infrastructure. It imports the reference package read-only from the path
-given by ``--ref`` (default ``/root/reference``) and writes small JSON / NPZ fixtures next to
-itself. The fixtures are committed; the script is not needed at test time.
+This script is test infrastructure. It imports the reference package read-only from the
+checkout given by ``--ref`` (or the ``TNKIT_REF`` environment variable; one of the two is
+required) and writes small JSON / NPZ fixtures next to itself. The fixtures are committed; the
+script is not needed at test time.
 
 usage:
+  export TNKIT_REF=<path of a tnkit 0.3.0 checkout>
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py small      # seconds
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py dmrg       # a few minutes
-  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py c2         # ~25 min on 8 cores
+  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py c2         # ~30 min on 8 cores
   PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py hubbard    # a minute
 
 Modes:
@@ -16,9 +18,12 @@ Modes:
          apply_one_site, update_left_env, update_right_env and truncated_svd, plus a thick-restart
          Lanczos known answer.  -> local_problems.npz, local_problems.json
   dmrg   Per-sweep energies of whole reference DMRG runs at small and medium sizes (TFIM N=10
-         chi=32 dense; XXZ N=12 U(1); XXZ N=64 U(1) at chi=64/128).  -> dmrg_small.json
-  c2     The XXZ N=64 U(1) chi=1024 six-sweep run: energies, sweep times, matvec counts and every
-         bond's sector dims.  -> c2_xxz_n64_chi1024.json
+         chi=32 dense; XXZ N=12 U(1); XXZ N=64 U(1) at chi=64/128), with the discarded weight
+         and every bond's entanglement entropy of the final state (the reference's
+         all_entropies of its to_dense_mps).  -> dmrg_small.json
+  c2     The XXZ N=64 U(1) chi=1024 six-sweep run: energies, sweep times, matvec counts, every
+         bond's sector dims, every bond's entropy and the mid bond's Schmidt spectrum.
+         -> c2_xxz_n64_chi1024.json
   hubbard  The Fermi-Hubbard chain (t=1, U=4, half filling) under U(1) x U(1) (N_up, N_dn)
          blocks, with the hand-written width-6 MPO of tnkit_gb300/workloads.py: the
          reference's block MPO tensor of a bulk site, its seeded random block MPS, and the
@@ -76,6 +81,19 @@ def _bt(prefix, t, arrays, meta):
     t = t.canonical()
     arrays[prefix] = np.asarray(t.data)
     meta[prefix] = {"legs": _legs_json(t.struct), "charge": int(t.struct.charge)}
+
+
+def _block_spectra(mps, site_charges):
+    """Every bond's entropy of a block MPS and its Schmidt spectra, by the reference's own
+    route: to_dense_mps (tnkit/block_backend.py:462-466), then the one-sweep
+    _schmidt_sweep / _entropy of all_entropies (tnkit/observables.py:313-387)."""
+    from tnkit.block_backend import to_dense_mps
+    from tnkit.observables import _canon, _entropy, _schmidt_sweep, _backend_for
+    dense = [np.asarray(t) for t in to_dense_mps(mps, site_charges)]
+    be = _backend_for(dense)
+    canon = _canon(dense, be)
+    spectra = [np.asarray(s, dtype=np.float64) for s in _schmidt_sweep(canon, be, len(dense) - 1)]
+    return [float(_entropy(s)) for s in spectra], spectra
 
 
 def mode_small(ref):
@@ -226,10 +244,12 @@ def mode_dmrg(ref):
         t0 = time.perf_counter()
         E, mps, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=sweeps, tol=0, rtol=0,
                             expand=0, backend="numpy-real")
+        ent, _ = _block_spectra(mps, [[1, -1]] * N)
         out[f"xxz_n{N}_chi{chi}"] = {
             "E": float(E), "energies": [float(e) for e in info["energies"]],
             "matvec_calls": int(info["matvec_calls"]), "sweep_s": info["sweep_s"],
             "discarded_weight": float(info["discarded_weight"]),
+            "entropies": ent,
             "bonds": [{"charges": [int(c) for c in m.legs[2].charges],
                        "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
             "wall_s": time.perf_counter() - t0}
@@ -247,15 +267,19 @@ def mode_c2(ref):
     t0 = time.perf_counter()
     E, mps, info = dmrg(Wb, chi, charge=0, seed=1, n_sweeps=6, tol=0, rtol=0, expand=0,
                         backend="numpy-real", verbose=True)
+    wall = time.perf_counter() - t0
+    ent, spectra = _block_spectra(mps, [[1, -1]] * N)
     rec = {"E": float(E), "energies": [float(e) for e in info["energies"]],
            "matvec_calls": int(info["matvec_calls"]), "sweep_s": info["sweep_s"],
            "phase_time": info["phase_time"],
            "discarded_weight": float(info["discarded_weight"]),
+           "entropies": ent,
+           "mid_bond_spectrum": [float(x) for x in spectra[N // 2 - 1]],
            "bonds": [{"charges": [int(c) for c in m.legs[2].charges],
                       "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
            "host": {"cpu_count": os.cpu_count(),
                     "omp": os.environ.get("OMP_NUM_THREADS")},
-           "wall_s": time.perf_counter() - t0}
+           "wall_s": wall}
     with open(os.path.join(HERE, "c2_xxz_n64_chi1024.json"), "w") as f:
         json.dump(rec, f, indent=1)
     print("E", E)
@@ -301,9 +325,11 @@ def mode_hubbard(ref):
         t0 = time.perf_counter()
         E, mps, info = dmrg(Wbn, chi, charge=(N // 2, N // 2), seed=1, n_sweeps=sweeps, tol=0,
                             rtol=0, expand=0, backend="numpy-real")
+        ent, _ = _block_spectra(mps, [list(HUBBARD_SITE_CHARGES)] * N)
         runs[f"n{N}_chi{chi}"] = {
             "E": float(E), "energies": [float(e) for e in info["energies"]],
             "discarded_weight": float(info["discarded_weight"]),
+            "entropies": ent,
             "bonds": [{"charges": [list(c) for c in m.legs[2].charges],
                        "dims": [int(d) for d in m.legs[2].dims]} for m in mps],
             "wall_s": time.perf_counter() - t0}
@@ -365,8 +391,11 @@ def mode_tdvp(ref):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp", "hubbard"])
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("TNKIT_REF"),
+                    help="path of the reference tnkit checkout (or set TNKIT_REF)")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref or the TNKIT_REF environment variable")
     ref = _import_ref(a.ref)
     {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2, "tdvp": mode_tdvp,
      "hubbard": mode_hubbard}[a.mode](ref)

@@ -100,7 +100,7 @@ def test_hellmann_feynman_gradient_matches_exact_and_finite_differences():
     g = energy_gradient_xxz(M, delta)
     assert np.abs(g - g_ed).max() <= 1e-8 * np.abs(g_ed).max(), (g, g_ed)
     assert abs(float(J @ g) - E) <= 1e-10 * abs(E)          # E = sum_i J_i <h_i>
-    h = 1e-4
+    h = 1e-5                      # the central-difference step the configuration names
     for i in (0, 4, 8):
         Jp, Jm = J.copy(), J.copy()
         Jp[i] += h

@@ -13,6 +13,10 @@
 // must not use the array's name as a device pointer (on the host it names a stand-in object), so
 // the first call on each device looks its device address up with cudaGetSymbolAddress, with that
 // device current, and caches it; that first call should therefore come before any stream capture.
+// The cached address belongs to the device's current primary context: after cudaDeviceReset (or
+// anything else that destroys that context) the module is loaded again at a new address and the
+// cached one is stale, so a process that resets a device must not call this entry point on it
+// again.
 // Every call shares the one array, which keeps the previous call's contents: calls that overlap
 // on the GPU (different streams, or threads, without ordering between them) race on it. Nothing
 // in the scratch needs to start at zero: every element a call reads is first written by that

@@ -17,6 +17,7 @@
 #include <climits>
 #include <cmath>
 #include <map>
+#include <new>
 #include <stdexcept>
 #include <unordered_map>
 #include <utility>
@@ -748,23 +749,26 @@ void table(const std::vector<T>& v, const void** data, int64_t* count) {
     *count = (int64_t)v.size();
 }
 
-}  // namespace
-
-extern "C" int tnk_apply_plan_build(const tnk_apply_plan_in* in, void** handle) {
-    if (!in || !handle) {
-        tnk::set_error("tnk_apply_plan_build: null argument");
-        return TNK_ERR_ARG;
-    }
-    *handle = nullptr;
-    PlanBuild* pb = new PlanBuild();
+// Runs one builder into a fresh PlanBuild with every C++ exception turned into a status code
+// (no exception may cross the C ABI: a ctypes caller would abort), then hands the plan over.
+template <typename F>
+int guarded_build(const char* what, void** handle, F&& build) {
+    PlanBuild* pb = nullptr;
     int rc;
     try {
-        rc = apply_build(in, pb);
+        pb = new PlanBuild();
+        rc = build(pb);
     } catch (const Overflow&) {
-        tnk::set_error("plan_apply: a table entry exceeds 32 bits");
+        tnk::set_error("%s: a table entry exceeds 32 bits", what);
+        rc = TNK_ERR_SIZE;
+    } catch (const std::bad_alloc&) {
+        tnk::set_error("%s: out of host memory", what);
         rc = TNK_ERR_SIZE;
     } catch (const std::exception& e) {
-        tnk::set_error("plan_apply: %s", e.what());
+        tnk::set_error("%s: %s", what, e.what());
+        rc = TNK_ERR_ARG;
+    } catch (...) {
+        tnk::set_error("%s: unexpected exception", what);
         rc = TNK_ERR_ARG;
     }
     if (rc) {
@@ -775,29 +779,26 @@ extern "C" int tnk_apply_plan_build(const tnk_apply_plan_in* in, void** handle) 
     return TNK_OK;
 }
 
+}  // namespace
+
+extern "C" int tnk_apply_plan_build(const tnk_apply_plan_in* in, void** handle) {
+    if (!in || !handle) {
+        tnk::set_error("tnk_apply_plan_build: null argument");
+        return TNK_ERR_ARG;
+    }
+    *handle = nullptr;
+    return guarded_build("plan_apply", handle,
+                         [&](PlanBuild* pb) { return apply_build(in, pb); });
+}
+
 extern "C" int tnk_env_plan_build(const tnk_env_plan_in* in, void** handle) {
     if (!in || !handle) {
         tnk::set_error("tnk_env_plan_build: null argument");
         return TNK_ERR_ARG;
     }
     *handle = nullptr;
-    PlanBuild* pb = new PlanBuild();
-    int rc;
-    try {
-        rc = env_build(in, pb);
-    } catch (const Overflow&) {
-        tnk::set_error("plan_env: a table entry exceeds 32 bits");
-        rc = TNK_ERR_SIZE;
-    } catch (const std::exception& e) {
-        tnk::set_error("plan_env: %s", e.what());
-        rc = TNK_ERR_ARG;
-    }
-    if (rc) {
-        delete pb;
-        return rc;
-    }
-    *handle = pb;
-    return TNK_OK;
+    return guarded_build("plan_env", handle,
+                         [&](PlanBuild* pb) { return env_build(in, pb); });
 }
 
 extern "C" int tnk_tensordot_plan_build(const tnk_layout_desc* a, const tnk_layout_desc* b,
@@ -808,20 +809,8 @@ extern "C" int tnk_tensordot_plan_build(const tnk_layout_desc* a, const tnk_layo
         return TNK_ERR_ARG;
     }
     *handle = nullptr;
-    PlanBuild* pb = new PlanBuild();
-    int rc;
-    try {
-        rc = tensordot_build(a, b, out, nc, pb);
-    } catch (const Overflow&) {
-        tnk::set_error("plan_tensordot: a table entry exceeds 32 bits");
-        rc = TNK_ERR_SIZE;
-    }
-    if (rc) {
-        delete pb;
-        return rc;
-    }
-    *handle = pb;
-    return TNK_OK;
+    return guarded_build("plan_tensordot", handle,
+                         [&](PlanBuild* pb) { return tensordot_build(a, b, out, nc, pb); });
 }
 
 extern "C" int tnk_plan_tc_build(const tnk_gemm_task* t1, int64_t nt1, const tnk_gemm_seg* s1,
@@ -833,23 +822,8 @@ extern "C" int tnk_plan_tc_build(const tnk_gemm_task* t1, int64_t nt1, const tnk
         return TNK_ERR_ARG;
     }
     *handle = nullptr;
-    PlanBuild* pb = new PlanBuild();
-    int rc;
-    try {
-        rc = tc_build(t1, nt1, s1, t2, nt2, t3, nt3, s3, pb);
-    } catch (const Overflow&) {
-        tnk::set_error("plan_tc: a table entry exceeds 32 bits");
-        rc = TNK_ERR_SIZE;
-    } catch (const std::exception& e) {
-        tnk::set_error("plan_tc: %s", e.what());
-        rc = TNK_ERR_ARG;
-    }
-    if (rc) {
-        delete pb;
-        return rc;
-    }
-    *handle = pb;
-    return TNK_OK;
+    return guarded_build("plan_tc", handle,
+                         [&](PlanBuild* pb) { return tc_build(t1, nt1, s1, t2, nt2, t3, nt3, s3, pb); });
 }
 
 extern "C" int tnk_plan_split_k(const tnk_gemm_task* t, int64_t nt, const tnk_gemm_seg* s,
@@ -861,20 +835,8 @@ extern "C" int tnk_plan_split_k(const tnk_gemm_task* t, int64_t nt, const tnk_ge
         return TNK_ERR_ARG;
     }
     *handle = nullptr;
-    PlanBuild* pb = new PlanBuild();
-    int rc;
-    try {
-        rc = split_build(t, nt, s, ws_base, slots, max_chunks, tile_m, tile_n, pb);
-    } catch (const Overflow&) {
-        tnk::set_error("plan_split_k: a table entry exceeds 32 bits");
-        rc = TNK_ERR_SIZE;
-    }
-    if (rc) {
-        delete pb;
-        return rc;
-    }
-    *handle = pb;
-    return TNK_OK;
+    return guarded_build("plan_split_k", handle,
+                         [&](PlanBuild* pb) { return split_build(t, nt, s, ws_base, slots, max_chunks, tile_m, tile_n, pb); });
 }
 
 extern "C" int tnk_planb_table(const void* handle, int32_t id, const void** data,

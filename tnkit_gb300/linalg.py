@@ -442,25 +442,31 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
         for _, _, M in blocks:
             mats.append(M)
             shapes.append((tuple(M.shape), scale))
+    if not mats:
+        raise ValueError("the matrices have no allowed blocks")
     if method == "svd":
         fn = lambda M: tuple(torch.linalg.svd(M, full_matrices=False, driver=driver)) + (None,)
         facs = _concurrent().map([fn] * len(mats), mats, mats[0].device) if len(mats) > 1 \
             else [fn(M) for M in mats]
     else:
         blas = _host_blas() if host != "never" else None
-        on_host = ([False] * len(mats) if blas is None else
-                   [True] * len(mats) if host == "always" else
+        # host='always' factors every sector with host LAPACK whether or not the library's
+        # thread control was found (as truncated_svd does); 'auto' needs that control to split
+        on_host = ([True] * len(mats) if host == "always" else
+                   [False] * len(mats) if blas is None else
                    _assign_sectors([sh for sh, _ in shapes], True))
         fns = [_gram_pick(sc)(M, _svd_gram_host if h else _svd_gram_native)
                if sc in ("right", "left") else (_svd_gram_host if h else _svd_gram_native)
                for M, (_, sc), h in zip(mats, shapes, on_host)]
-        if any(on_host):
+        if any(on_host) and blas is not None:
             prev = blas[1]()
             blas[0](max(1, prev // _HOST_THREADS_DIV))
             try:
                 facs = _map_hybrid(fns, mats, on_host, mats[0].device)
             finally:
                 blas[0](prev)
+        elif any(on_host):
+            facs = _map_hybrid(fns, mats, on_host, mats[0].device)
         elif len(mats) > 1:
             facs = _concurrent().map(fns, mats, mats[0].device)
         else:
