@@ -340,6 +340,18 @@ int tnk_zgemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c,
 int tnk_zaxpby_f64(const double* x, double* y, int64_t n, const double* sa, double fa,
                    const double* sb, double fb, void* stream);
 
+/* Eigenvalues (ascending) and eigenvectors of `batch` real symmetric tridiagonal matrices of
+ * order n <= TNK_TRIDIAG_MAX_N, on the device: matrix b has diagonal d[b*ld_d + i] and
+ * off-diagonal e[b*ld_e + i] (i < n - 1); lam[b*n + j] and column j of the row-major n x n
+ * V[b*n*n ...] are its j-th eigenpair. Implicit QL with Wilkinson-type shifts, one thread block
+ * per matrix; info[b] = 0, or the index + 1 of an eigenvalue that did not converge. Replaces the
+ * tridiagonal eigensolve of the reference's Krylov exponential, expm_sym_tridiag_eigh(_batched)
+ * (tnkit/backend.py:643-661, :729-751), whose torch.linalg.eigh it computes. */
+#define TNK_TRIDIAG_MAX_N 128
+int tnk_tridiag_eig_f64(const double* d, const double* e, int64_t n, int64_t batch,
+                        int64_t ld_d, int64_t ld_e, double* lam, double* V, int32_t* info,
+                        void* stream);
+
 /* ----------------------------------------------------------------------------------------
  * Truncation: the per-sector factorisation of tnkit/blocks.py:1380-1462 with method='gram'
  * (the block SVD through the smaller Gram matrix, tnkit/blocks.py:1345-1377) on cuSOLVER and

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "libtnkit_gb300.so")
 
 TNK_OK, TNK_ERR_ARG, TNK_ERR_CUDA, TNK_ERR_SIZE, TNK_ERR_DEVICE = 0, 1, 2, 3, 4
 TNK_RED_ELEMS = 65536
+TNK_TRIDIAG_MAX_N = 128
 
 
 class LibraryMissing(RuntimeError):
@@ -135,6 +136,7 @@ _SIGS = {
     "tnk_zmultidot_f64": ([_P, _I64, _I32, _P, _I64, _P, _P, _P], C.c_int),
     "tnk_zgemv_sub_f64": ([_P, _I64, _I32, _P, _P, _I64, _P], C.c_int),
     "tnk_zaxpby_f64": ([_P, _P, _I64, _P, _D, _P, _D, _P], C.c_int),
+    "tnk_tridiag_eig_f64": ([_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P], C.c_int),
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
     "tnk_env_plan_build": ([_P, _P], C.c_int),

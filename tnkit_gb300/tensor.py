@@ -57,16 +57,22 @@ class BlockTensor:
         return f"BlockTensor({self.layout})"
 
     @staticmethod
-    def from_reference(t, device="cuda") -> "BlockTensor":
-        """Wrap a reference `tnkit.blocks.BlockTensor` (any struct; re-laid out canonically by
-        the reference's own `.canonical()` first) without copying its numbers' meaning."""
+    def from_reference(t, device="cuda", dtype=None) -> "BlockTensor":
+        """This package's tensor of a reference `tnkit.blocks.BlockTensor` (any struct; laid out
+        canonically by the reference's own `.canonical()` first): the same canonical buffer,
+        block for block, moved to `device`. Real data become float64 and complex data
+        complex128 unless `dtype` is given; a real tensor also keeps its host copy (MPO tensors'
+        entries become plan coefficients)."""
         import torch
         c = t.canonical()
         lay = layout_of([Leg.of(l) for l in c.struct.legs], c.struct.charge)
-        host = np.ascontiguousarray(np.asarray(c.data if isinstance(c.data, np.ndarray)
-                                               else c.data.detach().cpu().numpy()),
-                                    dtype=np.float64)
-        return BlockTensor(lay, torch.as_tensor(host, device=device), host)
+        d = c.data
+        x = d.detach() if isinstance(d, torch.Tensor) else torch.as_tensor(np.asarray(d))
+        if dtype is None:
+            dtype = torch.complex128 if torch.is_complex(x) else torch.float64
+        x = x.to(dtype=dtype).contiguous()
+        host = None if torch.is_complex(x) else x.cpu().numpy()
+        return BlockTensor(lay, x.to(device), host)
 
 
 def dense_layout(shape: Sequence[int], signs: Sequence[int]) -> Layout:
