@@ -181,13 +181,19 @@ def main():
                          "at N=1)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the whole chi=1024 DMRG leg (FP64 against mixed-ff, ~2 minutes)")
-    ap.add_argument("--batch", action="store_true",
-                    help="also time the 64-chain batched local problems (sequential, batched, "
-                         "graph-captured)")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 64-chain batched local problems (sequential, batched, "
+                         "graph-captured; a few seconds, run by default at N=1)")
     ap.add_argument("--batch-dmrg", action="store_true",
                     help="also run the 16-chain batched DMRG against one chain after another: "
                          "minutes")
     ap.add_argument("--batch-sweeps", type=int, default=2)
+    ap.add_argument("--batch-chains", type=int, default=16,
+                    help="chains of the batched-DMRG leg: the first half Ising and half XXZ of "
+                         "the 64 seed-2 draws (64: all of them)")
+    ap.add_argument("--c5", action="store_true",
+                    help="also run the differentiated configuration: disordered XXZ N=48 chi=512 "
+                         "DMRG, dE/dJ_i by Hellmann-Feynman, central differences at three bonds")
     ap.add_argument("--batch-pipeline", action="store_true",
                     help="batched DMRG with the two chain groups' phases overlapped")
     ap.add_argument("--sweep-chi", type=int, default=1024)
@@ -377,10 +383,12 @@ def main():
                                      "float_float": per_step + 1}
     if args.sweep or (world == 1 and not args.no_sweep):
         line["sweep"] = sweep_leg(torch, args)
-    if args.batch:
+    if world == 1 and not args.no_batch:
         line["batch"] = batch_leg(torch, dev, flush, max(args.steps, 5))
     if args.batch_dmrg:
         line["batch_dmrg"] = batch_dmrg_leg(torch, args)
+    if args.c5:
+        line["c5_gradient"] = c5_leg(torch, args)
     if not args.no_cpu:
         dt, reps = cpu_matvec_baseline(th, L, W1, W2, R)
         line["cpu_baseline"] = {"value": flops_ref / dt / 1e9, "unit": "GFLOP/s",
@@ -558,17 +566,19 @@ def batch_leg(torch, dev, flush, steps):
 
 
 def batch_dmrg_leg(torch, args):
-    """Whole DMRG of a sample of the 64-chain workload -- the first 8 Ising and first 8 XXZ
-    chains of the seed-2 draws, `--batch-sweeps` sweeps each, seeds 0..15 -- run one chain after
-    another with `dmrg` (FP64) and as one lockstep batch (`dmrg_batch`, FP64 and float-float);
-    after an untimed warm-up of both drivers. Wall-clock seconds and the largest energy
-    difference between the batched and the one-by-one runs."""
+    """Whole DMRG of the 64-chain workload or a sample of it -- the first `--batch-chains` / 2
+    Ising and as many XXZ chains of the seed-2 draws (all 64 with --batch-chains 64),
+    `--batch-sweeps` sweeps each, seeds 0..K-1 -- run one chain after another with `dmrg` (FP64)
+    and as one lockstep batch (`dmrg_batch`, FP64 and float-float); after an untimed warm-up of
+    both drivers. Wall-clock seconds and the largest energy difference between the batched and
+    the one-by-one runs."""
     from tnkit_gb300 import batch as B, workloads
     from tnkit_gb300.batch_dmrg import dmrg_batch
     from tnkit_gb300.dmrg import dmrg
     from tnkit_gb300.mpo import to_block_mpo
     draws = B.chain_draws(64, 2)
-    sel = [d for d in draws if d[0] == "tfim"][:8] + [d for d in draws if d[0] == "xxz"][:8]
+    half = max(1, args.batch_chains // 2)
+    sel = [d for d in draws if d[0] == "tfim"][:half] + [d for d in draws if d[0] == "xxz"][:half]
 
     def mk(m, g, N):
         return workloads.tfim_mpo(N, g) if m == "tfim" else \
@@ -578,9 +588,9 @@ def batch_dmrg_leg(torch, args):
                **dict(kw, n_sweeps=1))
     dmrg(mk("xxz", 1.0, 8), 16, charge=0, **dict(kw, n_sweeps=1))
     torch.cuda.synchronize()
-    out = {"workload": "DMRG of 16 chains (the first 8 transverse-field Ising and first 8 U(1) "
-                       "XXZ chains of the 64-chain seed-2 draws), "
-                       f"{args.batch_sweeps} sweeps each, seeds 0..15",
+    out = {"workload": f"DMRG of {len(sel)} chains (the first {half} transverse-field Ising and "
+                       f"first {half} U(1) XXZ chains of the 64-chain seed-2 draws), "
+                       f"{args.batch_sweeps} sweeps each, seeds 0..{len(sel) - 1}",
            "chains": [list(d) for d in sel]}
     for prec in ("f64", "ff"):
         t0 = time.perf_counter()
@@ -664,6 +674,24 @@ def sweep_leg(torch, args):
                             "largest_sector": int(max(M[N // 2].legs[0].dims))}}
         if ref is not None:
             rec["abs_dE_vs_reference"] = abs(E - ref["E"])
+            rec["discarded_weight_reference"] = ref["discarded_weight"]
+            rec["abs_discarded_weight_diff"] = abs(info["discarded_weight"] -
+                                                   ref["discarded_weight"])
+            if "entropies" in ref:
+                # the final state's Schmidt spectra (exact per-sector SVD sweep, after the timed
+                # run) against the reference's own (its all_entropies of to_dense_mps)
+                from tnkit_gb300.observables import _entropy, schmidt_spectra
+                sp = schmidt_spectra(M)
+                S = np.array([_entropy(x) for x in sp])
+                Sr = np.asarray(ref["entropies"])
+                mid = sp[N // 2 - 1]
+                mr = np.asarray(ref["mid_bond_spectrum"])
+                k = min(len(mid), len(mr))
+                rec["entropy_max_rel_err_vs_reference"] = float(np.max(np.abs(S - Sr) /
+                                                                       np.abs(Sr)))
+                rec["mid_entropy"] = float(S[N // 2 - 1])
+                rec["mid_spectrum_max_abs_err_vs_reference"] = float(np.max(np.abs(mid[:k] -
+                                                                                   mr[:k])))
         out[prec] = rec
     if "f64" in out:
         for p in precs:
@@ -671,6 +699,55 @@ def sweep_leg(torch, args):
                 out[p]["abs_dE_vs_f64"] = abs(out[p]["E"] - out["f64"]["E"])
                 out[p]["speedup_total_vs_f64"] = out["f64"]["total_s"] / out[p]["total_s"]
     return out
+
+
+def c5_leg(torch, args):
+    """The differentiated configuration: the disordered XXZ chain N=48 (J_i uniform in
+    [0.5, 1.5] from seed 2, Delta=1) under U(1) at chi=512. The ground state by DMRG in FP64 (the
+    Hamiltonian is real, so its ground state is real: the reference's complex128 run reaches
+    the same state times a phase), then dE/dJ_i of every bond by Hellmann-Feynman
+    (grad.energy_gradient_xxz: each bond's two-site operator applied by the matvec kernel at the
+    bond's orthogonality centre), checked by sum_i J_i dE/dJ_i = E and by central differences
+    (h = 1e-5) of DMRG energies restarted from the ground state at three bonds."""
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.dmrg import dmrg
+    from tnkit_gb300.grad import energy_gradient_xxz
+    from tnkit_gb300.mpo import to_block_mpo
+    N, chi, delta, h = 48, 512, 1.0, 1e-5
+    J = np.random.default_rng(2).uniform(0.5, 1.5, N - 1)
+
+    def run(Jv, init=None, sweeps=10):
+        Wb = to_block_mpo(workloads.xxz_disordered_mpo(Jv, delta), [[1, -1]] * N)[0]
+        kw = dict(charge=0) if init is None else dict(init_mps=init)
+        return dmrg(Wb, chi, seed=1, n_sweeps=sweeps, tol=1e-13, rtol=0, expand=0,
+                    eig_tol=1e-12, **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E, M, info = run(J)
+    torch.cuda.synchronize()
+    t_dmrg = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g = energy_gradient_xxz(M, delta)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    fd = {}
+    t0 = time.perf_counter()
+    for i in (0, N // 2 - 1, N - 2):
+        Jp, Jm = J.copy(), J.copy()
+        Jp[i] += h
+        Jm[i] -= h
+        ep = run(Jp, init=M, sweeps=4)[0]
+        em = run(Jm, init=M, sweeps=4)[0]
+        d = (ep - em) / (2 * h)
+        fd[str(i)] = {"fd": d, "hf": float(g[i]), "rel_err": abs(d - g[i]) / abs(g[i])}
+    t_fd = time.perf_counter() - t0
+    return {"workload": "disordered XXZ N=48, J_i uniform in [0.5, 1.5] (seed 2), Delta=1, "
+                        "U(1), chi=512; DMRG seed 1, tol 1e-13, eig_tol 1e-12; FP64",
+            "E": E, "sweeps": info["sweeps"], "dmrg_s": t_dmrg, "gradient_s": t_grad,
+            "gradient": [float(x) for x in g],
+            "sum_J_dE_dJ_minus_E": float(J @ g - E),
+            "central_differences": dict(fd, h=h, seconds=t_fd),
+            "max_rel_err_vs_central_differences": max(v["rel_err"] for k, v in fd.items())}
 
 
 if __name__ == "__main__":

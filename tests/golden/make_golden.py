@@ -29,6 +29,10 @@ Modes:
          reference's block MPO tensor of a bulk site, its seeded random block MPS, and the
          per-sweep energies of its block DMRG (N=6 chi=16, N=8 chi=32), with the exact ground
          energy of N=6 from the dense Hamiltonian.  -> hubbard_u1u1.npz, hubbard_u1u1.json
+  grad   Hellmann-Feynman coupling gradients of the disordered XXZ chain (N=10, J_i uniform in
+         [0.5, 1.5] from seed 2, delta=1) on complex U(1) blocks: the reference's ground state
+         and, per bond, its mpo_expectation of dH/dJ_i (the one-bond MPO), with central finite
+         differences of the reference's energies (h=1e-5) at three bonds.  -> grad_xxz10.json
   tdvp   Two-site TDVP of the XXZ N=10 chain on complex U(1) blocks from a seeded random state:
          the initial tensors, the reference's Krylov exponential on a fixed vector, and the
          state vector after 4 steps of dt=0.05.  -> tdvp_xxz10.npz, tdvp_xxz10.json
@@ -340,6 +344,43 @@ def mode_hubbard(ref):
         json.dump(meta, f, indent=1)
 
 
+def mode_grad(ref):
+    """dE/dJ_i by the reference's own observables (tnkit/dmrg_excited.py:185-211)."""
+    from tnkit import dmrg, get_backend, U1, to_block_mpo
+    from tnkit.block_backend import BlockBackend
+    from tnkit.dmrg_excited import mpo_expectation
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tnkit_gb300.workloads import xxz_disordered_mpo
+    N, chi, delta = 10, 32, 1.0
+    J = np.random.default_rng(2).uniform(0.5, 1.5, N - 1)
+    be = get_backend("numpy")
+    q = [[1, -1]] * N
+
+    def ground(Jv):
+        Wb, _ = to_block_mpo(xxz_disordered_mpo(Jv, delta), q, be, sym=U1())
+        return dmrg(Wb, chi, charge=0, seed=1, n_sweeps=8, tol=1e-14, rtol=0, expand=0,
+                    eig_tol=1e-12, backend=BlockBackend(be))
+    E, mps, info = ground(J)
+    grads = []
+    for i in range(N - 1):
+        e = np.zeros(N - 1)
+        e[i] = 1.0
+        Hb, _ = to_block_mpo(xxz_disordered_mpo(e, delta), q, be, sym=U1())
+        grads.append(complex(mpo_expectation(mps, Hb)).real)
+    h = 1e-5
+    fd = {}
+    for i in (0, 4, 8):
+        Jp, Jm = J.copy(), J.copy()
+        Jp[i] += h
+        Jm[i] -= h
+        fd[str(i)] = (float(ground(Jp)[0]) - float(ground(Jm)[0])) / (2 * h)
+    rec = {"N": N, "chi": chi, "delta": delta, "J": [float(x) for x in J], "E": float(E),
+           "hf_grad": grads, "fd_h": h, "fd_grad": fd, "backend": "numpy (complex128)"}
+    with open(os.path.join(HERE, "grad_xxz10.json"), "w") as f:
+        json.dump(rec, f, indent=1)
+    print("E", E, "grads", grads)
+
+
 def _dense_vector(mps):
     """The state vector of a block MPS with every leg in sector order (its flat amplitudes)."""
     v = np.ones((1,), complex)
@@ -390,7 +431,7 @@ def mode_tdvp(ref):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp", "hubbard"])
+    ap.add_argument("mode", choices=["small", "dmrg", "c2", "tdvp", "hubbard", "grad"])
     ap.add_argument("--ref", default=os.environ.get("TNKIT_REF"),
                     help="path of the reference tnkit checkout (or set TNKIT_REF)")
     a = ap.parse_args()
@@ -398,4 +439,4 @@ if __name__ == "__main__":
         ap.error("give the reference checkout with --ref or the TNKIT_REF environment variable")
     ref = _import_ref(a.ref)
     {"small": mode_small, "dmrg": mode_dmrg, "c2": mode_c2, "tdvp": mode_tdvp,
-     "hubbard": mode_hubbard}[a.mode](ref)
+     "hubbard": mode_hubbard, "grad": mode_grad}[a.mode](ref)

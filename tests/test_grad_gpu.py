@@ -1,7 +1,8 @@
 """Gradients through the kernels on the GPU: the autograd matvec against torch's numerical
 Jacobian, the local-energy gradient, and dE/dJ_i of the disordered XXZ chain by Hellmann-Feynman
-against exact diagonalisation and central finite differences of DMRG energies (h = 1e-4, the
-bar 1e-6 relative)."""
+against exact diagonalisation, the reference's own mpo_expectation of dH/dJ_i (tests/golden/
+grad_xxz10.json) and central finite differences of DMRG energies (h = 1e-5, the bar 1e-6
+relative)."""
 import itertools
 
 import numpy as np
@@ -156,3 +157,22 @@ def test_mps_energy_gradient_finite_differences(model):
             A.data[k] = x0
             fd = (Ep - Em) / (2 * h)
             assert abs(fd - float(g[i].data[k])) <= 1e-6 * max(1.0, abs(fd)), (i, k, fd)
+
+
+def test_hellmann_feynman_gradient_matches_reference_mpo_expectation():
+    """dE/dJ_i of the disordered XXZ chain (N=10, J from seed 2) against the reference's
+    mpo_expectation(psi, dH/dJ_i) on its own complex128 ground state (tnkit/dmrg_excited.py:
+    185-211), and the reference's central finite differences (h = 1e-5)."""
+    import json
+    import os
+    from conftest import GOLDEN
+    from tnkit_gb300.grad import energy_gradient_xxz
+    ref = json.load(open(os.path.join(GOLDEN, "grad_xxz10.json")))
+    J = np.asarray(ref["J"])
+    E, M, info = _dmrg_xxz(J, ref["delta"], chi=ref["chi"])
+    assert abs(E - ref["E"]) <= 1e-12 * abs(ref["E"])
+    g = energy_gradient_xxz(M, ref["delta"])
+    hf = np.asarray(ref["hf_grad"])
+    assert np.abs(g - hf).max() <= 1e-8 * np.abs(hf).max(), (g, hf)
+    for i, fd in ref["fd_grad"].items():
+        assert abs(g[int(i)] - fd) <= 1e-6 * abs(fd)

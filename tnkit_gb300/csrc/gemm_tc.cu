@@ -114,6 +114,32 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
         : "memory");
 }
 
+// Bounded parity wait that also gives up when the CTA's abort flag is raised by the other role.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parity,
+                                                   volatile int* abort_flag) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned i = 0; i < WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 255) == 255 && *abort_flag) return false;
+    }
+    return false;
+}
+
+// Warp roles: warp 0 lane 0 streams the operand tiles by TMA into the STAGES-deep ring (waiting
+// for the MMA issuer to release a slot before refilling it), warp 1 lane 0 issues the MMAs as
+// tiles land and releases each slot with tcgen05.commit, so loads run STAGES - 1 K steps ahead
+// of the tensor core without either thread waiting on its own work. After the last MMA all four
+// warps move the accumulator out: TMEM -> registers (32 columns per tcgen05.ld) -> a padded
+// shared-memory tile (the operand ring, idle by then) -> global memory row by row, 32
+// consecutive columns per store instruction.
 template <int PASSES>
 __global__ void __launch_bounds__(NT, 1)
 gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict__ segs,
@@ -121,6 +147,8 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                void* __restrict__ Cout, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     constexpr int NTILE = (PASSES == 3) ? 4 : 2;        // Ah, Bh (, Al, Bl) per stage
+    constexpr int LDS = BN + 1;                         // staging row stride (floats)
+    static_assert(BM * LDS * 4 <= STAGES * NTILE * TILE_BYTES, "staging tile fits the ring");
     uint8_t* base = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* stage_mem = base;
@@ -128,7 +156,8 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     uint64_t* empty = full + STAGES;
     uint64_t* done = empty + STAGES;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-    int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    int* counts = const_cast<int*>(abort_flag) + 1;     // [0] issued loads, [1] consumed
 
     const tnk_gemm_tile tile = tiles[blockIdx.x];
     const tnk_gemm_task task = tasks[tile.task];
@@ -148,6 +177,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
         }
         mbar_init(done, 1);
         *abort_flag = 0;
+        counts[0] = counts[1] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -160,9 +190,16 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     for (int s = task.seg_begin; s < task.seg_end; ++s) nk += (segs[s].k + BK - 1) / BK;
 
     if (threadIdx.x == 0 && nk > 0) {
-        // load cursor over (segment, k0)
+        // TMA producer: cursor over (segment, k0)
         int ls = task.seg_begin, lk = 0, issued = 0;
-        auto issue = [&](int slot) {
+        for (int i = 0; i < nk; ++i) {
+            const int slot = i % STAGES;
+            if (i >= STAGES &&
+                !mbar_wait_or_abort(&empty[slot], ((i / STAGES) - 1) & 1, abort_flag)) {
+                if (!*abort_flag) atomicExch(err, 2);
+                *abort_flag = 1;
+                break;
+            }
             while (lk >= segs[ls].k) { ++ls; lk = 0; }
             const TcSeg g = segs[ls];
             if (lk == 0) {
@@ -183,15 +220,18 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
             }
             lk += BK;
             ++issued;
-        };
-        for (int s = 0; s < STAGES && s < nk; ++s) issue(s);
-        bool ok = true;
+        }
+        counts[0] = issued;
+    } else if (threadIdx.x == 32 && nk > 0) {
+        // MMA issuer
         int consumed = 0;
         for (int i = 0; i < nk; ++i) {
             const int slot = i % STAGES;
-            const unsigned ph = (i / STAGES) & 1;
-            if (!mbar_wait(&full[slot], ph)) { ok = false; atomicExch(err, 1); break; }
-            consumed = i + 1;
+            if (!mbar_wait_or_abort(&full[slot], (i / STAGES) & 1, abort_flag)) {
+                if (!*abort_flag) atomicExch(err, 1);
+                *abort_flag = 1;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             uint8_t* st = stage_mem + slot * NTILE * TILE_BYTES;
 #pragma unroll
@@ -207,21 +247,18 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                 }
             }
             mma_commit(&empty[slot]);
-            if (issued < nk) {
-                if (!mbar_wait(&empty[slot], ph)) { ok = false; atomicExch(err, 2); break; }
-                issue(slot);
-            }
+            consumed = i + 1;
         }
-        if (!ok) {
-            *abort_flag = 1;
-            // drain: wait (bounded) for the TMA copies this CTA issued and did not consume, so
-            // none lands in shared memory after the CTA has exited
-            for (int j = consumed; j < issued; ++j)
-                mbar_wait(&full[j % STAGES], (j / STAGES) & 1);
-        }
+        counts[1] = consumed;
         mma_commit(done);       // arrives once every MMA issued above has completed
     }
     __syncthreads();
+    if (threadIdx.x == 0 && *abort_flag) {
+        // drain: wait (bounded) for the TMA copies issued and not consumed, so none lands in
+        // shared memory after the CTA has moved on or exited
+        for (int j = counts[1]; j < counts[0]; ++j)
+            mbar_wait(&full[j % STAGES], (j / STAGES) & 1);
+    }
     const bool have_acc = nk > 0;
     bool acc_ready = true;
     if (have_acc) acc_ready = mbar_wait(done, 0);
@@ -230,32 +267,45 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     // CTA-uniform: TMEM loads are .sync.aligned and must be issued by whole warps
     const int bad = __syncthreads_or((*abort_flag != 0) || !acc_ready);
 
-    // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes)
-    const int row = tile.m0 + warp * 32 + lane;
-    const bool f64 = (task.flags & 2) != 0;
-    const bool row_ok = !bad && row < task.m;
-    const int64_t rbase = task.c_off + (int64_t)row * task.ldc;
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-        uint32_t v[16];
+    // epilogue: warp w owns accumulator rows 32w..32w+31 (its TMEM lane quarter)
+    float* stg = reinterpret_cast<float*>(stage_mem);
+    const int rloc = warp * 32 + lane;
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t v[32];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0u;
+        for (int j = 0; j < 32; ++j) v[j] = 0u;
         if (have_acc && !bad) {
             const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
             asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
                   "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+                  "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+                  "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                  "=r"(v[30]), "=r"(v[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         }
-        if (row_ok) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = tile.n0 + c0 + j;
-                if (col < task.n) {
-                    const float x = __uint_as_float(v[j]);
+        for (int j = 0; j < 32; ++j) stg[rloc * LDS + c0 + j] = __uint_as_float(v[j]);
+    }
+    __syncwarp();
+    if (!bad) {
+        const bool f64 = (task.flags & 2) != 0;
+        const int rows = min(32, task.m - (tile.m0 + warp * 32));
+        const int cols = min(BN, task.n - tile.n0);
+        for (int r = 0; r < rows; ++r) {
+            const int row = tile.m0 + warp * 32 + r;
+            const int64_t rbase = task.c_off + (int64_t)row * task.ldc + tile.n0;
+            const float* src = stg + (warp * 32 + r) * LDS;
+#pragma unroll
+            for (int q = 0; q < BN / 32; ++q) {
+                const int col = q * 32 + lane;
+                if (col < cols) {
+                    const float x = src[col];
                     if (f64)
                         reinterpret_cast<double*>(Cout)[rbase + col] = (double)x;
                     else
@@ -275,6 +325,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
 
 constexpr size_t smem_bytes(int passes) {
     return 1024 + (size_t)STAGES * ((passes == 3) ? 4 : 2) * TILE_BYTES + 256;
+    // (1024: alignment slack of the ring; 256: barriers, TMEM slot, abort flag, counters)
 }
 
 }  // namespace
