@@ -295,6 +295,51 @@ def main():
         t_g3 += e[2].elapsed_time(e[3]) / 1e3
     t_g1, t_c2, t_g3 = t_g1 / nrep, t_c2 / nrep, t_g3 / nrep
 
+    # --- the other inner product of the FP64 grouped GEMM (tnk_gemm_f64_variant), same
+    # problem, same timing: the default variant is the headline above ---
+    var0 = lib.tnk_gemm_f64_variant(-1)
+    var1 = 1 - var0
+    lib.tnk_gemm_f64_variant(var1)
+    y_alt = torch.empty_like(x)
+    for _ in range(3):
+        op(x, y_alt)
+    torch.cuda.synchronize()
+    t_alt = 0.0
+    t_alt_g = 0.0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        op(x, y_alt)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t_alt += a.elapsed_time(b) / 1e3
+    for i in range(nrep):
+        flush.fill_(float(i))
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_f64(cplan.t1, cplan.s1, cplan.tiles1, cplan.n_tiles1,
+                                            L.data.data_ptr(), x.data_ptr(), R.data.data_ptr(),
+                                            ws.data_ptr(), ws.data_ptr(), sp), "gemm1")
+        e[1].record(stream)
+        _lib.check(lib.tnk_combine_f64(cplan.t2, cplan.c2, cplan.items2, cplan.n_items2,
+                                       ws.data_ptr(), ws.data_ptr(), sp), "comb")
+        e[2].record(stream)
+        _lib.check(lib.tnk_grouped_gemm_f64(cplan.t3, cplan.s3, cplan.tiles3, cplan.n_tiles3,
+                                            L.data.data_ptr(), x.data_ptr(), R.data.data_ptr(),
+                                            ws.data_ptr(), y_alt.data_ptr(), sp), "gemm3")
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        t_alt_g += (e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])) / 1e3
+    t_alt_g /= nrep
+    lib.tnk_gemm_f64_variant(var0)
+    op(x, y_alt)                          # the result of the alternative, checked below
+    lib.tnk_gemm_f64_variant(var1)
+    op(x, y_alt)
+    lib.tnk_gemm_f64_variant(var0)
+    torch.cuda.synchronize()
+    alt_err = float((y_alt - y).abs().max() / y.abs().max())
+
     # --- end to end through the C ABI: pinned host theta in, pinned host result out ---
     h_in = torch.empty(x.numel(), dtype=torch.float64, pin_memory=True)
     h_in.copy_(x.cpu())
@@ -372,6 +417,20 @@ def main():
                     "d2h_bytes_per_step": x.numel() * 8, "max_rel_err_vs_device": err_e2e},
             "gpu_launches": per_step * args.steps,
             "clocks": clocks}
+    names = {0: "fp64 FMA tile (4 x 4 per thread)", 1: "DMMA tile (mma.sync m8n8k4 f64)"}
+    line["fp64_variants"] = {
+        "headline": names[var0],
+        "headline_gemm_ms": t_gemm * 1e3,
+        "headline_executed_tflops": 2 * hp.macs / t_gemm / 1e12,
+        "other": names[var1],
+        "other_ms_per_step": t_alt / args.steps * 1e3,
+        "other_value": flops_ref * args.steps / t_alt / 1e9,
+        "other_gemm_ms": t_alt_g * 1e3,
+        "other_credited_tflops": gemm_flops / t_alt_g / 1e12,
+        "other_executed_tflops": 2 * hp.macs / t_alt_g / 1e12,
+        "other_max_rel_diff": alt_err,
+        "note": "executed = the FLOPs the plan runs (skipped unused intermediate blocks "
+                "excluded); credited = the reference's algorithmic FLOPs of the two GEMM stages"}
     line["mixed"] = mixed_leg(torch, dev, th, L, W1, W2, R, y, flush, flops_ref, parts,
                               args.steps, ms)
     line["float_float"] = ff_leg(torch, th, L, W1, W2, R, y, flush, flops_ref, parts,
@@ -506,9 +565,10 @@ def batch_leg(torch, dev, flush, steps):
     singles = [ops.TwoSiteOperator(th, L, W1, W2, R) for th, L, W1, W2, R in probs]
     op = B.BatchedTwoSiteOperator(probs)
     opf = B.BatchedTwoSiteOperator(probs, precision="ff")
+    opt = B.BatchedTwoSiteOperator(probs, precision="tc")
     flops = 2 * op.ref_macs
     x = torch.randn(op.n, dtype=torch.float64, device=dev)
-    y, yf, yg = (torch.empty_like(x) for _ in range(3))
+    y, yf, yg, yt = (torch.empty_like(x) for _ in range(4))
     xs, ys = op.split(x), [torch.empty_like(v) for v in op.split(x)]
     stream = torch.cuda.current_stream()
 
@@ -519,7 +579,9 @@ def batch_leg(torch, dev, flush, steps):
         run_seq()
         op(x, y)
         opf(x, yf)
+        opt(x, yt)
     torch.cuda.synchronize()
+    opt.tc.check_device_error()
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph):
         op(x, yg)
@@ -529,6 +591,7 @@ def batch_leg(torch, dev, flush, steps):
     err = float((y - ref).abs().max() / ref.abs().max())
     errf = float((yf - ref).abs().max() / ref.abs().max())
     errg = float((yg - y).abs().max())
+    errt = float((yt - ref).abs().max() / ref.abs().max())
 
     def timed(fn):
         t = 0.0
@@ -546,6 +609,7 @@ def batch_leg(torch, dev, flush, steps):
     bat = timed(lambda: op(x, y))
     gra = timed(graph.replay)
     bff = timed(lambda: opf(x, yf))
+    btc = timed(lambda: opt(x, yt))
     draws = B.chain_draws(64, 2)
 
     def launches(hp):      # stages with work (an empty stage launches nothing)
@@ -562,7 +626,10 @@ def batch_leg(torch, dev, flush, steps):
                                 bat["ms_per_step"], max_rel_err_vs_sequential=err),
             "graph_f64": dict(gra, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
                               gra["ms_per_step"], max_abs_diff_vs_batched=errg),
-            "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf)}
+            "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf),
+            "batched_tc": dict(btc, launches=4, max_rel_err_vs_sequential_f64=errt,
+                               note="split-TF32 tcgen05 grouped GEMMs of the same batched plan "
+                                    "(theta staging, two GEMM stages, FP32 combination)")}
 
 
 def batch_dmrg_leg(torch, args):
@@ -592,7 +659,7 @@ def batch_dmrg_leg(torch, args):
                        f"first {half} U(1) XXZ chains of the 64-chain seed-2 draws), "
                        f"{args.batch_sweeps} sweeps each, seeds 0..{len(sel) - 1}",
            "chains": [list(d) for d in sel]}
-    for prec in ("f64", "ff"):
+    for prec in ("f64", "ff", "mixed"):
         t0 = time.perf_counter()
         Eb, _, info = dmrg_batch([mk(m, g, N) for m, g, N, _ in sel],
                                  [chi for *_, chi in sel],
@@ -602,6 +669,7 @@ def batch_dmrg_leg(torch, args):
         torch.cuda.synchronize()
         out[f"batched_{prec}"] = {"s": time.perf_counter() - t0, "phase_time": info["phase_time"],
                                   "rounds": info["rounds"], "batched_iterations": info["matvecs"],
+                                  "batched_iterations_tc": info["matvecs_lo"],
                                   "pipeline": info["pipeline"], "E": Eb}
     t0 = time.perf_counter()
     Es, ph = [], {"eig": 0.0, "trunc": 0.0, "env": 0.0}
@@ -613,7 +681,7 @@ def batch_dmrg_leg(torch, args):
             ph[k] += inf["phase_time"][k]
     torch.cuda.synchronize()
     out["sequential_f64"] = {"s": time.perf_counter() - t0, "phase_time": ph, "E": Es}
-    for prec in ("f64", "ff"):
+    for prec in ("f64", "ff", "mixed"):
         b = out[f"batched_{prec}"]
         b["speedup_vs_sequential_f64"] = out["sequential_f64"]["s"] / b["s"]
         b["max_abs_dE_vs_sequential"] = float(np.max(np.abs(np.array(b["E"]) - np.array(Es))))

@@ -186,6 +186,13 @@ int tnk_grouped_gemm_ff(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
                         const double* b1, const double* b2, const double* b3, double* C,
                         void* stream);
 
+/* The inner product of the FP64 grouped GEMM kernel behind every FP64 entry point, process-wide:
+ * 0 = per-thread FP64 FMAs (4 x 4 register tile), 1 = FP64 tensor MMAs (mma.sync m8n8k4,
+ * 8 x 8 tiles per warp instruction). Same tables, loaders and results (to rounding). Any other
+ * value leaves the setting unchanged. Returns the previous setting. No counterpart in the
+ * reference (it calls cuBLAS through torch). */
+int tnk_gemm_f64_variant(int32_t variant);
+
 /* One grouped GEMM stage on its own (a two-operand block contraction, e.g. theta = M_i M_i+1,
  * tnkit/blocks.py:1156-1192 tensordot). Slots 0..3 = b0..b3; C is the output base. */
 int tnk_grouped_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
@@ -297,6 +304,26 @@ int tnk_gemv_sub_f64(const double* V, int64_t ldv, int32_t nv, const double* c, 
 int tnk_cgs_pass_f64(const double* V, int64_t ldv, int32_t nv, const double* cin, double* w,
                      int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
                      void* stream);
+/* The same pass over many independent vectors concatenated in one batch vector (the chains of
+ * a batched Lanczos): chain c occupies [off[c], off[c+1]) of w and of every basis row (ldv = the
+ * batch length); the chains ids[0..nseg) are processed in one launch, each with its own
+ * coefficients cin + c*rec_stride, output out + c*rec_stride and completion counter counter[y]
+ * (y = its position in ids; zero before the call, left zero). max_len >= the longest listed
+ * segment; nseg * 66 <= TNK_RED_ELEMS (66 partial doubles per CTA). off and ids are device arrays. No
+ * reduction mixes chains: each chain's results equal tnk_cgs_pass_f64 on its segment up to the
+ * order of its partial sums. Replaces the per-chain passes of a batched solve (the reference
+ * runs one chain per call, its CGS2 at tnkit/eigensolver.py:567-599). */
+int tnk_cgs_pass_seg_f64(const double* V, int64_t ldv, int32_t nv, const double* cin, double* w,
+                         const int64_t* off, const int32_t* ids, int32_t nseg, int64_t max_len,
+                         int64_t rec_stride, double* out, int32_t mode, double* red,
+                         uint32_t* counter, void* stream);
+/* y_c = x_c * (f / s[c * s_stride]) on the segments [off[c], off[c+1]) of the chains
+ * ids[0..nseg) (device arrays), max_len >= the longest: the per-chain normalisation of a
+ * batched Lanczos step in one launch (the reference: one chain's `w / beta`,
+ * tnkit/eigensolver.py:600-604). */
+int tnk_scale_div_seg_f64(const double* x, double* y, const int64_t* off, const int32_t* ids,
+                          int32_t nseg, int64_t max_len, const double* s, int64_t s_stride,
+                          double f, void* stream);
 /* The same pass on FP32 vectors (FP32 arithmetic; coefficients and results in double): the
  * Krylov basis of the tensor-core stage of the mixed-precision solve, whose operator is only
  * ~1e-6 accurate, is kept in FP32. */

@@ -37,6 +37,32 @@ def test_batched_tables_match_each_problem():
         assert _rel(got[starts[k, 1]:starts[k + 1, 1]], want) <= 1e-13
 
 
+def test_batched_tensor_core_relayout_matches_each_problem():
+    """The tensor-core re-layout of a batched plan (staged K-major FP32 blocks of every
+    problem's operands in one buffer), interpreted with emulated split TF32, gives each
+    problem's own FP64 matvec to split-TF32 accuracy."""
+    from table_interp import run_tc_plan
+    specs = [("tfim", 0.7, 16, 16), ("xxz", 0.3, 16, 32), ("xxz", 1.0, 24, 24)]
+    probs = [B.chain_problem(*s, seed=90 + k, device="cpu") for k, s in enumerate(specs)]
+    plans = [P.plan_apply(th, L.layout, [(W1.layout, _host_of(W1)), (W2.layout, _host_of(W2))],
+                          R.layout) for th, L, W1, W2, R in probs]
+    sizes = np.array([[L.host.size, th.size, R.host.size, hp.ws1 + hp.ws2_unsplit]
+                      for (th, L, _, _, R), hp in zip(probs, plans)], np.int64)
+    starts = np.vstack([np.zeros(4, np.int64), np.cumsum(sizes, 0)])
+    hb = B.batch_plan(plans, [tuple(int(v) for v in starts[k]) for k in range(len(plans))],
+                      [int(starts[k, 1]) for k in range(len(plans))], int(starts[-1, 3]),
+                      int(starts[-1, 1]))
+    tc = P.HostPlanTC(hb, None, None, None)
+    rng = np.random.default_rng(4)
+    thetas = [rng.standard_normal(th.size) for th, *_ in probs]
+    Lcat = np.concatenate([p[1].host for p in probs])
+    Rcat = np.concatenate([p[4].host for p in probs])
+    got = run_tc_plan(tc, Lcat, np.concatenate(thetas), Rcat, passes=3)
+    for k, ((th, L, W1, W2, R), hp) in enumerate(zip(probs, plans)):
+        want = run_plan3(hp, L.host, thetas[k], R.host)
+        assert _rel(got[starts[k, 1]:starts[k + 1, 1]], want) <= 2e-5
+
+
 def test_chain_draws_reproducible():
     d = B.chain_draws(64, 2)
     assert d == B.chain_draws(64, 2) and len(d) == 64

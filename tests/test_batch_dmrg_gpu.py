@@ -23,7 +23,10 @@ def _built():
     build.build()
 
 
-def test_batched_lanczos_matches_eigvalsh():
+@pytest.mark.parametrize("segmented", [True, False])
+def test_batched_lanczos_matches_eigvalsh(segmented):
+    """Every chain's lowest eigenpair, with the Gram-Schmidt passes and normalisations as one
+    segmented launch for all chains (tnk_cgs_pass_seg_f64) or one launch per chain."""
     from tnkit_gb300.batch_dmrg import lanczos_ground_batched
     rng = np.random.default_rng(5)
     sizes = [1, 3, 7, 40, 120, 300, 55]
@@ -39,7 +42,8 @@ def test_batched_lanczos_matches_eigvalsh():
             torch.mv(H, x[a:b], out=out[a:b])
         return out
     x0 = torch.as_tensor(rng.standard_normal(off[-1]), device="cuda")
-    E, X, info = lanczos_ground_batched(op, x0, off, tol=1e-10, max_iter=600, m=30, k=8)
+    E, X, info = lanczos_ground_batched(op, x0, off, tol=1e-10, max_iter=600, m=30, k=8,
+                                        segmented=segmented)
     assert info["converged"].all() and info["restarts"] > 0
     for H, e, a, b in zip(Hs, E, off[:-1], off[1:]):
         ev, evec = np.linalg.eigh(H)
@@ -49,7 +53,8 @@ def test_batched_lanczos_matches_eigvalsh():
         assert abs(abs(x @ evec[:, 0]) - 1.0) <= 1e-8
 
 
-@pytest.mark.parametrize("precision,pipeline", [("f64", True), ("ff", True), ("f64", False)])
+@pytest.mark.parametrize("precision,pipeline", [("f64", True), ("ff", True), ("f64", False),
+                                                ("mixed", False)])
 def test_dmrg_batch_matches_independent_runs(precision, pipeline):
     from tnkit_gb300 import workloads
     from tnkit_gb300.batch_dmrg import dmrg_batch
@@ -75,3 +80,37 @@ def test_dmrg_batch_matches_independent_runs(precision, pipeline):
         assert abs(e - E1) <= 1e-10 * abs(E1), (m, N, e, E1)
     ref = json.load(open(os.path.join(GOLDEN, "dmrg_small.json")))["c1_tfim_n10_chi32"]
     assert abs(Eb[0] - ref["free_fermion"]) <= 1e-11 * abs(ref["free_fermion"])
+
+
+def test_segmented_passes_equal_per_chain_passes():
+    """One segmented launch per Gram-Schmidt pass gives each chain the per-chain pass's
+    coefficients and vector (only the order of partial sums differs: 1e-14)."""
+    from tnkit_gb300.batch_dmrg import _Segments, _MAXNV
+    rng = np.random.default_rng(8)
+    sizes = [5, 1000, 129, 40000, 7, 3000]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    n = int(off[-1])
+    nv = 9
+    V = torch.as_tensor(rng.standard_normal((nv, n)), device="cuda")
+    w0 = torch.as_tensor(rng.standard_normal(n), device="cuda")
+    act = [0, 1, 3, 5]
+    A = _Segments(off, n, torch.device("cuda"), segmented=True)
+    B = _Segments(off, n, torch.device("cuda"), segmented=False)
+    wa, wb = w0.clone(), w0.clone()
+    A.cgs2_all(V, nv, wa, act)
+    for c in act:
+        B.cgs2(V, nv, wb, c)
+    ra, rb = A.read().copy(), B.read().copy()
+    for c in act:
+        a, b = off[c], off[c + 1]
+        assert np.allclose(ra[c, :1 + 2 * _MAXNV], rb[c, :1 + 2 * _MAXNV], rtol=1e-13,
+                           atol=1e-13 * np.abs(rb[c]).max())
+        assert torch.allclose(wa[a:b], wb[a:b], rtol=0, atol=1e-13 * float(wb[a:b].abs().max()))
+    for c in (2, 4):                     # chains not listed are untouched
+        a, b = off[c], off[c + 1]
+        assert torch.equal(wa[a:b], w0[a:b])
+    ya, yb = torch.zeros_like(w0), torch.zeros_like(w0)
+    A.scale_div_all(wa, ya, act)
+    for c in act:
+        B.scale_div(wb, yb, c)
+    assert torch.allclose(ya, yb, rtol=1e-13, atol=0)

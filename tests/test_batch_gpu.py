@@ -1,7 +1,8 @@
 """The batched operator (tnkit_gb300.batch.BatchedTwoSiteOperator) on the GPU: one set of
 launches for many chains' local problems gives each problem's own FP64 matvec (only the split-K
-summation order differs), the float-float variant stays within FP64-grade accuracy, and a CUDA
-graph capture of the batched call replays it exactly."""
+summation order differs), the float-float variant stays within FP64-grade accuracy, the
+tensor-core variant (split TF32) within 2e-5, and a CUDA graph capture of the batched call
+replays it exactly."""
 import numpy as np
 import pytest
 
@@ -28,12 +29,14 @@ def _rel(a, b):
     return float((a - b).abs().max() / b.abs().max())
 
 
-@pytest.mark.parametrize("precision,tol", [("f64", 1e-13), ("ff", 1e-12)])
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-13), ("ff", 1e-12), ("tc", 2e-5)])
 def test_batched_matches_each_problem(problems, precision, tol):
     from tnkit_gb300 import batch as B, ops
     op = B.BatchedTwoSiteOperator(problems, precision=precision)
     x = torch.randn(op.n, dtype=torch.float64, device="cuda")
     y = op(x)
+    if op.tc is not None:
+        op.tc.check_device_error()
     for xk, yk, (th, L, W1, W2, R) in zip(op.split(x), op.split(y), problems):
         ref = ops.TwoSiteOperator(th, L, W1, W2, R)(xk.contiguous())
         assert _rel(yk, ref) <= tol

@@ -107,3 +107,20 @@ def test_chi1024_mid_bond_properties():
     assert float((lhs - rhs).abs().max() / rhs.abs().max()) <= 1e-13
     got = op(x).cpu().numpy()
     assert _rel(got, _oracle_two_site(th, L, W1, W2, R)) <= TOL
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_two_site_matches_oracle_with_either_fp64_inner_product(variant):
+    """The FP64 grouped GEMM's FMA tile (0) and its DMMA tile (mma.sync m8n8k4, 1) give the
+    oracle's matvec at a chi=256-like bond and the reference's golden two-site result."""
+    from tnkit_gb300 import _lib, ops, workloads
+    lib = _lib.lib()
+    prev = lib.tnk_gemm_f64_variant(variant)
+    try:
+        th, L, W1, W2, R = workloads.mid_bond_problem(dims=(3, 24, 61, 80, 61, 24, 3),
+                                                      charges=(-6, -4, -2, 0, 2, 4, 6), seed=9)
+        got = ops.apply_two_site(th, L, W1, W2, R).data.cpu().numpy()
+        ref = _oracle_two_site(th, L, W1, W2, R)
+        assert _rel(got, ref) <= TOL
+    finally:
+        lib.tnk_gemm_f64_variant(prev)

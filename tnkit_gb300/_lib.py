@@ -113,6 +113,9 @@ _SIGS = {
     "tnk_scale_div_f64": ([_P, _P, _I64, _P, _D, _P], C.c_int),
     "tnk_cgs_pass_f64": ([_P, _I64, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P], C.c_int),
     "tnk_cgs_pass_f32": ([_P, _I64, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P], C.c_int),
+    "tnk_scale_div_seg_f64": ([_P, _P, _P, _P, _I32, _I64, _P, _I64, _D, _P], C.c_int),
+    "tnk_cgs_pass_seg_f64": ([_P, _I64, _I32, _P, _P, _P, _P, _I32, _I64, _I64, _P, _I32, _P,
+                              _P, _P], C.c_int),
     "tnk_scale_div_f32": ([_P, _P, _I64, _P, _D, _P], C.c_int),
     "tnk_rotate_f32": ([_P, _I64, _I32, _P, _I32, _P, _I64, _I64, _P], C.c_int),
     "tnk_svd_gram_ws_f64": ([_I64, _I64, _P], C.c_int),
@@ -136,6 +139,7 @@ _SIGS = {
     "tnk_zmultidot_f64": ([_P, _I64, _I32, _P, _I64, _P, _P, _P], C.c_int),
     "tnk_zgemv_sub_f64": ([_P, _I64, _I32, _P, _P, _I64, _P], C.c_int),
     "tnk_zaxpby_f64": ([_P, _P, _I64, _P, _D, _P, _D, _P], C.c_int),
+    "tnk_gemm_f64_variant": ([_I32], C.c_int),
     "tnk_tridiag_eig_f64": ([_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P], C.c_int),
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),

@@ -95,11 +95,13 @@ class BatchedTwoSiteOperator:
     """H_eff of K independent local problems (theta_layout, L, W1, W2, R) as one operator on the
     concatenation of their theta vectors: `op(x, out)` with x[offsets[k]:offsets[k+1]] problem
     k's theta. The environments are copied once into arena buffers; every call is one launch per
-    stage for the whole batch. precision 'f64' (FP64 grouped GEMM) or 'ff' (float-float)."""
+    stage for the whole batch. precision 'f64' (FP64 grouped GEMM), 'ff' (float-float) or 'tc'
+    (the tensor-core split-TF32 operator of the same batched plan: operands staged once in FP32,
+    one tcgen05 grouped-GEMM launch per GEMM stage for all problems; ~1e-6 relative)."""
 
     def __init__(self, problems: Sequence[Problem], precision: str = "f64"):
-        if precision not in ("f64", "ff"):
-            raise ValueError("precision must be 'f64' or 'ff'")
+        if precision not in ("f64", "ff", "tc"):
+            raise ValueError("precision must be 'f64', 'ff' or 'tc'")
         if not problems:
             raise ValueError("no problems")
         dev = problems[0][1].data.device
@@ -119,6 +121,7 @@ class BatchedTwoSiteOperator:
                         self.n)
         self.host = hp
         self.plan = ops.DevicePlan3(hp, dev, ff=precision == "ff")
+        self.tc = None
         self.K = len(plans)
         self._owners(plans, starts)
         self.active = np.ones(self.K, bool)
@@ -130,8 +133,11 @@ class BatchedTwoSiteOperator:
         self.R = torch.cat([p[4].data.reshape(-1) for p in problems])
         need = self.plan.ws_elems + (self.plan.out_elems if precision == "ff" else 0)
         self.ws = torch.empty(max(need, 1), dtype=torch.float64, device=dev)
-        self.fn = ops._APPLY2[precision]
+        self.fn = ops._APPLY2["f64" if precision == "tc" else precision]
         self.Lx, self.Rx = self.L, self.R
+        if precision == "tc":
+            from .mixed import TwoSiteOperatorTC
+            self.tc = TwoSiteOperatorTC.from_host_plan(hp, self.L, self.R, self.n)
         if precision == "ff":        # float-float copies of the arenas, split once
             lib, sp = _lib.lib(), _lib.stream_ptr()
             self.Lx, self.Rx = torch.empty_like(self.L), torch.empty_like(self.R)
@@ -164,6 +170,8 @@ class BatchedTwoSiteOperator:
         and combination items) of the others are dropped; tables and buffers stay. A skipped
         problem's part of the output is left as it was."""
         mask = np.asarray(mask, bool)
+        if self.tc is not None:
+            raise NotImplementedError("set_active is not available on the tensor-core batch")
         if mask.shape != (self.K,):
             raise ValueError(f"need one flag per problem ({self.K})")
         if np.array_equal(mask, self.active):
@@ -185,7 +193,10 @@ class BatchedTwoSiteOperator:
         if x.numel() != self.n:
             raise ValueError(f"batch vector of {x.numel()} entries, operator takes {self.n}")
         y = torch.empty_like(x) if out is None else out
-        self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+        if self.tc is not None:
+            self.tc(x, y)
+        else:
+            self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
         self.calls += 1
         return y
 

@@ -37,18 +37,61 @@ _SUB, _DOT, _NRM = 1, 2, 4
 
 
 class _Segments:
-    """Per-chain launches of the Lanczos vector kernels on segments of a batch vector."""
+    """The Lanczos vector kernels on the chains' segments of a batch vector: per chain
+    (`cgs2`, `nrm2`, `scale_div`: one launch per chain each) or, with `segmented`, every listed
+    chain in one launch per pass (`cgs2_all`, `nrm2_all`, `scale_div_all`:
+    tnk_cgs_pass_seg_f64 / tnk_scale_div_seg_f64, grid rows = chains)."""
 
-    def __init__(self, offsets: Sequence[int], n: int, device):
+    def __init__(self, offsets: Sequence[int], n: int, device, segmented: bool = True):
         self.off = [int(x) for x in offsets]
         self.K = len(self.off) - 1
         self.n = int(n)
         self.lib = _lib.lib()
         self.sp = _lib.stream_ptr()
         self.red = torch.empty(_lib.TNK_RED_ELEMS, dtype=torch.float64, device=device)
-        self.cnt = torch.zeros(4, dtype=torch.int32, device=device)
+        self.cnt = torch.zeros(max(4, self.K), dtype=torch.int32, device=device)
         self.rec = torch.zeros((self.K, _REC), dtype=torch.float64, device=device)
         self.hrec = torch.zeros((self.K, _REC), dtype=torch.float64, pin_memory=True)
+        self.segmented = segmented
+        self.off_dev = torch.as_tensor(np.asarray(self.off, np.int64), device=device)
+        self.lens = np.diff(np.asarray(self.off, np.int64))
+        self._ids_key, self._ids = None, None
+        self.device = device
+
+    def ids(self, act):
+        """Device int32 list of the chains `act` (uploaded when the set changes)."""
+        key = tuple(int(c) for c in act)
+        if key != self._ids_key:
+            self._ids = torch.as_tensor(np.asarray(key, np.int32), device=self.device)
+            self._ids_key = key
+        return self._ids
+
+    def _seg_pass(self, V, nv, w, act, cin_slot, out_slot, mode):
+        ids = self.ids(act)
+        rec = self.rec.data_ptr()
+        cin = None if cin_slot is None else rec + 8 * cin_slot
+        _lib.check(self.lib.tnk_cgs_pass_seg_f64(
+            None if V is None else V.data_ptr(), self.n, nv, cin, w.data_ptr(),
+            self.off_dev.data_ptr(), ids.data_ptr(), len(act), int(self.lens[list(act)].max()),
+            _REC, rec + 8 * out_slot, mode, self.red.data_ptr(), self.cnt.data_ptr(), self.sp),
+            "cgs_pass_seg")
+
+    def cgs2_all(self, V, nv, w, act):
+        """cgs2 of every chain in `act`, three launches in all."""
+        self._seg_pass(V, nv, w, act, None, 1, _DOT)
+        self._seg_pass(V, nv, w, act, 1, 1 + _MAXNV, _SUB | _DOT)
+        self._seg_pass(V, nv, w, act, 1 + _MAXNV, 0, _SUB | _NRM)
+
+    def nrm2_all(self, x, act):
+        self._seg_pass(None, 0, x, act, None, 0, _NRM)
+
+    def scale_div_all(self, x, y, act):
+        """y_c = x_c / beta_c for every chain in `act`, one launch."""
+        ids = self.ids(act)
+        _lib.check(self.lib.tnk_scale_div_seg_f64(
+            x.data_ptr(), y.data_ptr(), self.off_dev.data_ptr(), ids.data_ptr(), len(act),
+            int(self.lens[list(act)].max()), self.rec.data_ptr(), _REC, 1.0, self.sp),
+            "scale_div_seg")
 
     def seg(self, k):
         k = int(k)
@@ -89,15 +132,18 @@ class _Segments:
 
 
 def lanczos_ground_batched(op, x0: torch.Tensor, offsets: Sequence[int], tol: float = 1e-9,
-                           max_iter: int = 200, m: int = 40, k: int = 10):
+                           max_iter: int = 200, m: int = 40, k: int = 10,
+                           segmented: bool = True):
     """Lowest eigenpair of each of K symmetric operators applied together by `op(x, out)` on
     the concatenation of their vectors (chain c at [offsets[c], offsets[c+1])), from the start
-    x0. Returns (E (K,), X (the K unit Ritz vectors, concatenated), info)."""
+    x0. With `segmented` every Gram-Schmidt pass and normalisation is one launch for all active
+    chains, else one launch per chain. Returns (E (K,), X (the K unit Ritz vectors,
+    concatenated), info)."""
     if m + 1 > _MAXNV or m < 2 or not 0 < k < m:
         raise ValueError(f"need 0 < k < m <= {_MAXNV - 1}")
     dev = x0.device
     n = x0.numel()
-    S = _Segments(offsets, n, dev)
+    S = _Segments(offsets, n, dev, segmented)
     K = S.K
     Vb = torch.empty((m + 1, n), dtype=torch.float64, device=dev)
     w = torch.empty(n, dtype=torch.float64, device=dev)
@@ -105,19 +151,29 @@ def lanczos_ground_batched(op, x0: torch.Tensor, offsets: Sequence[int], tol: fl
     E = np.full(K, np.nan)
     iters = np.zeros(K, np.int64)
     conv = np.zeros(K, bool)
-    for c in range(K):
-        S.nrm2(x0, c)
+    if segmented:
+        S.nrm2_all(x0, list(range(K)))
+    else:
+        for c in range(K):
+            S.nrm2(x0, c)
     nrm0 = S.read()[:, 0].copy()
     active = np.isfinite(nrm0) & (nrm0 > 1e-300)
-    for c in np.nonzero(active)[0]:
-        S.scale_div(x0, Vb[0], c)
+    if segmented:
+        if active.any():
+            S.scale_div_all(x0, Vb[0], np.nonzero(active)[0])
+    else:
+        for c in np.nonzero(active)[0]:
+            S.scale_div(x0, Vb[0], c)
     T = np.zeros((K, m + 1, m + 1))
     j, it, restarts = 0, 0, 0
     while active.any():
         op(Vb[j], w)
         act = np.nonzero(active)[0]
-        for c in act:
-            S.cgs2(Vb, j + 1, w, c)
+        if segmented:
+            S.cgs2_all(Vb, j + 1, w, act)
+        else:
+            for c in act:
+                S.cgs2(Vb, j + 1, w, c)
         h = S.read()
         alpha, beta = h[:, 1 + j].copy(), h[:, 0].copy()
         T[act, j, j] = alpha[act]
@@ -158,14 +214,20 @@ def lanczos_ground_batched(op, x0: torch.Tensor, offsets: Sequence[int], tol: fl
                 T[c, np.arange(kk), np.arange(kk)] = ev[q, :kk]
                 T[c, :kk, kk] = border
                 T[c, kk, :kk] = border
-                S.scale_div(w, Vb[kk], c)
+                if not segmented:
+                    S.scale_div(w, Vb[kk], c)
+            if segmented:
+                S.scale_div_all(w, Vb[kk], act[keep])
             j = kk
             restarts += 1
         else:
             for q in keep:
                 c = act[q]
                 T[c, j, j + 1] = T[c, j + 1, j] = beta[c]
-                S.scale_div(w, Vb[j + 1], c)
+                if not segmented:
+                    S.scale_div(w, Vb[j + 1], c)
+            if segmented:
+                S.scale_div_all(w, Vb[j + 1], act[keep])
             j += 1
     torch.cuda.current_stream().synchronize()
     return E, X, {"iters": iters, "converged": conv, "restarts": restarts, "matvecs": it}
@@ -179,8 +241,9 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
     chain that has one (a sweep is N-1 bonds left to right, then N-1 right to left), all local
     problems in one batched Lanczos on one batched plan; truncation and the environment update
     stay per chain. Options as `dmrg` (n_sweeps, eig_tol, restart_m, restart_k, max_iter,
-    svd_method, svd_driver, device; precision 'f64' or 'ff' for the batched matvec; no
-    convergence stop: every chain runs n_sweeps). With `pipeline` the chains run as two groups
+    svd_method, svd_driver, device; precision 'f64' or 'ff' for the batched matvec, or 'mixed' /
+    'mixed-ff': each round's problems first solved together on the tensor cores to mixed_tol_lo,
+    then polished in FP64 / float-float; no convergence stop: every chain runs n_sweeps). With `pipeline` the chains run as two groups
     whose eigensolver and truncation phases overlap (the results are the same; measured on
     GB300 it gains ~3 %: both phases need the FP64 units and the host cores). Returns
     (energies, MPSs, info) with each chain's final energy, MPS and per-sweep energies."""
@@ -188,8 +251,8 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
     K = len(mpos)
     if len(chis) != K:
         raise ValueError("one bond dimension per chain")
-    if o.precision not in ("f64", "ff"):
-        raise ValueError("the batched matvec runs precision 'f64' or 'ff'")
+    if o.precision not in ("f64", "ff", "mixed", "mixed-ff"):
+        raise ValueError("the batched solve runs precision 'f64', 'ff', 'mixed' or 'mixed-ff'")
     if o.sites != 2 or (o.expand not in (None, 0)) or o.trunc != "svd":
         raise NotImplementedError("batched DMRG is two-site, expand=0, trunc='svd'")
     charges = list(charges) if charges is not None else [None] * K
@@ -208,7 +271,7 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
                        "disc": 0.0})
     rounds = max(len(ch["sched"]) for ch in chains)
     phase = {"eig": 0.0, "trunc": 0.0, "env": 0.0}
-    stats = {"matvecs": 0}
+    stats = {"matvecs": 0, "matvecs_lo": 0}
     E_last = np.full(K, np.nan)
     main = torch.cuda.current_stream(device)
 
@@ -223,10 +286,20 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
             th = ops.tensordot(ch["M"][i], ch["M"][i + 1], 1)
             thetas.append(th)
             probs.append((th.layout, ch["L"][i], ch["W"][i], ch["W"][i + 1], ch["R"][i + 2]))
-        op = BatchedTwoSiteOperator(probs, precision=o.precision)
         x0 = torch.cat([t.data for t in thetas])
         mi = o.max_iter if o.max_iter is not None else max(
             min(t.layout.size, max(200, 4 * chains[c]["chi"])) for c, t in zip(act, thetas))
+        hi = "ff" if o.precision in ("ff", "mixed-ff") else "f64"
+        if o.precision in ("mixed", "mixed-ff"):
+            # every chain's problem on the tensor cores first (split TF32, the batched plan's
+            # tcgen05 operator) to tol_lo, then polished at `hi` from those vectors
+            op_lo = BatchedTwoSiteOperator(probs, precision="tc")
+            _, x0, info_lo = lanczos_ground_batched(op_lo, x0, op_lo.offsets,
+                                                    tol=o.mixed_tol_lo, max_iter=mi,
+                                                    m=o.restart_m, k=o.restart_k)
+            op_lo.tc.check_device_error()
+            stats["matvecs_lo"] += info_lo["matvecs"]
+        op = BatchedTwoSiteOperator(probs, precision=hi)
         E, X, info = lanczos_ground_batched(op, x0, op.offsets, tol=o.eig_tol, max_iter=mi,
                                             m=o.restart_m, k=o.restart_k)
         stats["matvecs"] += info["matvecs"]
@@ -322,6 +395,6 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
     energies = [float(e) for e in E_last]
     return energies, [ch["M"] for ch in chains], {
         "energies": [ch["energies"] for ch in chains], "rounds": rounds,
-        "matvecs": stats["matvecs"], "phase_time": phase,
+        "matvecs": stats["matvecs"], "matvecs_lo": stats["matvecs_lo"], "phase_time": phase,
         "wall_s": time.perf_counter() - t_wall, "pipeline": pipeline,
         "discarded_weight": [ch["disc"] for ch in chains]}

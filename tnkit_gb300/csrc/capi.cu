@@ -24,6 +24,11 @@ int vec_axpby(const double*, double*, int64_t, const double*, double, const doub
 int vec_scale_div(const double*, double*, int64_t, const double*, double, cudaStream_t);
 int vec_cgs_pass(const double*, int64_t, int, const double*, double*, int64_t, double*, int,
                  double*, unsigned*, cudaStream_t);
+int vec_scale_div_seg(const double*, double*, const int64_t*, const int32_t*, int, int64_t,
+                      const double*, int64_t, double, cudaStream_t);
+int vec_cgs_pass_seg(const double*, int64_t, int, const double*, double*, const int64_t*,
+                     const int32_t*, int, int64_t, int64_t, double*, int, double*, unsigned*,
+                     cudaStream_t);
 int vec_cgs_pass_f32(const float*, int64_t, int, const double*, float*, int64_t, double*, int,
                      double*, unsigned*, cudaStream_t);
 int vec_scale_div_f32(const float*, float*, int64_t, const double*, double, cudaStream_t);
@@ -162,6 +167,21 @@ int tnk_cgs_pass_f64(const double* V, int64_t ldv, int32_t nv, const double* cin
                      int64_t n, double* out, int32_t mode, double* red, uint32_t* counter,
                      void* stream) {
     return vec_cgs_pass(V, ldv, nv, cin, w, n, out, mode, red, counter, (cudaStream_t)stream);
+}
+
+int tnk_cgs_pass_seg_f64(const double* V, int64_t ldv, int32_t nv, const double* cin, double* w,
+                         const int64_t* off, const int32_t* ids, int32_t nseg, int64_t max_len,
+                         int64_t rec_stride, double* out, int32_t mode, double* red,
+                         uint32_t* counter, void* stream) {
+    return vec_cgs_pass_seg(V, ldv, nv, cin, w, off, ids, nseg, max_len, rec_stride, out, mode,
+                            red, counter, (cudaStream_t)stream);
+}
+
+int tnk_scale_div_seg_f64(const double* x, double* y, const int64_t* off, const int32_t* ids,
+                          int32_t nseg, int64_t max_len, const double* s, int64_t s_stride,
+                          double f, void* stream) {
+    return vec_scale_div_seg(x, y, off, ids, nseg, max_len, s, s_stride, f,
+                             (cudaStream_t)stream);
 }
 
 int tnk_cgs_pass_f32(const float* V, int64_t ldv, int32_t nv, const double* cin, float* w,

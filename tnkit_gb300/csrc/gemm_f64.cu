@@ -153,7 +153,112 @@ gemm_f64_kernel(const tnk_gemm_task* __restrict__ tasks, const tnk_gemm_seg* __r
     }
 }
 
+
+// The same tile on the FP64 tensor path: mma.sync m8n8k4 (DMMA) instead of per-thread FMAs.
+// Eight warps as a 2 x 4 grid of 32 x 16 warp tiles; per K step of 4 each warp issues 4 x 2
+// MMAs from 4 A fragments (a = A[lane/4][lane%4] of an 8 x 4 slice) and 2 B fragments
+// (b = B[lane%4][lane/4] of a 4 x 8 slice), accumulating c = C[lane/4][2 (lane%4) + {0, 1}] of
+// each 8 x 8 tile in registers. Loaders, shared-memory tiles and the epilogue's flags are the
+// FMA kernel's; only the inner product differs (one instruction per 512 flops instead of 2).
+__device__ __forceinline__ void dmma_8x8x4(double& c0, double& c1, double a, double b) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                 : "+d"(c0), "+d"(c1)
+                 : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(NT, 2)
+gemm_f64_dmma_kernel(const tnk_gemm_task* __restrict__ tasks,
+                     const tnk_gemm_seg* __restrict__ segs, const tnk_gemm_tile* __restrict__ tiles,
+                     Slots slots, double* __restrict__ C) {
+    __shared__ double As[2][BK * PADA];
+    __shared__ double Bs[2][BK * PADB];
+    const tnk_gemm_tile tile = tiles[blockIdx.x];
+    const tnk_gemm_task task = tasks[tile.task];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+    const int g = lane >> 2, q = lane & 3;
+    const int M = task.m, N = task.n, m0 = tile.m0, n0 = tile.n0;
+
+    double acc[4][2][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+    int cur = 0;
+    for (int si = task.seg_begin; si < task.seg_end; ++si) {
+        const tnk_gemm_seg sg = segs[si];
+        SegView s;
+        s.a = slots.p[sg.a_buf] + sg.a_off;
+        s.b = slots.p[sg.b_buf] + sg.b_off;
+        s.a_rs = sg.a_rs; s.a_cs = sg.a_cs; s.b_rs = sg.b_rs; s.b_cs = sg.b_cs;
+        s.k = sg.k; s.coef = sg.coef;
+        if (s.k <= 0) continue;
+        double ra[4], rb[4];
+        load_a(s, m0, M, 0, tid, ra);
+        load_b(s, n0, N, 0, tid, rb);
+        store_a(s, tid, ra, As[cur]);
+        store_b(s, tid, rb, Bs[cur]);
+        __syncthreads();
+        for (int k0 = 0; k0 < s.k; k0 += BK) {
+            const bool more = k0 + BK < s.k;
+            if (more) {
+                load_a(s, m0, M, k0 + BK, tid, ra);
+                load_b(s, n0, N, k0 + BK, tid, rb);
+            }
+            const double* as = As[cur];
+            const double* bs = Bs[cur];
+#pragma unroll
+            for (int kk = 0; kk < BK; kk += 4) {
+                double a[4], b[2];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) a[i] = as[(kk + q) * PADA + wm + 8 * i + g];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) b[j] = bs[(kk + q) * PADB + wn + 8 * j + g];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) dmma_8x8x4(acc[i][j][0], acc[i][j][1], a[i], b[j]);
+            }
+            if (more) {
+                store_a(s, tid, ra, As[cur ^ 1]);
+                store_b(s, tid, rb, Bs[cur ^ 1]);
+            }
+            __syncthreads();
+            cur ^= 1;
+        }
+    }
+
+    const bool accumulate = (task.flags & 1) != 0;
+    const int64_t ccs = (task.flags & 4) ? 2 : 1;
+    double* c = ((task.flags & 16) ? const_cast<double*>(slots.p[3]) : C) + task.c_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = m0 + wm + 8 * i + g;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int n = n0 + wn + 8 * j + 2 * q + h;
+                if (n >= N) continue;
+                double* p = c + (int64_t)m * task.ldc + (int64_t)n * ccs;
+                *p = accumulate ? *p + acc[i][j][h] : acc[i][j][h];
+            }
+        }
+    }
+}
+
+int g_gemm_f64_variant = 0;     // 0: FP64 FMA tile, 1: DMMA tile (tnk_gemm_f64_variant)
+
 }  // namespace
+
+// Selects the inner product of every FP64 grouped GEMM launched afterwards (process-wide).
+extern "C" int tnk_gemm_f64_variant(int32_t variant) {
+    const int prev = g_gemm_f64_variant;
+    if (variant == 0 || variant == 1) g_gemm_f64_variant = variant;
+    return prev;
+}
 
 int launch_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
                     const tnk_gemm_tile* tiles, int64_t n_tiles, Slots slots, double* C,
@@ -166,6 +271,10 @@ int launch_gemm_f64(const tnk_gemm_task* tasks, const tnk_gemm_seg* segs,
     if (!tasks || !segs || !tiles || !C) {
         set_error("grouped gemm: null table or output pointer");
         return TNK_ERR_ARG;
+    }
+    if (g_gemm_f64_variant == 1) {
+        gemm_f64_dmma_kernel<<<(unsigned)n_tiles, NT, 0, stream>>>(tasks, segs, tiles, slots, C);
+        return check_launch("gemm_f64_dmma_kernel");
     }
     gemm_f64_kernel<<<(unsigned)n_tiles, NT, 0, stream>>>(tasks, segs, tiles, slots, C);
     return check_launch("gemm_f64_kernel");

@@ -217,13 +217,34 @@ __global__ void __launch_bounds__(CG_NT) finish_kernel(const double* __restrict_
     finish_partials(red, nb, prow, nrow, root != 0, fin, CG_FIN_ELEMS, out);
 }
 
+// Segmented launches: many independent vectors (chains) concatenated in one batch vector, chain
+// c at [off[c], off[c+1]); grid row y works on chain ids[y] alone, with its own coefficient
+// vector cin + c*rec_stride, output out + c*rec_stride, partial rows and completion counter
+// (counter + y): one launch performs the pass of every listed chain, no reduction mixing them.
+struct CgsSeg {
+    const int64_t* off;          // null: one segment, the plain pass
+    const int32_t* ids;
+    int64_t rec_stride;
+};
+
 template <typename T, int NVB, int MODE>
 __global__ void __launch_bounds__(CG_NT) cgs_kernel(const T* __restrict__ V, int64_t ldv, int nv,
                                                    const double* __restrict__ cin,
                                                    T* __restrict__ w, int64_t n,
                                                    double* __restrict__ red,
                                                    unsigned* __restrict__ counter,
-                                                   double* __restrict__ out) {
+                                                   double* __restrict__ out, CgsSeg seg) {
+    if (seg.off) {
+        const int c = seg.ids[blockIdx.y];
+        const int64_t a = seg.off[c];
+        n = seg.off[c + 1] - a;
+        V += a;
+        w += a;
+        if (cin) cin += (int64_t)c * seg.rec_stride;
+        if (out) out += (int64_t)c * seg.rec_stride;
+        if (red) red += (int64_t)blockIdx.y * gridDim.x * PSTRIDE;
+        if (counter) counter += blockIdx.y;
+    }
     constexpr bool SUB = (MODE & CG_SUB) != 0;
     constexpr bool DOT = (MODE & CG_DOT) != 0;
     constexpr bool NRM = (MODE & CG_NRM) != 0;
@@ -368,10 +389,21 @@ int cgs_grid(int64_t n, int nv) {
 
 template <typename T, int NVB, int MODE>
 int launch_cgs_t(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64_t n,
-                 double* red, unsigned* counter, double* out, cudaStream_t st) {
-    const int g = cgs_grid<T, NVB, MODE>(n, nv);
+                 double* red, unsigned* counter, double* out, cudaStream_t st,
+                 CgsSeg seg = CgsSeg{nullptr, nullptr, 0}, int nseg = 1) {
+    int g = cgs_grid<T, NVB, MODE>(n, nv);
+    if (seg.off) {
+        // every chain gets the same number of CTAs; all of their partial rows fit the
+        // reduction buffer (n here is the longest segment)
+        const int per = (TNK_RED_ELEMS / PSTRIDE) / nseg;
+        g = g > per ? per : g;
+        g = g < 1 ? 1 : g;
+        cgs_kernel<T, NVB, MODE><<<dim3(g, nseg), CG_NT, cg_ring_bytes(nv, (int)sizeof(T)), st>>>(
+            V, ldv, nv, cin, w, n, red, counter, out, seg);
+        return check_launch("cgs_kernel (segmented)");
+    }
     cgs_kernel<T, NVB, MODE><<<g, CG_NT, cg_ring_bytes(nv, (int)sizeof(T)), st>>>(
-        V, ldv, nv, cin, w, n, red, counter, out);
+        V, ldv, nv, cin, w, n, red, counter, out, seg);
     int rc = check_launch("cgs_kernel");
     if (rc || counter || !(MODE & (CG_DOT | CG_NRM))) return rc;
     finish_kernel<<<1, CG_NT, 0, st>>>(red, g, cg_prow(MODE, nv), (MODE & CG_DOT) ? nv : 1,
@@ -382,10 +414,13 @@ int launch_cgs_t(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64
 // One launch of a fixed mode over nv <= 64 rows (NVB, the accumulator count, picked from nv).
 template <int MODE, typename T>
 int launch_cgs(const T* V, int64_t ldv, int nv, const double* cin, T* w, int64_t n,
-               double* red, unsigned* counter, double* out, cudaStream_t st) {
-    if (nv <= 16) return launch_cgs_t<T, 16, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
-    if (nv <= 32) return launch_cgs_t<T, 32, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
-    return launch_cgs_t<T, 64, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st);
+               double* red, unsigned* counter, double* out, cudaStream_t st,
+               CgsSeg seg = CgsSeg{nullptr, nullptr, 0}, int nseg = 1) {
+    if (nv <= 16)
+        return launch_cgs_t<T, 16, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st, seg, nseg);
+    if (nv <= 32)
+        return launch_cgs_t<T, 32, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st, seg, nseg);
+    return launch_cgs_t<T, 64, MODE>(V, ldv, nv, cin, w, n, red, counter, out, st, seg, nseg);
 }
 
 __global__ void __launch_bounds__(NT) axpby_kernel(const double* __restrict__ x,
@@ -412,6 +447,21 @@ __global__ void __launch_bounds__(NT) scale_div_kernel(const double* __restrict_
     const double a = f / s[0];
     for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n; k += (int64_t)gridDim.x * NT)
         y[k] = x[k] * a;
+}
+
+// Segmented scale: grid row y scales chain ids[y]'s segment [off[c], off[c+1]) of x into y by
+// f / s[c * s_stride] (each chain its own device scalar).
+__global__ void __launch_bounds__(NT) scale_div_seg_kernel(const double* __restrict__ x,
+                                                           double* __restrict__ y,
+                                                           const int64_t* __restrict__ off,
+                                                           const int32_t* __restrict__ ids,
+                                                           const double* s, int64_t s_stride,
+                                                           double f) {
+    const int c = ids[blockIdx.y];
+    const int64_t a = off[c], n = off[c + 1] - a;
+    const double m = f / s[(int64_t)c * s_stride];
+    for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < n; k += (int64_t)gridDim.x * NT)
+        y[a + k] = x[a + k] * m;
 }
 
 // Thick-restart rotation of an FP32 Krylov basis: out[q*ldo + k] = sum_r Y[r*kk + q] V[r*ldv + k]
@@ -529,6 +579,46 @@ int vec_cgs_pass(const double* V, int64_t ldv, int nv, const double* cin, double
     return cgs_pass_t<double>(V, ldv, nv, cin, w, n, out, mode, red, counter, st);
 }
 
+// The segmented pass: chains ids[0..nseg) of the batch (offsets `off`, device arrays), the
+// longest of them `max_len` entries, coefficient and output records rec_stride doubles apart,
+// one completion counter per listed chain (counter[0..nseg), zero before the call and left
+// zero after it).
+int vec_cgs_pass_seg(const double* V, int64_t ldv, int nv, const double* cin, double* w,
+                     const int64_t* off, const int32_t* ids, int nseg, int64_t max_len,
+                     int64_t rec_stride, double* out, int mode, double* red, unsigned* counter,
+                     cudaStream_t st) {
+    const bool sub = mode & CG_SUB, dot = mode & CG_DOT, nrm = mode & CG_NRM;
+    if (nseg < 0 || nseg > 65535 || max_len < 0 || nv < 0 || nv > MAXNV || mode < 1 ||
+        mode > 7 || (dot && nrm) || (nseg > 0 && (!off || !ids || !w)) ||
+        ((sub || dot) && (ldv < max_len || (nv > 0 && !V))) || (sub && !cin) ||
+        ((dot || nrm) && (!out || !red || ((uintptr_t)red & 15) || !counter)) ||
+        rec_stride < 0 || (nseg > 0 && (int64_t)nseg * PSTRIDE > TNK_RED_ELEMS)) {
+        set_error("cgs_pass_seg: bad argument (mode=%d, nv=%d, nseg=%d, max_len=%lld)", mode, nv,
+                  nseg, (long long)max_len);
+        return TNK_ERR_ARG;
+    }
+    if (nseg == 0 || max_len == 0) return TNK_OK;
+    const CgsSeg seg{off, ids, rec_stride};
+    switch (mode) {
+        case CG_SUB:
+            if (nv == 0) return TNK_OK;
+            return launch_cgs<CG_SUB>(V, ldv, nv, cin, w, max_len, nullptr, nullptr, nullptr, st,
+                                      seg, nseg);
+        case CG_DOT:
+            return launch_cgs<CG_DOT>(V, ldv, nv, cin, w, max_len, red, counter, out, st, seg,
+                                      nseg);
+        case CG_SUB | CG_DOT:
+            return launch_cgs<CG_SUB | CG_DOT>(V, ldv, nv, cin, w, max_len, red, counter, out,
+                                               st, seg, nseg);
+        case CG_NRM:
+            return launch_cgs<CG_NRM>(V, ldv, 0, nullptr, w, max_len, red, counter, out, st, seg,
+                                      nseg);
+        default:  // CG_SUB | CG_NRM
+            return launch_cgs<CG_SUB | CG_NRM>(V, ldv, nv, cin, w, max_len, red, counter, out,
+                                               st, seg, nseg);
+    }
+}
+
 int vec_cgs_pass_f32(const float* V, int64_t ldv, int nv, const double* cin, float* w,
                      int64_t n, double* out, int mode, double* red, unsigned* counter,
                      cudaStream_t st) {
@@ -555,6 +645,24 @@ int vec_scale_div(const double* x, double* y, int64_t n, const double* s, double
     if (n == 0) return TNK_OK;
     scale_div_kernel<<<grid_for(n, 16 * NSM), NT, 0, stream>>>(x, y, n, s, f);
     return check_launch("scale_div_kernel");
+}
+
+int vec_scale_div_seg(const double* x, double* y, const int64_t* off, const int32_t* ids,
+                      int nseg, int64_t max_len, const double* s, int64_t s_stride, double f,
+                      cudaStream_t stream) {
+    if (nseg < 0 || nseg > 65535 || max_len < 0 || s_stride < 0 ||
+        (nseg > 0 && (!x || !y || !off || !ids || !s))) {
+        set_error("scale_div_seg: bad argument");
+        return TNK_ERR_ARG;
+    }
+    if (nseg == 0 || max_len == 0) return TNK_OK;
+    int64_t gx = (max_len + NT - 1) / NT;
+    const int64_t cap = (16 * NSM + nseg - 1) / nseg;
+    if (gx > cap) gx = cap;
+    if (gx < 1) gx = 1;
+    scale_div_seg_kernel<<<dim3((unsigned)gx, (unsigned)nseg), NT, 0, stream>>>(
+        x, y, off, ids, s, s_stride, f);
+    return check_launch("scale_div_seg_kernel");
 }
 
 int vec_scale_div_f32(const float* x, float* y, int64_t n, const double* s, double f,

@@ -34,17 +34,30 @@ class TwoSiteOperatorTC:
 
     def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
                  R: BlockTensor, passes: int = 3):
-        if passes not in (1, 3):
-            raise ValueError("passes must be 1 (TF32) or 3 (split TF32)")
-        dev = L.data.device
-        self.device = dev
-        self.passes = passes
         key = _two_site_key(theta_layout, L, W1, W2, R)
         tc = _PLANS.get_or(("tc",) + key, lambda: P.HostPlanTC(
             host_plan_two_site(theta_layout, L, W1, W2, R), theta_layout, L.layout, R.layout))
+        self._setup(tc, L.data, R.data, theta_layout.size, passes)
+
+    @classmethod
+    def from_host_plan(cls, hp, L_data: torch.Tensor, R_data: torch.Tensor, n: int,
+                       passes: int = 3) -> "TwoSiteOperatorTC":
+        """The tensor-core operator of any two-site three-stage plan `hp` (a HostPlan3 whose
+        slot 0 is `L_data`, slot 2 `R_data` and slot 1 a vector of n entries), e.g. a batched
+        plan over many chains' local problems."""
+        self = cls.__new__(cls)
+        self._setup(P.HostPlanTC(hp, None, None, None), L_data, R_data, n, passes)
+        return self
+
+    def _setup(self, tc, L_data: torch.Tensor, R_data: torch.Tensor, n: int, passes: int):
+        if passes not in (1, 3):
+            raise ValueError("passes must be 1 (TF32) or 3 (split TF32)")
+        dev = L_data.device
+        self.device = dev
+        self.passes = passes
         self.host = tc
         self.macs = tc.macs
-        self.n = theta_layout.size
+        self.n = n
         self.stage = torch.empty(2 * tc.stage_elems, dtype=torch.float32, device=dev)
         self.y32 = torch.empty(max(tc.y32_elems, 1), dtype=torch.float32, device=dev)
         self.err = torch.zeros(16, dtype=torch.int32, device=dev)
@@ -67,13 +80,13 @@ class TwoSiteOperatorTC:
                              self.y32.data_ptr(), self.err.data_ptr(), passes, 0)
         sp = _lib.stream_ptr()
         split = 1 if passes == 3 else 0
-        _lib.check(lib.tnk_stage_f32(a[12], a[13], len(tc.cvt_items["L"]), L.data.data_ptr(),
+        _lib.check(lib.tnk_stage_f32(a[12], a[13], len(tc.cvt_items["L"]), L_data.data_ptr(),
                                      self.stage.data_ptr(), tc.stage_elems, split, sp),
                    "stage L")
-        _lib.check(lib.tnk_stage_f32(a[14], a[15], len(tc.cvt_items["R"]), R.data.data_ptr(),
+        _lib.check(lib.tnk_stage_f32(a[14], a[15], len(tc.cvt_items["R"]), R_data.data_ptr(),
                                      self.stage.data_ptr(), tc.stage_elems, split, sp),
                    "stage R")
-        self.L, self.R = L, R        # staged copies were taken; keep the sources alive anyway
+        self.L, self.R = L_data, R_data   # staged copies were taken; keep the sources alive
         self.calls = 0
 
     def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
