@@ -46,6 +46,24 @@ def test_lanczos_expm_matches_reference(tg, route):
     assert np.abs(y.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("m", [20, 30])
+def test_lanczos_expm_fixed_matches_reference(tg, m):
+    """The fixed-dimension exponential with every coefficient on the device (no host read
+    during the solve, the tridiagonal eigendecomposition by the library's kernel) gives the
+    reference's adaptive vector once m is above the dimension the adaptive solver needed."""
+    from tnkit_gb300.expm import lanczos_expm_fixed
+    meta, A = tg
+    H = torch.as_tensor(A["expm_H"], device="cuda")
+    v = torch.as_tensor(A["expm_v"], device="cuda")
+    assert m > meta["expm"]["krylov_dim"]
+    info = {}
+    y = lanczos_expm_fixed(lambda x, out: out.copy_(H @ x), v, meta["expm"]["tau_imag"] * 1j,
+                           m, info=info)
+    ref = A["expm_y"]
+    assert info["krylov_dim"] == m
+    assert np.abs(y.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
 def test_complex_contractions_match_oracle(golden):
     from tnkit_gb300 import BlockTensor, Leg, layout_of, ops
     from oracle.blocks_np import BT, Leg as OL
@@ -77,7 +95,11 @@ def test_complex_contractions_match_oracle(golden):
                O.update_right_env(oR, oB, oW2).flat()) <= 1e-13
 
 
-def test_tdvp2_state_matches_reference(tg):
+@pytest.mark.parametrize("fast_expm", [None, 20, "auto"])
+def test_tdvp2_state_matches_reference(tg, fast_expm):
+    """Four TDVP2 steps from the reference's seeded state: its final state vector and bonds,
+    with the adaptive Krylov exponential and with the fixed-dimension one (a fixed m, and m
+    calibrated on the first step: the reference's fast_expm)."""
     from tnkit_gb300 import BlockTensor, Leg, layout_of, workloads
     from tnkit_gb300.mpo import to_block_mpo
     from tnkit_gb300.tdvp import tdvp2_evolve, dense_vector
@@ -94,7 +116,8 @@ def test_tdvp2_state_matches_reference(tg):
     assert np.abs(v0 - A["init_vector"]).max() <= 1e-13 * np.abs(A["init_vector"]).max()
     Wb = to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
     prof = {}
-    out, rec = tdvp2_evolve(mps, Wb, p["chi"], p["dt"], p["n_steps"], profile=prof)
+    out, rec = tdvp2_evolve(mps, Wb, p["chi"], p["dt"], p["n_steps"], profile=prof,
+                            fast_expm=fast_expm)
     v = dense_vector(out)
     ref = A["final_vector"]
     assert abs(abs(np.vdot(ref, v)) / (np.linalg.norm(ref) * np.linalg.norm(v)) - 1) <= 1e-11

@@ -168,3 +168,77 @@ def lanczos_expm(matvec: Callable, v: torch.Tensor, tau: complex, m: int = 30,
                                      out.data_ptr(), n, sp), "zgemv_sub")
     torch.cuda.current_stream().synchronize()
     return out
+
+
+def lanczos_expm_fixed(matvec: Callable, v: torch.Tensor, tau: complex, m: int,
+                       info: Optional[dict] = None) -> torch.Tensor:
+    """exp(tau H) v from exactly `m` Lanczos steps with no host round trip (the reference's
+    lanczos_expm_fixed, tnkit/eigensolver.py:95-217, with its 'eigh' route): every Lanczos
+    coefficient stays in device memory -- the three-term subtraction, the two CGS passes and
+    the normalisation read alpha and beta from there -- and the tridiagonal's eigendecomposition
+    (tnk_tridiag_eig_f64), the coefficients beta0 exp(tau T) e_1 and the combination of the
+    basis run on the device after the last step. Breakdown needs no branch: a beta at
+    rounding level is clamped (the reference's guard_denom) before it divides, and the
+    coefficients of the later vectors are at rounding level. Nothing is read back; the caller
+    synchronises when it needs the result. `m` is capped at the vector length."""
+    if not (v.is_cuda and v.dtype == torch.complex128):
+        raise TypeError("lanczos_expm_fixed needs a complex128 CUDA vector")
+    from .tridiag import tridiag_eigh_batched
+    lib = _lib.lib()
+    sp = _lib.stream_ptr()
+    dev = v.device
+    v = v.reshape(-1)
+    n = v.numel()
+    m = max(1, min(int(m), n))
+    if m + 1 > _MAXNV:
+        raise ValueError(f"Krylov dimension {m} exceeds {_MAXNV - 1}")
+    red = torch.empty(_lib.TNK_RED_ELEMS, dtype=torch.float64, device=dev)
+    c1 = torch.zeros(2 * _MAXNV, dtype=torch.float64, device=dev)
+    c2 = torch.zeros(2 * _MAXNV, dtype=torch.float64, device=dev)
+    # beta_k as complex numbers (beta, 0) in bc[2k], bc[2k+1]; beta0 in b0[0], b0[1] = 0
+    bc = torch.zeros(2 * (m + 1), dtype=torch.float64, device=dev)
+    b0 = torch.zeros(2, dtype=torch.float64, device=dev)
+    alph = torch.zeros(m, dtype=torch.float64, device=dev)
+    V = torch.empty((m, n), dtype=torch.complex128, device=dev)
+    w = torch.empty(n, dtype=torch.complex128, device=dev)
+    _lib.check(lib.tnk_nrm2_f64(_real(v).data_ptr(), 2 * n, b0.data_ptr(), red.data_ptr(), sp),
+               "nrm2")
+    beta0 = b0[:1].clone()
+    b0[:1].clamp_(min=1e-200)
+    _lib.check(lib.tnk_scale_div_f64(_real(v).data_ptr(), _real(V[0]).data_ptr(), 2 * n,
+                                     b0.data_ptr(), 1.0, sp), "scale_div")
+    for k in range(m):
+        matvec(V[k], w)
+        if k > 0:
+            _lib.check(lib.tnk_zaxpby_f64(V[k - 1].data_ptr(), w.data_ptr(), n,
+                                          bc.data_ptr() + 16 * (k - 1), -1.0, None, 1.0, sp),
+                       "zaxpby")
+        for cc in (c1, c2):
+            _lib.check(lib.tnk_zmultidot_f64(V.data_ptr(), n, k + 1, w.data_ptr(), n,
+                                             cc.data_ptr(), red.data_ptr(), sp), "zmultidot")
+            _lib.check(lib.tnk_zgemv_sub_f64(V.data_ptr(), n, k + 1, cc.data_ptr(),
+                                             w.data_ptr(), n, sp), "zgemv_sub")
+            if cc is c1:
+                alph[k:k + 1].copy_(c1[2 * k:2 * k + 1])   # Re <V_k, w>: the Lanczos alpha
+        if k < m - 1:
+            _lib.check(lib.tnk_nrm2_f64(_real(w).data_ptr(), 2 * n, bc.data_ptr() + 16 * k,
+                                        red.data_ptr(), sp), "nrm2")
+            bc[2 * k:2 * k + 1].clamp_(min=1e-200)
+            _lib.check(lib.tnk_scale_div_f64(_real(w).data_ptr(), _real(V[k + 1]).data_ptr(),
+                                             2 * n, bc.data_ptr() + 16 * k, 1.0, sp),
+                       "scale_div")
+    e = bc[0:2 * (m - 1):2].reshape(1, -1) if m > 1 else None
+    lam, Z = tridiag_eigh_batched(alph.reshape(1, -1), e, check=False)
+    lam, Z = lam[0], Z[0]
+    ph = torch.exp(torch.as_tensor(complex(tau), dtype=torch.complex128, device=dev) *
+                   lam.to(torch.complex128))
+    Zc = Z.to(torch.complex128)
+    coef = beta0.to(torch.complex128) * (Zc @ (ph * Zc[0, :]))
+    cneg = torch.view_as_real(-coef).reshape(-1).contiguous()
+    out = torch.zeros(n, dtype=torch.complex128, device=dev)
+    _lib.check(lib.tnk_zgemv_sub_f64(V.data_ptr(), n, m, cneg.data_ptr(), out.data_ptr(), n,
+                                     sp), "zgemv_sub")
+    if info is not None:
+        info.update(krylov_dim=m, err_est=float("nan"), beta1=float("nan"),
+                    est_ref=float("nan"), est_ref_j=0, capped=False)
+    return out

@@ -259,7 +259,7 @@ def run_dmrg(mpo, chi, o, precision: str = "f64"):
 
 
 _TDVP_TAKES = {"backend", "measure", "meas_every", "trunc", "chi_max", "renorm", "seed",
-               "canonicalize", "keep_device", "krylov_m", "profile"}
+               "canonicalize", "keep_device", "krylov_m", "profile", "fast_expm"}
 
 
 def run_tdvp2(mps, mpo, chi, dt, n_steps, o, precision: str = "f64"):
@@ -291,11 +291,15 @@ def run_tdvp2(mps, mpo, chi, dt, n_steps, o, precision: str = "f64"):
         back = _dense_mps_out
     measure = None if o.measure is None else (lambda ms: o.measure(back(ms)))
     cap = int(chi if o.chi_max is None else o.chi_max)
+    fe = o.fast_expm
+    if isinstance(fe, dict):            # the reference's re-entrant form: its fixed m, or 'auto'
+        fe = fe.get("m") or "auto"
     prof = {} if o.profile is not None else None
     out, records = tdvp2_evolve(M, W, cap, dt, n_steps, measure=measure,
                                 meas_every=o.meas_every, krylov_m=o.krylov_m, renorm=o.renorm,
                                 canonicalize=o.canonicalize, profile=prof,
-                                svd_method="gram" if o.trunc == "gram" else "svd")
+                                svd_method="gram" if o.trunc == "gram" else "svd",
+                                fast_expm=fe)
     if prof is not None:
         o.profile.update(prof)
     centre = 0 if (o.canonicalize or n_steps > 0) else None
