@@ -231,7 +231,10 @@ def main():
     build.build()
     _lib.load()
     th, L, W1, W2, R = workloads.mid_bond_problem(seed=3 + rank, device=dev)
-    op = ops.TwoSiteOperator(th.layout, L, W1, W2, R)
+    # the schedule (FP64 inner product, stage-3 split-K, tile order) picked by the autotuner on
+    # this problem; every FP64 launch of the legs below uses its inner product
+    op = ops.TwoSiteOperator(th.layout, L, W1, W2, R, tune=True)
+    _lib.lib().tnk_gemm_f64_variant(op.inner)
     p = op.plan
     hp = p.host
     ref_macs = P.two_site_ref_macs(th.layout, L.layout, W1.layout, W2.layout, R.layout)
@@ -417,6 +420,10 @@ def main():
                     "d2h_bytes_per_step": x.numel() * 8, "max_rel_err_vs_device": err_e2e},
             "gpu_launches": per_step * args.steps,
             "clocks": clocks}
+    line["autotune"] = {"choice": op.tuned.schedule.label(), "ms": op.tuned.ms,
+                        "candidates_ms": op.tuned.table,
+                        "how": "each candidate schedule once untimed, then 3 matvecs between "
+                               "CUDA events on the launching stream (L2 not flushed)"}
     names = {0: "fp64 FMA tile (4 x 4 per thread)", 1: "DMMA tile (mma.sync m8n8k4 f64)"}
     line["fp64_variants"] = {
         "headline": names[var0],
@@ -563,8 +570,8 @@ def batch_leg(torch, dev, flush, steps):
     from tnkit_gb300 import batch as B, ops
     probs = B.batch_problems(64, seed=2, device=dev)
     singles = [ops.TwoSiteOperator(th, L, W1, W2, R) for th, L, W1, W2, R in probs]
-    op = B.BatchedTwoSiteOperator(probs)
-    opf = B.BatchedTwoSiteOperator(probs, precision="ff")
+    op = B.BatchedTwoSiteOperator(probs, tune=True)
+    opf = B.BatchedTwoSiteOperator(probs, precision="ff", tune=True)
     opt = B.BatchedTwoSiteOperator(probs, precision="tc")
     flops = 2 * op.ref_macs
     x = torch.randn(op.n, dtype=torch.float64, device=dev)
@@ -623,10 +630,13 @@ def batch_leg(torch, dev, flush, steps):
             "gflop_per_step": flops / 1e9,
             "sequential_f64": dict(seq, launches=n_seq),
             "batched_f64": dict(bat, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
-                                bat["ms_per_step"], max_rel_err_vs_sequential=err),
+                                bat["ms_per_step"], max_rel_err_vs_sequential=err,
+                                autotune=op.tuned.schedule.label(),
+                                autotune_candidates_ms=op.tuned.table),
             "graph_f64": dict(gra, launches=n_bat, speedup_vs_sequential=seq["ms_per_step"] /
                               gra["ms_per_step"], max_abs_diff_vs_batched=errg),
-            "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf),
+            "batched_ff": dict(bff, launches=n_bat + 1, max_rel_err_vs_sequential_f64=errf,
+                               autotune=opf.tuned.schedule.label()),
             "batched_tc": dict(btc, launches=4, max_rel_err_vs_sequential_f64=errt,
                                note="split-TF32 tcgen05 grouped GEMMs of the same batched plan "
                                     "(theta staging, two GEMM stages, FP32 combination)")}

@@ -99,7 +99,7 @@ class BatchedTwoSiteOperator:
     (the tensor-core split-TF32 operator of the same batched plan: operands staged once in FP32,
     one tcgen05 grouped-GEMM launch per GEMM stage for all problems; ~1e-6 relative)."""
 
-    def __init__(self, problems: Sequence[Problem], precision: str = "f64"):
+    def __init__(self, problems: Sequence[Problem], precision: str = "f64", tune: bool = False):
         if precision not in ("f64", "ff", "tc"):
             raise ValueError("precision must be 'f64', 'ff' or 'tc'")
         if not problems:
@@ -138,6 +138,23 @@ class BatchedTwoSiteOperator:
         if precision == "tc":
             from .mixed import TwoSiteOperatorTC
             self.tc = TwoSiteOperatorTC.from_host_plan(hp, self.L, self.R, self.n)
+        self.inner, self.tuned = None, None
+        if tune and precision != "tc":
+            from . import autotune as AT
+            xt = torch.randn(self.n, dtype=torch.float64, device=dev)
+            yt = torch.empty_like(xt)
+            ff = precision == "ff"
+
+            def run(dp):
+                w = ops.workspace(dp.ws_elems + (dp.out_elems if ff else 0), dev)
+                dp.run(self.fn, self.Lx, xt, self.Rx, yt, w)
+            t = AT.tune(hp, run, ff=ff)
+            self.host = AT.scheduled_plan(hp, t.schedule)
+            self.plan = ops.DevicePlan3(self.host, dev, ff=ff)
+            need = self.plan.ws_elems + (self.plan.out_elems if ff else 0)
+            self.ws = torch.empty(max(need, 1), dtype=torch.float64, device=dev)
+            self._owners(plans, starts)
+            self.inner, self.tuned = t.schedule.inner, t
         if precision == "ff":        # float-float copies of the arenas, split once
             lib, sp = _lib.lib(), _lib.stream_ptr()
             self.Lx, self.Rx = torch.empty_like(self.L), torch.empty_like(self.R)
@@ -195,8 +212,15 @@ class BatchedTwoSiteOperator:
         y = torch.empty_like(x) if out is None else out
         if self.tc is not None:
             self.tc(x, y)
-        else:
+        elif self.inner is None:
             self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+        else:
+            lib = _lib.lib()
+            prev = lib.tnk_gemm_f64_variant(self.inner)
+            try:
+                self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+            finally:
+                lib.tnk_gemm_f64_variant(prev)
         self.calls += 1
         return y
 

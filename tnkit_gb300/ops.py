@@ -360,7 +360,7 @@ class TwoSiteOperator:
     precision 'f64' runs the FP64 grouped GEMM, 'ff' the float-float one (same plan)."""
 
     def __init__(self, theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
-                 R: BlockTensor, precision: str = "f64"):
+                 R: BlockTensor, precision: str = "f64", tune: bool = False):
         if precision not in _APPLY2:
             raise ValueError(f"precision must be one of {sorted(_APPLY2)}")
         self.fn = _APPLY2[precision]
@@ -382,6 +382,27 @@ class TwoSiteOperator:
         else:
             self.Lx, self.Rx = L.data, R.data
         self.calls = 0
+        self.inner, self.tuned = None, None
+        if tune:
+            self._tune(ff)
+
+    def _tune(self, ff: bool):
+        """Pick the plan's schedule (inner product, split-K, tile order) by timing the
+        candidates on this problem's operands (autotune.tune; cached per shape class)."""
+        from . import autotune as AT
+        hp = self.plan.host
+        dt = torch.complex128 if self.cplx else torch.float64
+        xt = torch.randn(self.n, dtype=dt, device=self.device)
+        yt = torch.empty_like(xt)
+
+        def run(dp):
+            w = workspace(dp.ws_elems + (dp.out_elems if ff else 0), self.device)
+            dp.run(self.fn, self.Lx, xt, self.Rx, yt, w)
+        t = AT.tune(hp, run, ff=ff)
+        self.plan = DevicePlan3(AT.scheduled_plan(hp, t.schedule), self.device, ff=ff)
+        self.ws = workspace(self.plan.ws_elems + (self.plan.out_elems if ff else 0),
+                            self.device)
+        self.inner, self.tuned = t.schedule.inner, t
 
     @property
     def macs(self):
@@ -389,7 +410,15 @@ class TwoSiteOperator:
 
     def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         y = torch.empty_like(x) if out is None else out
-        self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+        if self.inner is None:
+            self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+        else:
+            lib = _lib.lib()
+            prev = lib.tnk_gemm_f64_variant(self.inner)
+            try:
+                self.plan.run(self.fn, self.Lx, x, self.Rx, y, self.ws)
+            finally:
+                lib.tnk_gemm_f64_variant(prev)
         self.calls += 1
         return y
 
