@@ -113,4 +113,4 @@ def test_segmented_passes_equal_per_chain_passes():
     A.scale_div_all(wa, ya, act)
     for c in act:
         B.scale_div(wb, yb, c)
-    assert torch.allclose(ya, yb, rtol=1e-13, atol=0)
+    assert torch.allclose(ya, yb, rtol=0, atol=1e-12 * float(yb.abs().max()))

@@ -138,6 +138,9 @@ class BatchedTwoSiteOperator:
         if precision == "tc":
             from .mixed import TwoSiteOperatorTC
             self.tc = TwoSiteOperatorTC.from_host_plan(hp, self.L, self.R, self.n)
+        # the FP64 / float-float launches can drop converged problems' tiles (set_active); the
+        # tensor-core operator computes every problem on every call
+        self.supports_mask = precision != "tc"
         self.inner, self.tuned = None, None
         if tune and precision != "tc":
             from . import autotune as AT

@@ -200,7 +200,7 @@ def lanczos_ground_batched(op, x0: torch.Tensor, offsets: Sequence[int], tol: fl
         keep = np.nonzero(~done)[0]
         if len(keep) == 0:
             break
-        if done.any() and hasattr(op, "set_active"):
+        if done.any() and getattr(op, "supports_mask", False):
             op.set_active(active)                     # converged chains leave the launches
         if cur >= m:                                  # thick restart, all chains in step
             kk = min(k, cur - 1)
