@@ -513,8 +513,8 @@ def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps,
         _lib.check(lib.tnk_combine_f32(c.t2, c.c2, c.items2, c.n_items2, c.y32, c.stage,
                                        c.lo_off, 1, sp), "comb32")
         e[2].record(stream)
-        _lib.check(lib.tnk_grouped_gemm_tc(c.t3, c.s3, c.tiles3, c.n_tiles3, c.maps,
-                                           y.data_ptr(), c.err, 3, sp), "tc3")
+        _lib.check(lib.tnk_grouped_gemm_tc_bn(c.t3, c.s3, c.tiles3, c.n_tiles3, c.maps,
+                                              y.data_ptr(), c.err, 3, c.bn3 or 128, sp), "tc3")
         e[3].record(stream)
         torch.cuda.synchronize()
         tg += (e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])) / 1e3

@@ -234,7 +234,9 @@ typedef struct {
 /* The tensor-core two-site plan. `stage` is one FP32 buffer holding every staged operand (L, R,
  * theta^T, Z) at the tables' offsets, hi parts first and lo parts at +lo_off; `y32` holds the
  * stage-1 output. `maps` are the CUtensorMaps (128 bytes each, 64-byte aligned) of the staged
- * blocks; `err` is a device word that a kernel sets (nonzero) if a bounded wait timed out. */
+ * blocks; `err` is a device word that a kernel sets (nonzero) if a bounded wait timed out.
+ * bn3: the tile width of stage 3 (128 x bn3 tiles; 0 means 128, or 64, in which case the maps
+ * of stage 3's B operands must have boxes of 64 rows, tnk_tc_encode_tmaps_box). */
 typedef struct {
     const tnk_cvt_task* cvt; const tnk_cvt_item* cvt_items; int64_t n_cvt_items;
     const tnk_gemm_task* t1; const tnk_tc_seg* s1; const tnk_gemm_tile* tiles1; int64_t n_tiles1;
@@ -244,7 +246,7 @@ typedef struct {
     float* stage; int64_t lo_off;
     float* y32;
     int* err;
-    int32_t passes, pad;
+    int32_t passes, bn3;
 } tnk_tc_plan;
 
 /* out = H_eff theta (FP64 canonical buffers) through the tensor cores: stage theta, two tcgen05
@@ -258,10 +260,17 @@ int tnk_stage_f32(const tnk_cvt_task* tasks, const tnk_cvt_item* items, int64_t 
 /* Encode n 2-D FP32 tensor maps (host side; needs the CUDA driver): desc4 holds (element offset
  * from `base`, rows, cols, row stride) per map; out receives n * 128 bytes. */
 int tnk_tc_encode_tmaps(const float* base, const int64_t* desc4, int64_t n, void* out);
+/* The same with a fifth column per map: the box rows (128, or 64 for the B operands of a stage
+ * run with 128 x 64 tiles). */
+int tnk_tc_encode_tmaps_box(const float* base, const int64_t* desc5, int64_t n, void* out);
 /* One tensor-core grouped GEMM stage (flags bit 1 of a task: FP64 output, else FP32). */
 int tnk_grouped_gemm_tc(const tnk_gemm_task* tasks, const tnk_tc_seg* segs,
                         const tnk_gemm_tile* tiles, int64_t n_tiles, const void* maps, void* C,
                         int* err, int32_t passes, void* stream);
+/* The same with 128 x bn tiles (bn = 128 or 64; B maps with boxes of bn rows). */
+int tnk_grouped_gemm_tc_bn(const tnk_gemm_task* tasks, const tnk_tc_seg* segs,
+                           const tnk_gemm_tile* tiles, int64_t n_tiles, const void* maps,
+                           void* C, int* err, int32_t passes, int32_t bn, void* stream);
 /* Stage 2 on FP32 data (hi/lo split of the result when `split`). */
 int tnk_combine_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
                     const tnk_comb_item* items, int64_t n_items, const float* src, float* dst,

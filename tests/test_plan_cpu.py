@@ -181,3 +181,23 @@ def test_split_k_stage_balances_and_matches():
     work = (kc[t["seg_end"]] - kc[t["seg_begin"]]) * np.minimum(64, t["m"]) * np.minimum(64, t["n"])
     tot = float((work * (-(-t["m"] // 64)) * (-(-t["n"] // 64))).sum())
     assert work.max() <= 2.0 * tot / P.SLOTS
+
+
+def test_tensor_core_stage3_tile_width():
+    """A stage 3 with fewer 128 x 128 tiles than SMs runs 128 x 64 tiles: every output block is
+    covered exactly once, and exactly the maps of stage 3's B operands get 64-row boxes."""
+    from tnkit_gb300 import workloads
+    th, L, W1, W2, R = workloads.mid_bond_problem(device="cpu")
+    hp = P.plan_apply(th.layout, L.layout, [(W1.layout, W1.host), (W2.layout, W2.host)], R.layout)
+    tc = P.HostPlanTC(hp, th.layout, L.layout, R.layout)
+    assert len(P._tiles(tc.t3, tc.s3, P.TC_TILE)) < P.TC_FILL and tc.bn3 == 64
+    for k, t in enumerate(tc.t3):
+        mine = tc.tiles3[tc.tiles3["task"] == k]
+        cells = {(int(a), int(b)) for a, b in zip(mine["m0"], mine["n0"])}
+        want = {(a, b) for a in range(0, int(t["m"]), 128) for b in range(0, int(t["n"]), 64)}
+        assert cells == want and len(mine) == len(want)
+    d = tc.map_desc_box()
+    b3 = set(tc.s3["b_map"].tolist())
+    for i in range(len(tc.maps)):
+        assert d[2 * i, 4] == d[2 * i + 1, 4] == (64 if i in b3 else 128)
+    assert np.array_equal(d[:, :4], tc.map_desc())

@@ -90,7 +90,7 @@ class TcPlan(C.Structure):
                 ("n_tiles3", C.c_int64),
                 ("maps", C.c_void_p), ("stage", C.c_void_p), ("lo_off", C.c_int64),
                 ("y32", C.c_void_p), ("err", C.c_void_p), ("passes", C.c_int32),
-                ("pad", C.c_int32)]
+                ("bn3", C.c_int32)]
 
 
 _P, _I64, _I32, _D = C.c_void_p, C.c_int64, C.c_int32, C.c_double
@@ -129,7 +129,9 @@ _SIGS = {
     "tnk_apply_two_site_tc": ([_P, _P, _P, _P], C.c_int),
     "tnk_stage_f32": ([_P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
     "tnk_tc_encode_tmaps": ([_P, _P, _I64, _P], C.c_int),
+    "tnk_tc_encode_tmaps_box": ([_P, _P, _I64, _P], C.c_int),
     "tnk_grouped_gemm_tc": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _P], C.c_int),
+    "tnk_grouped_gemm_tc_bn": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _I32, _P], C.c_int),
     "tnk_combine_f32": ([_P, _P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
     "tnk_ff_split": ([_P, _P, _I64, _P], C.c_int),
     "tnk_contract3_ff": ([_P, _P, _P, _P, _P, _P, _I64, _P], C.c_int),

@@ -29,10 +29,10 @@ static_assert(sizeof(TcSeg) == 16, "TcSeg layout");
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int BM = 128, BK = 32;
 constexpr int STAGES = 3;
 constexpr int NT = 128;
-constexpr int TILE_BYTES = BM * BK * 4;     // 16 KiB (BN == BM)
+constexpr int TILE_BYTES = BM * BK * 4;     // 16 KiB: one A tile (and a B tile of 128 rows)
 constexpr unsigned WAIT_LIMIT = 1u << 26;   // tries per mbarrier wait (well over a second)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -94,16 +94,20 @@ __device__ __forceinline__ uint64_t smem_desc(const void* p) {
     return d;
 }
 
-// Instruction descriptor of kind::tf32: D = F32, A = B = TF32, both K-major, M = 128, N = 128.
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptor of kind::tf32: D = F32, A = B = TF32, both K-major, M = 128, N = BNT.
+template <int BNT>
+__host__ __device__ constexpr uint32_t idesc_tf32() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BNT >> 3) << 17) |
+           ((uint32_t)(BM >> 4) << 24);
+}
 
+template <int BNT>
 __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+        "l"(a), "l"(b), "r"(idesc_tf32<BNT>()), "r"(acc)
         : "memory");
 }
 
@@ -139,20 +143,25 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parit
 // of the tensor core without either thread waiting on its own work. After the last MMA all four
 // warps move the accumulator out: TMEM -> registers (32 columns per tcgen05.ld) -> a padded
 // shared-memory tile (the operand ring, idle by then) -> global memory row by row, 32
-// consecutive columns per store instruction.
-template <int PASSES>
+// consecutive columns per store instruction. BNT is the tile width (128, or 64 for stages with
+// few, long tasks: twice the CTAs at half the work each), with B tiles of BNT rows.
+template <int PASSES, int BNT>
 __global__ void __launch_bounds__(NT, 1)
 gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict__ segs,
                const tnk_gemm_tile* __restrict__ tiles, const CUtensorMap* __restrict__ maps,
                void* __restrict__ Cout, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
-    constexpr int NTILE = (PASSES == 3) ? 4 : 2;        // Ah, Bh (, Al, Bl) per stage
-    constexpr int LDS = BN + 1;                         // staging row stride (floats)
-    static_assert(BM * LDS * 4 <= STAGES * NTILE * TILE_BYTES, "staging tile fits the ring");
+    constexpr int A_BYTES = TILE_BYTES;                 // 128 x 32 FP32
+    constexpr int B_BYTES = BNT * BK * 4;               // BNT x 32 FP32 (a multiple of 1 KiB)
+    constexpr int PAIR = A_BYTES + B_BYTES;
+    constexpr int STAGE_BYTES = (PASSES == 3) ? 2 * PAIR : PAIR;  // Ah, Bh (, Al, Bl)
+    constexpr int LDS = BNT + 1;                        // staging row stride (floats)
+    static_assert(BM * LDS * 4 <= STAGES * STAGE_BYTES, "staging tile fits the ring");
+    static_assert(B_BYTES % 1024 == 0, "B tiles keep the 1 KiB swizzle alignment");
     uint8_t* base = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* stage_mem = base;
-    uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * NTILE * TILE_BYTES);
+    uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
     uint64_t* empty = full + STAGES;
     uint64_t* done = empty + STAGES;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
@@ -166,7 +175,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
-                     "r"(BN)
+                     "r"(BNT)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -210,13 +219,14 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                     tmap_acquire(&maps[2 * g.b_map + 1]);
                 }
             }
-            uint8_t* st = stage_mem + slot * NTILE * TILE_BYTES;
-            mbar_expect_tx(&full[slot], NTILE * TILE_BYTES);
+            uint8_t* st = stage_mem + slot * STAGE_BYTES;
+            mbar_expect_tx(&full[slot], STAGE_BYTES);
             tma_load_2d(st, &maps[2 * g.a_map], &full[slot], lk, tile.m0);
-            tma_load_2d(st + TILE_BYTES, &maps[2 * g.b_map], &full[slot], lk, tile.n0);
+            tma_load_2d(st + A_BYTES, &maps[2 * g.b_map], &full[slot], lk, tile.n0);
             if (PASSES == 3) {
-                tma_load_2d(st + 2 * TILE_BYTES, &maps[2 * g.a_map + 1], &full[slot], lk, tile.m0);
-                tma_load_2d(st + 3 * TILE_BYTES, &maps[2 * g.b_map + 1], &full[slot], lk, tile.n0);
+                tma_load_2d(st + PAIR, &maps[2 * g.a_map + 1], &full[slot], lk, tile.m0);
+                tma_load_2d(st + PAIR + A_BYTES, &maps[2 * g.b_map + 1], &full[slot], lk,
+                            tile.n0);
             }
             lk += BK;
             ++issued;
@@ -233,17 +243,17 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            uint8_t* st = stage_mem + slot * NTILE * TILE_BYTES;
+            uint8_t* st = stage_mem + slot * STAGE_BYTES;
 #pragma unroll
             for (int kk = 0; kk < BK / 8; ++kk) {
                 const uint64_t ah = smem_desc(st + kk * 32);
-                const uint64_t bh = smem_desc(st + TILE_BYTES + kk * 32);
-                mma_tf32(tmem, ah, bh, (i > 0 || kk > 0) ? 1u : 0u);
+                const uint64_t bh = smem_desc(st + A_BYTES + kk * 32);
+                mma_tf32<BNT>(tmem, ah, bh, (i > 0 || kk > 0) ? 1u : 0u);
                 if (PASSES == 3) {
-                    const uint64_t al = smem_desc(st + 2 * TILE_BYTES + kk * 32);
-                    const uint64_t bl = smem_desc(st + 3 * TILE_BYTES + kk * 32);
-                    mma_tf32(tmem, ah, bl, 1u);
-                    mma_tf32(tmem, al, bh, 1u);
+                    const uint64_t al = smem_desc(st + PAIR + kk * 32);
+                    const uint64_t bl = smem_desc(st + PAIR + A_BYTES + kk * 32);
+                    mma_tf32<BNT>(tmem, ah, bl, 1u);
+                    mma_tf32<BNT>(tmem, al, bh, 1u);
                 }
             }
             mma_commit(&empty[slot]);
@@ -270,7 +280,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     // epilogue: warp w owns accumulator rows 32w..32w+31 (its TMEM lane quarter)
     float* stg = reinterpret_cast<float*>(stage_mem);
     const int rloc = warp * 32 + lane;
-    for (int c0 = 0; c0 < BN; c0 += 32) {
+    for (int c0 = 0; c0 < BNT; c0 += 32) {
         uint32_t v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0u;
@@ -296,13 +306,13 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     if (!bad) {
         const bool f64 = (task.flags & 2) != 0;
         const int rows = min(32, task.m - (tile.m0 + warp * 32));
-        const int cols = min(BN, task.n - tile.n0);
+        const int cols = min(BNT, task.n - tile.n0);
         for (int r = 0; r < rows; ++r) {
             const int row = tile.m0 + warp * 32 + r;
             const int64_t rbase = task.c_off + (int64_t)row * task.ldc + tile.n0;
             const float* src = stg + (warp * 32 + r) * LDS;
 #pragma unroll
-            for (int q = 0; q < BN / 32; ++q) {
+            for (int q = 0; q < BNT / 32; ++q) {
                 const int col = q * 32 + lane;
                 if (col < cols) {
                     const float x = src[col];
@@ -318,23 +328,41 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(BN)
+                     "r"(BNT)
                      : "memory");
     }
 }
 
-constexpr size_t smem_bytes(int passes) {
-    return 1024 + (size_t)STAGES * ((passes == 3) ? 4 : 2) * TILE_BYTES + 256;
+constexpr size_t smem_bytes(int passes, int bn) {
+    return 1024 + (size_t)STAGES * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) + 256;
     // (1024: alignment slack of the ring; 256: barriers, TMEM slot, abort flag, counters)
+}
+
+template <int PASSES, int BNT>
+int launch_tc_t(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
+                int64_t n_tiles, const void* maps, void* C, int* err, cudaStream_t stream) {
+    const size_t sm = smem_bytes(PASSES, BNT);
+    cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<PASSES, BNT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) {
+        set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
+        return TNK_ERR_CUDA;
+    }
+    gemm_tc_kernel<PASSES, BNT><<<(unsigned)n_tiles, NT, sm, stream>>>(
+        tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
+    return check_launch("gemm_tc_kernel");
 }
 
 }  // namespace
 
+// bn: the tile width of this stage, 128 or 64; the B operand maps must have boxes of bn rows.
 int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
-                   int64_t n_tiles, const void* maps, void* C, int* err, int passes,
+                   int64_t n_tiles, const void* maps, void* C, int* err, int passes, int bn,
                    cudaStream_t stream) {
-    if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3)) {
-        set_error("tc gemm: bad tile count %lld or passes %d", (long long)n_tiles, passes);
+    if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3) ||
+        (bn != 128 && bn != 64)) {
+        set_error("tc gemm: bad tile count %lld, passes %d or tile width %d", (long long)n_tiles,
+                  passes, bn);
         return TNK_ERR_ARG;
     }
     if (n_tiles == 0) return TNK_OK;
@@ -346,28 +374,11 @@ int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm
         set_error("tc gemm: tensor maps must be 64-byte aligned");
         return TNK_ERR_ARG;
     }
-    const size_t sm = smem_bytes(passes);
-    cudaError_t e;
-    if (passes == 3) {
-        e = cudaFuncSetAttribute(gemm_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sm);
-        if (e != cudaSuccess) {
-            set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
-            return TNK_ERR_CUDA;
-        }
-        gemm_tc_kernel<3><<<(unsigned)n_tiles, NT, sm, stream>>>(
-            tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
-    } else {
-        e = cudaFuncSetAttribute(gemm_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sm);
-        if (e != cudaSuccess) {
-            set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
-            return TNK_ERR_CUDA;
-        }
-        gemm_tc_kernel<1><<<(unsigned)n_tiles, NT, sm, stream>>>(
-            tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
-    }
-    return check_launch("gemm_tc_kernel");
+    if (passes == 3)
+        return bn == 128 ? launch_tc_t<3, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
+                         : launch_tc_t<3, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
+    return bn == 128 ? launch_tc_t<1, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
+                     : launch_tc_t<1, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
 }
 
 // --------------------------------------------------------------------------------------------
@@ -392,7 +403,7 @@ static EncodeTiledFn get_encoder() {
     return fn;
 }
 
-int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out) {
+int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out, int ncol) {
     EncodeTiledFn enc = get_encoder();
     if (!enc) {
         set_error("tensor maps: cuTensorMapEncodeTiled is unavailable");
@@ -400,8 +411,14 @@ int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out) {
     }
     CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(out);
     for (int64_t i = 0; i < n; ++i) {
-        const int64_t off = desc[4 * i], rows = desc[4 * i + 1], cols = desc[4 * i + 2],
-                      ld = desc[4 * i + 3];
+        const int64_t off = desc[ncol * i], rows = desc[ncol * i + 1],
+                      cols = desc[ncol * i + 2], ld = desc[ncol * i + 3];
+        const int64_t box_rows = ncol > 4 ? desc[ncol * i + 4] : BM;
+        if (box_rows != 128 && box_rows != 64) {
+            set_error("tensor map %lld: box rows %lld (128 or 64)", (long long)i,
+                      (long long)box_rows);
+            return TNK_ERR_ARG;
+        }
         const float* p = base + off;
         if ((reinterpret_cast<uintptr_t>(p) & 15) != 0 || (ld * 4) % 16 != 0 || rows < 1 ||
             cols < 1 || ld < cols) {
@@ -411,7 +428,7 @@ int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out) {
         }
         cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
         cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
-        cuuint32_t box[2] = {BK, BM};
+        cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
         cuuint32_t estr[2] = {1, 1};
         CUresult r = enc(&maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)p, dims, strides,
                          box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,

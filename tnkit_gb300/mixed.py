@@ -62,11 +62,11 @@ class TwoSiteOperatorTC:
         self.y32 = torch.empty(max(tc.y32_elems, 1), dtype=torch.float32, device=dev)
         self.err = torch.zeros(16, dtype=torch.int32, device=dev)
         lib = _lib.lib()
-        desc = np.ascontiguousarray(tc.map_desc())
+        desc = np.ascontiguousarray(tc.map_desc_box())
         nmaps = desc.shape[0]
         maps_host = np.zeros(max(nmaps, 1) * 128, np.uint8)
-        _lib.check(lib.tnk_tc_encode_tmaps(self.stage.data_ptr(), desc.ctypes.data, nmaps,
-                                           maps_host.ctypes.data), "tnk_tc_encode_tmaps")
+        _lib.check(lib.tnk_tc_encode_tmaps_box(self.stage.data_ptr(), desc.ctypes.data, nmaps,
+                                               maps_host.ctypes.data), "tnk_tc_encode_tmaps")
         arrays = [maps_host, tc.cvt["T"], tc.cvt_items["T"], tc.t1, tc.s1, tc.tiles1, tc.t2,
                   tc.c2, tc.items2, tc.t3, tc.s3, tc.tiles3, tc.cvt["L"], tc.cvt_items["L"],
                   tc.cvt["R"], tc.cvt_items["R"]]
@@ -77,7 +77,7 @@ class TwoSiteOperatorTC:
                              a[6], a[7], a[8], len(tc.items2),
                              a[9], a[10], a[11], len(tc.tiles3),
                              a[0], self.stage.data_ptr(), tc.stage_elems,
-                             self.y32.data_ptr(), self.err.data_ptr(), passes, 0)
+                             self.y32.data_ptr(), self.err.data_ptr(), passes, tc.bn3)
         sp = _lib.stream_ptr()
         split = 1 if passes == 3 else 0
         _lib.check(lib.tnk_stage_f32(a[12], a[13], len(tc.cvt_items["L"]), L_data.data_ptr(),

@@ -1111,6 +1111,7 @@ def two_site_ref_macs(theta: Layout, L: Layout, W1: Layout, W2: Layout, R: Layou
 # tensor-core (tcgen05, TF32) version of the two-site plan
 # --------------------------------------------------------------------------- #
 TC_TILE = 128             # must match gemm_tc.cu
+TC_FILL = 152             # SMs: a stage with fewer 128 x 128 tiles than this uses 128 x 64
 TC_ALIGN = 32             # staged block bases: 32 floats = 128 bytes (TMA needs 16)
 
 
@@ -1130,15 +1131,16 @@ def _grid_items(rows, cols, step_r, step_c):
     return tid, (local // tc[tid]) * step_r[tid], (local % tc[tid]) * step_c
 
 
-def _tiles(tasks, segs, tile):
-    """Every (task, m0, n0) tile, ordered by decreasing K (stable)."""
+def _tiles(tasks, segs, tile, tile_n=None):
+    """Every (task, m0, n0) tile of tile x tile_n (default square), ordered by decreasing K
+    (stable)."""
     if len(tasks) == 0:
         return np.zeros(0, GEMM_TILE)
     kcum = np.concatenate([[0], np.cumsum(segs["k"].astype(np.int64))]) if len(segs) else \
         np.zeros(1, np.int64)
     ktot = kcum[tasks["seg_end"]] - kcum[tasks["seg_begin"]]
     ktot = np.where(ktot == 0, 1, ktot)
-    tid, m0, n0 = _grid_items(tasks["m"], tasks["n"], tile, tile)
+    tid, m0, n0 = _grid_items(tasks["m"], tasks["n"], tile, tile if tile_n is None else tile_n)
     order = np.argsort(-ktot[tid], kind="stable")
     tl = np.zeros(len(tid), GEMM_TILE)
     tl["task"], tl["m0"], tl["n0"] = tid[order], m0[order], n0[order]
@@ -1173,6 +1175,17 @@ class HostPlanTC:
             self._python(t1, s1, t2, t3, s3)
         self.tiles1 = _tiles(self.t1, self.s1, TC_TILE)
         self.tiles3 = _tiles(self.t3, self.s3, TC_TILE)
+        # stage 3 (few output blocks, long K) in 128 x 64 tiles when its 128 x 128 tiles do not
+        # fill the SMs, provided its B operand maps (the staged R blocks) serve no other role:
+        # their boxes become 64 rows
+        self.bn3 = 128
+        b3 = set(self.s3["b_map"].tolist()) if len(self.s3) else set()
+        other = set(self.s1["a_map"].tolist()) | set(self.s1["b_map"].tolist()) | \
+            set(self.s3["a_map"].tolist())
+        if 0 < len(self.tiles3) < TC_FILL and not (b3 & other):
+            self.bn3 = 64
+            self.tiles3 = _tiles(self.t3, self.s3, TC_TILE, 64)
+        self._b3 = b3
         self.c2, self.items2 = c2, i2
         self.cvt_items = {k: _cvt_items(v) for k, v in self.cvt.items()}
         self.stage_elems = _rup(self.cursor, TC_ALIGN)    # hi region; lo at +stage_elems
@@ -1293,6 +1306,19 @@ class HostPlanTC:
         d[0::2] = m
         d[1::2] = m
         d[1::2, 0] += self.stage_elems
+        return d
+
+    def map_desc_box(self) -> np.ndarray:
+        """map_desc with a fifth column, the box rows of each map: 64 for stage 3's B operands
+        when stage 3 runs 128 x 64 tiles, else 128."""
+        d4 = self.map_desc()
+        d = np.zeros((len(d4), 5), np.int64)
+        d[:, :4] = d4
+        d[:, 4] = TC_TILE
+        if getattr(self, "bn3", TC_TILE) != TC_TILE and self._b3:
+            idx = np.asarray(sorted(self._b3), np.int64)
+            d[2 * idx, 4] = self.bn3
+            d[2 * idx + 1, 4] = self.bn3
         return d
 
 
