@@ -187,17 +187,19 @@ def _svd_gram_native(M: torch.Tensor, orth: int = 0):
 
 
 # --- host co-processing of the truncation -----------------------------------------------------
-# A chi=1024 bond's two or three largest sectors (~500 rows) are latency-bound in cuSOLVER (a
-# 522-row syevd is ~14 ms and two of them barely overlap), while the host's cores are idle
-# during the truncation. Sectors are split between the GPU path and host LAPACK (numpy, the
-# reference's own numpy branch of method='gram') by a greedy makespan on measured costs; numpy
-# releases the interpreter lock inside LAPACK. The host library's thread count is lowered to a
-# quarter of the cores for the duration (with more, its threads and cuSOLVER's host work slow
-# each other down).
-_GPU_MS_PER_ROW = 14.0 / 522          # cuSOLVER path: ~linear in n (latency-bound)
-_HOST_MS_522 = 28.6                   # numpy path with a quarter of the cores: ~n^2.1
-_HOST_MODE = "parallel"               # host sectors: 'parallel' (a worker each) or 'queue'
-_HOST_THREADS_DIV = 4                 # host library threads during the truncation: cores / this
+# A chi=1024 bond's largest sectors (~520 rows) are latency-bound in cuSOLVER: one Gram
+# factorisation takes ~17 ms, and calls on several streams do not overlap (the GPU path is one
+# lane). The host's cores are idle during the truncation, and host LAPACK calls from several
+# threads do run side by side when each uses a share of the cores. So sectors are scheduled over
+# one GPU lane and _HOST_LANES host lanes (numpy, the reference's own numpy branch of
+# method='gram'; numpy releases the interpreter lock inside LAPACK), longest first, each to the
+# lane that finishes it first, on costs measured on GB300 and its Grace host (522 rows: 17.3 ms
+# on the GPU path, 14.0 ms on the host path with 4 of the 16 cores). Each host lane runs its
+# sectors one after another with cores / _HOST_LANES library threads.
+_GPU_MS_PER_ROW = 17.3 / 522          # cuSOLVER Gram path: ~linear in n (latency-bound)
+_HOST_MS_522 = 14.0                   # host Gram path with cores / _HOST_LANES threads: ~n^2.1
+_HOST_LANES = 4                       # host sectors in flight at once
+_HOST_THREADS_DIV = _HOST_LANES       # host library threads per lane: cores / this
 _HOST_BLAS = {"lib": None, "tried": False}
 
 
@@ -222,38 +224,43 @@ def _host_blas():
     return _HOST_BLAS["lib"]
 
 
-def _map_hybrid(fns, mats, on_host, device):
-    """fns[i](mats[i]) for every sector: the GPU sectors one stream and worker each, the host
-    sectors (_HOST_MODE 'queue') one after another, largest first, in a single worker whose
-    LAPACK calls use the host library's threads; 'parallel' gives them a worker each too."""
-    if _HOST_MODE != "queue":
-        return _concurrent().map(fns, mats, device)
-    gpu = [i for i, h in enumerate(on_host) if not h]
-    host = sorted((i for i, h in enumerate(on_host) if h), key=lambda i: -min(mats[i].shape))
-    items = [fns[i] for i in gpu] + [lambda _: [fns[i](mats[i]) for i in host]]
-    res = _concurrent().map(items, [mats[i] for i in gpu] + [None], device)
+def _map_hybrid(fns, mats, lanes, device):
+    """fns[i](mats[i]) for every sector: each GPU sector (lane -1) on its own stream and worker,
+    each host lane's sectors one after another, largest first, in one worker per lane."""
+    gpu = [i for i, l in enumerate(lanes) if l < 0]
+    order = sorted(range(len(mats)), key=lambda i: -min(mats[i].shape))
+    host = [[i for i in order if lanes[i] == k] for k in range(max(lanes, default=-1) + 1)]
+    host = [ix for ix in host if ix]
+    items = [fns[i] for i in gpu] + [lambda _, ix=ix: [fns[i](mats[i]) for i in ix]
+                                     for ix in host]
+    res = _concurrent().map(items, [mats[i] for i in gpu] + [None] * len(host), device)
     out = [None] * len(mats)
     for i, r in zip(gpu, res[:len(gpu)]):
         out[i] = r
-    for i, r in zip(host, res[-1]):
-        out[i] = r
+    for ix, rs in zip(host, res[len(gpu):]):
+        for i, r in zip(ix, rs):
+            out[i] = r
     return out
 
 
-def _assign_sectors(shapes, host_ok: bool):
-    """Per sector True for the host path: greedy over sectors by decreasing size, each to the
-    side (a queue each) that finishes it first."""
-    if not host_ok or len(shapes) < 2:
-        return [False] * len(shapes)
+def _assign_sectors(shapes, host_ok: bool, gpu_ok: bool = True):
+    """Per sector its lane: -1 for the GPU path, 0.._HOST_LANES-1 for a host lane. Longest
+    processing time first: sectors by decreasing size, each to the lane that finishes it
+    first (the GPU lane alone when the host path is unavailable, host lanes alone when
+    gpu_ok is False)."""
+    if not host_ok or (gpu_ok and len(shapes) < 2):
+        return [-1] * len(shapes)
     order = sorted(range(len(shapes)), key=lambda i: -min(shapes[i]))
-    t_gpu = t_host = 0.0
-    out = [False] * len(shapes)
+    t_gpu, t_host = 0.0, [0.0] * _HOST_LANES
+    out = [-1] * len(shapes)
     for i in order:
         n = min(shapes[i])
         g = _GPU_MS_PER_ROW * n + 0.4
         h = _HOST_MS_522 * (n / 522.0) ** 2.1 + 0.05
-        if t_host + h < t_gpu + g:
-            out[i], t_host = True, t_host + h
+        k = min(range(_HOST_LANES), key=lambda j: t_host[j])
+        if not gpu_ok or t_host[k] + h < t_gpu + g:
+            out[i] = k
+            t_host[k] += h
         else:
             t_gpu += g
     return out
@@ -383,19 +390,22 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     if len(mats) > 1 and m.data.is_cuda:
         if method == "gram" and fn is _svd_gram_native and host != "never":
             blas = _host_blas()
-            on_host = _assign_sectors([tuple(M.shape) for M in mats], blas is not None) \
-                if host == "auto" else [True] * len(mats)
-            fns = [pick(M, _svd_gram_host if h else _svd_gram_native)
-                   for M, h in zip(mats, on_host)]
+            shapes = [tuple(M.shape) for M in mats]
+            lanes = _assign_sectors(shapes, blas is not None) if host == "auto" else \
+                _assign_sectors(shapes, True, gpu_ok=False)
+            fns = [pick(M, _svd_gram_host if l >= 0 else _svd_gram_native)
+                   for M, l in zip(mats, lanes)]
             if low:
                 fns = [_with_fp64_fallback(f) for f in fns]
-            if any(on_host) and blas is not None:
+            if any(l >= 0 for l in lanes) and blas is not None:
                 prev = blas[1]()
                 blas[0](max(1, prev // _HOST_THREADS_DIV))
                 try:
-                    facs = _map_hybrid(fns, mats, on_host, m.data.device)
+                    facs = _map_hybrid(fns, mats, lanes, m.data.device)
                 finally:
                     blas[0](prev)
+            elif any(l >= 0 for l in lanes):
+                facs = _map_hybrid(fns, mats, lanes, m.data.device)
             else:
                 facs = _concurrent().map(fns, mats, m.data.device)
         else:
@@ -452,21 +462,22 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
         blas = _host_blas() if host != "never" else None
         # host='always' factors every sector with host LAPACK whether or not the library's
         # thread control was found (as truncated_svd does); 'auto' needs that control to split
-        on_host = ([True] * len(mats) if host == "always" else
-                   [False] * len(mats) if blas is None else
-                   _assign_sectors([sh for sh, _ in shapes], True))
-        fns = [_gram_pick(sc)(M, _svd_gram_host if h else _svd_gram_native)
-               if sc in ("right", "left") else (_svd_gram_host if h else _svd_gram_native)
-               for M, (_, sc), h in zip(mats, shapes, on_host)]
-        if any(on_host) and blas is not None:
+        sh = [s_ for s_, _ in shapes]
+        lanes = (_assign_sectors(sh, True, gpu_ok=False) if host == "always" else
+                 [-1] * len(mats) if blas is None else _assign_sectors(sh, True))
+        fns = [_gram_pick(sc)(M, _svd_gram_host if l >= 0 else _svd_gram_native)
+               if sc in ("right", "left") else (_svd_gram_host if l >= 0 else _svd_gram_native)
+               for M, (_, sc), l in zip(mats, shapes, lanes)]
+        on_host = any(l >= 0 for l in lanes)
+        if on_host and blas is not None:
             prev = blas[1]()
             blas[0](max(1, prev // _HOST_THREADS_DIV))
             try:
-                facs = _map_hybrid(fns, mats, on_host, mats[0].device)
+                facs = _map_hybrid(fns, mats, lanes, mats[0].device)
             finally:
                 blas[0](prev)
-        elif any(on_host):
-            facs = _map_hybrid(fns, mats, on_host, mats[0].device)
+        elif on_host:
+            facs = _map_hybrid(fns, mats, lanes, mats[0].device)
         elif len(mats) > 1:
             facs = _concurrent().map(fns, mats, mats[0].device)
         else:
