@@ -130,14 +130,46 @@ def test_float_float_env_updates_match_fp64(scale):
         assert _rel(got, ref) <= 1e-13, (f.__name__, _rel(got, ref))
 
 
-@pytest.mark.parametrize("prec,polish", [("mixed-ff", 2), ("mixed-ff", 1), ("mixed", 1)])
-def test_sweep_schedule_reaches_fp64_energy(prec, polish):
+@pytest.mark.parametrize("prec,polish,mode", [("mixed-ff", 2, "lanczos"),
+                                              ("mixed-ff", 1, "lanczos"),
+                                              ("mixed", 1, "lanczos"), ("mixed", 1, "refine"),
+                                              ("mixed-ff", 1, "refine")])
+def test_sweep_schedule_reaches_fp64_energy(prec, polish, mode):
     """mixed_schedule='sweep': the opening sweeps on the tensor cores alone, the last one or two
-    polished (float-float or FP64), end within 1e-10 of the FP64 run's energy."""
+    polished (float-float or FP64; by Lanczos, or by defect correction with tensor-core
+    correction solves), end within 1e-10 of the FP64 run's energy."""
     from tnkit_gb300.dmrg import dmrg
     kw = dict(charge=0, seed=1, n_sweeps=6, tol=0, rtol=0, expand=0)
     E64, _, _ = dmrg(_xxz_blocks(32), 64, **kw)
     E, M, info = dmrg(_xxz_blocks(32), 64, precision=prec, mixed_schedule="sweep",
-                      polish_sweeps=polish, **kw)
+                      polish_sweeps=polish, polish_mode=mode, **kw)
     assert info["mixed_counts"]["lo"] > info["mixed_counts"]["hi"] > 0
     assert abs(E - E64) <= 1e-10, (E, E64)              # absolute, as the target states
+
+
+def test_refine_ground_reaches_fp64_eigenpair():
+    """Defect correction with the tensor-core operator as the inner solver reaches the FP64
+    ground state of a small U(1) local problem made symmetric, (H + H^T) / 2, in a few outer
+    steps, from a start 1e-3 away."""
+    from tnkit_gb300 import ops, workloads
+    from tnkit_gb300.mixed import TwoSiteOperatorTC, refine_ground
+    th, L, W1, W2, R = workloads.mid_bond_problem(dims=(2, 6, 10, 6, 2),
+                                                  charges=(-4, -2, 0, 2, 4), seed=4)
+    n = th.layout.size
+    op = ops.TwoSiteOperator(th.layout, L, W1, W2, R)
+    tc = TwoSiteOperatorTC(th.layout, L, W1, W2, R)
+    # a dense symmetric stand-in built from the operator, for the reference eigenpair
+    E = torch.eye(n, dtype=torch.float64, device="cuda")
+    H = torch.stack([op(E[:, j].contiguous()) for j in range(n)], 1) if n <= 4000 else None
+    if H is None:
+        pytest.skip("problem too large for the dense check")
+    Hs = 0.5 * (H + H.T)
+    ev, evec = torch.linalg.eigh(Hs)
+    sym64 = lambda x, out: out.copy_(Hs @ x)
+    sym_lo = lambda x, out: out.copy_(0.5 * (tc(x) + (H.T @ x)))      # ~1e-6 away from Hs
+    x0 = evec[:, 0] + 1e-3 * torch.randn(n, dtype=torch.float64, device="cuda")
+    th_, x, info = refine_ground(sym64, sym_lo, x0, tol=1e-10)
+    tc.check_device_error()
+    assert info["residual"] < 1e-10 and info["outer"] <= 3, info
+    assert abs(th_ - float(ev[0])) <= 1e-12 * abs(float(ev[0]))
+    assert abs(abs(float(torch.dot(x, evec[:, 0]))) - 1.0) <= 1e-10

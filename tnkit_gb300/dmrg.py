@@ -59,6 +59,10 @@ class DMRGOptions:
                                      # 'sweep': tensor-core solves alone in all but the last
                                      # `polish_sweeps` sweeps, the per-bond mixed solve there
     polish_sweeps: int = 2
+    polish_mode: str = "lanczos"          # mixed modes: 'lanczos' (high-precision Lanczos from the
+                                          # tensor-core vector) or 'refine' (defect correction:
+                                          # high-precision residuals, tensor-core correction
+                                          # solves, Lanczos only if still above eig_tol)
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
     svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
@@ -213,7 +217,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
             e, x, info = mixed_ground(theta.layout, L[i], W[i], W[i + 1], R[i + 2], op, v0,
                                       tol=o.eig_tol, max_iter=mi, m=o.restart_m,
                                       k=o.restart_k, tol_lo=o.mixed_tol_lo, basis=Vb,
-                                      counts=counts, tc_only=tc_only)
+                                      counts=counts, tc_only=tc_only,
+                                      polish_mode=o.polish_mode)
         else:
             e, x, info = lanczos_ground_restart(op, v0, tol=o.eig_tol, max_iter=mi,
                                                 m=o.restart_m, k=o.restart_k, basis=Vb)

@@ -140,11 +140,64 @@ def _fp64_residual(op64, v: torch.Tensor):
     return _scalars(v.device).residual(v, op64(v))
 
 
+def refine_ground(op64, op_lo, x: torch.Tensor, tol: float, outer: int = 3, inner: int = 24,
+                  check: int = 8, inner_tol: float = 1e-3):
+    """Polish an approximate lowest eigenvector of H by defect correction: every outer step
+    computes the residual r = H x - theta x in high precision (one matvec of `op64`, FP64 or
+    float-float, theta the Rayleigh quotient) and solves the Jacobi-Davidson correction
+    equation (I - x x^T)(H - theta)(I - x x^T) t = -r, t orthogonal to x, approximately with
+    the cheap operator `op_lo` (the tensor-core matvec, ~1e-6 relative) by conjugate gradients
+    (the projected operator is positive definite on x's complement once theta is below the
+    second eigenvalue), then x <- (x + t) / ||x + t||. The error the cheap operator leaves in t
+    is ~ ||H - H_lo|| / gap of t, so each outer step gains ~5 orders of magnitude; the FP64
+    residual decides when to stop (Jacobi-Davidson: Sleijpen and van der Vorst, SIAM J. Matrix
+    Anal. Appl. 17 (1996) 401; mixed-precision refinement of eigenpairs in the same spirit).
+    CG's scalars stay on the device; its residual is read every `check` steps.
+    Returns (theta, x, info) with info['residual'] the last FP64 residual norm (x unit norm)."""
+    x = x / torch.linalg.vector_norm(x)
+    y = torch.empty_like(x)
+    hi = lo = 0
+    theta, rn = 0.0, float("inf")
+    for it in range(outer + 1):
+        op64(x, y)
+        hi += 1
+        th = torch.dot(x, y)
+        r = y - th * x
+        rn = float(torch.linalg.vector_norm(r))
+        theta = float(th)
+        if rn < tol or it == outer or not np.isfinite(rn):
+            break
+        # CG on the projected correction equation, every vector orthogonal to x
+        t = torch.zeros_like(x)
+        res = -r
+        res -= torch.dot(x, res) * x
+        p = res.clone()
+        rr = torch.dot(res, res)
+        q = torch.empty_like(x)
+        for j in range(inner):
+            op_lo(p, q)
+            lo += 1
+            q -= th * p
+            q -= torch.dot(x, q) * x
+            pq = torch.dot(p, q)
+            alpha = rr / pq
+            t += alpha * p
+            res -= alpha * q
+            rr_new = torch.dot(res, res)
+            if (j + 1) % check == 0 and float(rr_new) ** 0.5 < inner_tol * rn:
+                break
+            p = res + (rr_new / rr) * p
+            rr = rr_new
+        x = x + t
+        x = x / torch.linalg.vector_norm(x)
+    return theta, x, {"residual": rn, "n_hi": hi, "n_lo": lo, "outer": it}
+
+
 def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: BlockTensor,
                  R: BlockTensor, op64, v0: torch.Tensor, tol: float = 1e-9,
                  max_iter: int = 200, m: int = 40, k: int = 10, tol_lo: float = 1e-4,
                  basis=None, counts=None, passes: int = 3, polish: Optional[int] = None,
-                 switch: float = 10.0, tc_only: bool = False):
+                 switch: float = 10.0, tc_only: bool = False, polish_mode: str = "lanczos"):
     """Lowest eigenpair of H_eff: tensor-core Lanczos to tol_lo, then FP64 Lanczos to tol.
 
     The warm start's FP64 residual is checked first (one FP64 matvec): a start already within
@@ -154,7 +207,13 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
     many iterations on the tensor cores.
 
     tc_only=True runs the tensor-core stage alone (to tol_lo, or until its residual stalls) and
-    returns its vector: the local solve of the opening sweeps of the 'sweep' schedule."""
+    returns its vector: the local solve of the opening sweeps of the 'sweep' schedule.
+
+    polish_mode='refine' polishes by defect correction (refine_ground: FP64 residuals,
+    tensor-core correction solves) before any high-precision Lanczos, which then runs only if
+    the residual is still above `tol` (and starts from the refined vector)."""
+    if polish_mode not in ("lanczos", "refine"):
+        raise ValueError("polish_mode must be 'lanczos' or 'refine'")
     if tc_only:
         op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
         e_lo, x32, info_lo = lanczos_ground_restart(
@@ -175,17 +234,26 @@ def mixed_ground(theta_layout: Layout, L: BlockTensor, W1: BlockTensor, W2: Bloc
         e, info_hi = th0, {"iters": 0, "converged": True}
         x = _scalars(v0.device).normalize_(v0.clone())
     else:
-        if r0 >= switch * tol_lo:
+        op_lo = None
+        if r0 >= switch * tol_lo or polish_mode == "refine":
             op_lo = TwoSiteOperatorTC(theta_layout, L, W1, W2, R, passes=passes)
+        if r0 >= switch * tol_lo:
             e_lo, x32, info_lo = lanczos_ground_restart(
                 _F32Vectors(op_lo, v0.numel(), v0.device), v0, tol=max(tol_lo, tol),
                 max_iter=max_iter, m=m, k=k, basis=basis, stall=8, dtype=torch.float32)
             op_lo.check_device_error()
-            n_lo = op_lo.calls
             x = x32.double()
-        e, x, info_hi = lanczos_ground_restart(op64, x, tol=tol,
-                                               max_iter=max_iter if polish is None else polish,
-                                               m=m, k=k, basis=basis)
+        info_hi = None
+        if polish_mode == "refine":
+            e, x, rinfo = refine_ground(op64, op_lo, x, tol)
+            op_lo.check_device_error()
+            if rinfo["residual"] < tol:
+                info_hi = {"iters": rinfo["outer"], "converged": True}
+        if info_hi is None:
+            e, x, info_hi = lanczos_ground_restart(op64, x, tol=tol,
+                                                   max_iter=max_iter if polish is None
+                                                   else polish, m=m, k=k, basis=basis)
+        n_lo = 0 if op_lo is None else op_lo.calls
     n_hi = getattr(op64, "calls", 0) - c0
     if counts is not None:
         counts["lo"] = counts.get("lo", 0) + n_lo
