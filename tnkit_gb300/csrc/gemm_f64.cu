@@ -15,6 +15,9 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 constexpr int PADA = BM + 1, PADB = BN + 1;
+// the DMMA tile's row stride: 68 doubles put the four k rows of a fragment load 8 banks apart,
+// so the 16 lanes of each half-warp read 16 distinct bank pairs
+constexpr int PADD = BM + 4;
 
 struct SegView {
     const double* a;
@@ -37,6 +40,7 @@ __device__ __forceinline__ void load_a(const SegView& s, int m0, int M, int k0, 
     }
 }
 
+template <int PAD = PADA>
 __device__ __forceinline__ void store_a(const SegView& s, int tid, const double (&ra)[4],
                                         double* As) {
     const bool kc = (s.a_cs == 1);
@@ -45,7 +49,7 @@ __device__ __forceinline__ void store_a(const SegView& s, int tid, const double 
         const int idx = tid + r * NT;
         const int mm = kc ? (idx >> 4) : (idx & (BM - 1));
         const int kk = kc ? (idx & (BK - 1)) : (idx >> 6);
-        As[kk * PADA + mm] = ra[r];
+        As[kk * PAD + mm] = ra[r];
     }
 }
 
@@ -62,6 +66,7 @@ __device__ __forceinline__ void load_b(const SegView& s, int n0, int N, int k0, 
     }
 }
 
+template <int PAD = PADB>
 __device__ __forceinline__ void store_b(const SegView& s, int tid, const double (&rb)[4],
                                         double* Bs) {
     const bool nc = (s.b_cs == 1);
@@ -70,7 +75,7 @@ __device__ __forceinline__ void store_b(const SegView& s, int tid, const double 
         const int idx = tid + r * NT;
         const int nn = nc ? (idx & (BN - 1)) : (idx >> 4);
         const int kk = nc ? (idx >> 6) : (idx & (BK - 1));
-        Bs[kk * PADB + nn] = rb[r];
+        Bs[kk * PAD + nn] = rb[r];
     }
 }
 
@@ -170,8 +175,8 @@ __global__ void __launch_bounds__(NT, 2)
 gemm_f64_dmma_kernel(const tnk_gemm_task* __restrict__ tasks,
                      const tnk_gemm_seg* __restrict__ segs, const tnk_gemm_tile* __restrict__ tiles,
                      Slots slots, double* __restrict__ C) {
-    __shared__ double As[2][BK * PADA];
-    __shared__ double Bs[2][BK * PADB];
+    __shared__ double As[2][BK * PADD];
+    __shared__ double Bs[2][BK * PADD];
     const tnk_gemm_tile tile = tiles[blockIdx.x];
     const tnk_gemm_task task = tasks[tile.task];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -197,8 +202,8 @@ gemm_f64_dmma_kernel(const tnk_gemm_task* __restrict__ tasks,
         double ra[4], rb[4];
         load_a(s, m0, M, 0, tid, ra);
         load_b(s, n0, N, 0, tid, rb);
-        store_a(s, tid, ra, As[cur]);
-        store_b(s, tid, rb, Bs[cur]);
+        store_a<PADD>(s, tid, ra, As[cur]);
+        store_b<PADD>(s, tid, rb, Bs[cur]);
         __syncthreads();
         for (int k0 = 0; k0 < s.k; k0 += BK) {
             const bool more = k0 + BK < s.k;
@@ -212,17 +217,17 @@ gemm_f64_dmma_kernel(const tnk_gemm_task* __restrict__ tasks,
             for (int kk = 0; kk < BK; kk += 4) {
                 double a[4], b[2];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) a[i] = as[(kk + q) * PADA + wm + 8 * i + g];
+                for (int i = 0; i < 4; ++i) a[i] = as[(kk + q) * PADD + wm + 8 * i + g];
 #pragma unroll
-                for (int j = 0; j < 2; ++j) b[j] = bs[(kk + q) * PADB + wn + 8 * j + g];
+                for (int j = 0; j < 2; ++j) b[j] = bs[(kk + q) * PADD + wn + 8 * j + g];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
                     for (int j = 0; j < 2; ++j) dmma_8x8x4(acc[i][j][0], acc[i][j][1], a[i], b[j]);
             }
             if (more) {
-                store_a(s, tid, ra, As[cur ^ 1]);
-                store_b(s, tid, rb, Bs[cur ^ 1]);
+                store_a<PADD>(s, tid, ra, As[cur ^ 1]);
+                store_b<PADD>(s, tid, rb, Bs[cur ^ 1]);
             }
             __syncthreads();
             cur ^= 1;
