@@ -267,6 +267,11 @@ int tnk_tc_encode_tmaps_box(const float* base, const int64_t* desc5, int64_t n, 
 int tnk_grouped_gemm_tc(const tnk_gemm_task* tasks, const tnk_tc_seg* segs,
                         const tnk_gemm_tile* tiles, int64_t n_tiles, const void* maps, void* C,
                         int* err, int32_t passes, void* stream);
+/* How tensor-core GEMM stages are scheduled from now on, process-wide: 0 = one CTA per output
+ * tile; 1 = stages with more tiles than SMs run one persistent CTA per SM with two TMEM
+ * accumulators (the epilogue of one tile under the MMAs of the next). Other values leave the
+ * setting unchanged; returns the previous one. No counterpart in the reference. */
+int tnk_tc_schedule(int32_t mode);
 /* The same with 128 x bn tiles (bn = 128 or 64; B maps with boxes of bn rows). */
 int tnk_grouped_gemm_tc_bn(const tnk_gemm_task* tasks, const tnk_tc_seg* segs,
                            const tnk_gemm_tile* tiles, int64_t n_tiles, const void* maps,

@@ -42,6 +42,39 @@ def test_tc_matvec_matches_fp64(scale, passes, tol):
     assert _rel(got, ref) <= tol, _rel(got, ref)
 
 
+@pytest.mark.parametrize("passes", [3, 1])
+def test_tc_persistent_schedule_equals_one_tile_per_cta(passes):
+    """Stages with more tiles than SMs run persistent CTAs with two TMEM accumulators when
+    tnk_tc_schedule(1) is set: the same MMAs per tile in the same order, so the result is the
+    one-tile-per-CTA result bit for bit -- on the chi=1024 mid bond (294 stage-1 tiles) and on
+    a 48-chain batched plan."""
+    from tnkit_gb300 import _lib, batch as B, ops, workloads
+    from tnkit_gb300.mixed import TwoSiteOperatorTC
+    lib = _lib.lib()
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=31)
+    optc = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=passes)
+    opb = B.BatchedTwoSiteOperator(B.batch_problems(48, seed=2), precision="tc")
+    xb = torch.randn(opb.n, dtype=torch.float64, device="cuda")
+    assert len(optc.host.tiles1) > 152
+    prev = lib.tnk_tc_schedule(0)
+    try:
+        a = optc(th.data)
+        ab = opb(xb)
+        lib.tnk_tc_schedule(1)
+        for _ in range(2):
+            b = optc(th.data)
+            bb = opb(xb)
+        torch.cuda.synchronize()
+    finally:
+        lib.tnk_tc_schedule(prev)
+    optc.check_device_error()
+    opb.tc.check_device_error()
+    assert torch.equal(a, b) and torch.equal(ab, bb)
+    if passes == 3:
+        ref = ops.TwoSiteOperator(th.layout, L, W1, W2, R)(th.data)
+        assert _rel(b, ref) <= 1e-4
+
+
 def test_tc_matvec_golden_problem(golden):
     """The reference's own (converged-state) XXZ N=12 local problem."""
     from tnkit_gb300 import BlockTensor, Leg, layout_of

@@ -131,6 +131,7 @@ _SIGS = {
     "tnk_tc_encode_tmaps": ([_P, _P, _I64, _P], C.c_int),
     "tnk_tc_encode_tmaps_box": ([_P, _P, _I64, _P], C.c_int),
     "tnk_grouped_gemm_tc": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _P], C.c_int),
+    "tnk_tc_schedule": ([_I32], C.c_int),
     "tnk_grouped_gemm_tc_bn": ([_P, _P, _P, _I64, _P, _P, _P, _I32, _I32, _P], C.c_int),
     "tnk_combine_f32": ([_P, _P, _P, _I64, _P, _P, _I64, _I32, _P], C.c_int),
     "tnk_ff_split": ([_P, _P, _I64, _P], C.c_int),

@@ -333,6 +333,252 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     }
 }
 
+// Persistent form of the same GEMM for stages with more tiles than SMs: one CTA per SM walks
+// the tiles blockIdx.x, blockIdx.x + gridDim.x, ... with the operand ring running on across
+// tile boundaries and two TMEM accumulators, so the epilogue of one tile overlaps the MMAs of
+// the next. Six warps: warp 0 lane 0 the TMA producer, warp 1 lane 0 the MMA issuer, warps 2-5
+// the epilogue (warp w reads TMEM lane quarter w % 4, i.e. rows 32 (w % 4) .. + 31 of the
+// tile, through its own padded 32 x 33 staging tile). Barriers: the ring's full / empty pair
+// per slot; acc_full[b] (the issuer's commit after a tile's last MMA into accumulator b) and
+// acc_empty[b] (one arrival per epilogue warp once it has read accumulator b). Every wait is
+// bounded and also ends when any role has raised the abort flag; a CTA that aborts records a
+// code in `err`, drains its own TMA copies, waits (bounded) for its MMAs and frees its TMEM.
+constexpr int NT_P = 192;
+
+template <int PASSES, int BNT>
+__global__ void __launch_bounds__(NT_P, 1)
+gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
+                          const TcSeg* __restrict__ segs, const tnk_gemm_tile* __restrict__ tiles,
+                          int n_tiles, const CUtensorMap* __restrict__ maps,
+                          void* __restrict__ Cout, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    constexpr int A_BYTES = TILE_BYTES;
+    constexpr int B_BYTES = BNT * BK * 4;
+    constexpr int PAIR = A_BYTES + B_BYTES;
+    constexpr int STAGE_BYTES = (PASSES == 3) ? 2 * PAIR : PAIR;
+    constexpr int LDW = 33;                               // per-warp staging row stride
+    uint8_t* base = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* ring = base;
+    float* stg_all = reinterpret_cast<float*>(base + STAGES * STAGE_BYTES);
+    uint64_t* full = reinterpret_cast<uint64_t*>(stg_all + 4 * 32 * LDW);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* done = acc_empty + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    int* counts = const_cast<int*>(abort_flag) + 1;       // [0] issued loads, [1] consumed
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(2 * BNT)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        counts[0] = counts[1] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    auto ksteps = [&](const tnk_gemm_task& task) {
+        int nk = 0;
+        for (int s = task.seg_begin; s < task.seg_end; ++s) nk += (segs[s].k + BK - 1) / BK;
+        return nk;
+    };
+
+    if (threadIdx.x == 0) {
+        // TMA producer over every K step of every tile of this CTA, one ring
+        int g = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+            const tnk_gemm_tile tile = tiles[t];
+            const tnk_gemm_task task = tasks[tile.task];
+            int ls = task.seg_begin, lk = 0;
+            const int nk = ksteps(task);
+            for (int i = 0; i < nk; ++i, ++g) {
+                const int slot = g % STAGES;
+                if (g >= STAGES &&
+                    !mbar_wait_or_abort(&empty[slot], ((g / STAGES) - 1) & 1, abort_flag)) {
+                    if (!*abort_flag) atomicExch(err, 12);
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                while (lk >= segs[ls].k) { ++ls; lk = 0; }
+                const TcSeg sg = segs[ls];
+                if (lk == 0) {
+                    tmap_acquire(&maps[2 * sg.a_map]);
+                    tmap_acquire(&maps[2 * sg.b_map]);
+                    if (PASSES == 3) {
+                        tmap_acquire(&maps[2 * sg.a_map + 1]);
+                        tmap_acquire(&maps[2 * sg.b_map + 1]);
+                    }
+                }
+                uint8_t* st = ring + slot * STAGE_BYTES;
+                mbar_expect_tx(&full[slot], STAGE_BYTES);
+                tma_load_2d(st, &maps[2 * sg.a_map], &full[slot], lk, tile.m0);
+                tma_load_2d(st + A_BYTES, &maps[2 * sg.b_map], &full[slot], lk, tile.n0);
+                if (PASSES == 3) {
+                    tma_load_2d(st + PAIR, &maps[2 * sg.a_map + 1], &full[slot], lk, tile.m0);
+                    tma_load_2d(st + PAIR + A_BYTES, &maps[2 * sg.b_map + 1], &full[slot], lk,
+                                tile.n0);
+                }
+                lk += BK;
+            }
+        }
+        counts[0] = g;
+    } else if (threadIdx.x == 32) {
+        // MMA issuer: tile j of this CTA accumulates into TMEM columns (j & 1) * BNT
+        int g = 0, j = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++j) {
+            const tnk_gemm_task task = tasks[tiles[t].task];
+            const int nk = ksteps(task);
+            const int b = j & 1;
+            if (j >= 2 && !mbar_wait_or_abort(&acc_empty[b], ((j >> 1) - 1) & 1, abort_flag)) {
+                if (!*abort_flag) atomicExch(err, 13);
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t acc = tmem + (uint32_t)(b * BNT);
+            for (int i = 0; i < nk; ++i, ++g) {
+                const int slot = g % STAGES;
+                if (!mbar_wait_or_abort(&full[slot], (g / STAGES) & 1, abort_flag)) {
+                    if (!*abort_flag) atomicExch(err, 11);
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint8_t* st = ring + slot * STAGE_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 8; ++kk) {
+                    const uint64_t ah = smem_desc(st + kk * 32);
+                    const uint64_t bh = smem_desc(st + A_BYTES + kk * 32);
+                    mma_tf32<BNT>(acc, ah, bh, (i > 0 || kk > 0) ? 1u : 0u);
+                    if (PASSES == 3) {
+                        const uint64_t al = smem_desc(st + PAIR + kk * 32);
+                        const uint64_t bl = smem_desc(st + PAIR + A_BYTES + kk * 32);
+                        mma_tf32<BNT>(acc, ah, bl, 1u);
+                        mma_tf32<BNT>(acc, al, bh, 1u);
+                    }
+                }
+                mma_commit(&empty[slot]);
+            }
+            if (ok) mma_commit(&acc_full[b]);      // arrives when this tile's MMAs are done
+        }
+        counts[1] = g;
+        mma_commit(done);                          // arrives when every MMA issued is done
+    } else if (warp >= 2) {
+        // epilogue: TMEM lane quarter q = warp % 4 holds rows 32 q .. 32 q + 31 of the tile
+        const int q = warp & 3;
+        float* stg = stg_all + (warp - 2) * 32 * LDW;
+        int j = 0;
+        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++j) {
+            const tnk_gemm_tile tile = tiles[t];
+            const tnk_gemm_task task = tasks[tile.task];
+            const int nk = ksteps(task);
+            const int b = j & 1;
+            bool okw = true;
+            if (lane == 0)
+                okw = mbar_wait_or_abort(&acc_full[b], (j >> 1) & 1, abort_flag);
+            okw = __shfl_sync(0xffffffffu, okw ? 1 : 0, 0) != 0;
+            if (!okw) {
+                if (lane == 0) {
+                    if (!*abort_flag) atomicExch(err, 14);
+                    *abort_flag = 1;
+                }
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const bool f64 = (task.flags & 2) != 0;
+            const int rows = min(32, task.m - (tile.m0 + q * 32));
+            const int cols = min(BNT, task.n - tile.n0);
+            for (int c0 = 0; c0 < BNT; c0 += 32) {
+                uint32_t v[32];
+#pragma unroll
+                for (int x = 0; x < 32; ++x) v[x] = 0u;
+                if (nk > 0) {
+                    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) +
+                                           (uint32_t)(b * BNT + c0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                          "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                          "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                          "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+                          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+                          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                          "=r"(v[30]), "=r"(v[31])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                }
+#pragma unroll
+                for (int x = 0; x < 32; ++x) stg[lane * LDW + x] = __uint_as_float(v[x]);
+                __syncwarp();
+                for (int r = 0; r < rows; ++r) {
+                    const int row = tile.m0 + q * 32 + r;
+                    const int col = c0 + lane;
+                    if (col < cols) {
+                        const int64_t o = task.c_off + (int64_t)row * task.ldc + tile.n0 + col;
+                        const float xv = stg[r * LDW + lane];
+                        if (f64)
+                            reinterpret_cast<double*>(Cout)[o] = (double)xv;
+                        else
+                            reinterpret_cast<float*>(Cout)[o] = xv;
+                    }
+                }
+                __syncwarp();
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                 smem_u32(&acc_empty[b]))
+                             : "memory");
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_flag) {
+        for (int gg = counts[1]; gg < counts[0]; ++gg)
+            mbar_wait(&full[gg % STAGES], (gg / STAGES) & 1);
+    }
+    if (threadIdx.x == 0 && !mbar_wait(done, 0)) atomicExch(err, 15);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(2 * BNT)
+                     : "memory");
+    }
+}
+
+constexpr size_t smem_bytes_p(int passes, int bn) {
+    return 1024 + (size_t)STAGES * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) +
+           4 * 32 * 33 * 4 + 256;
+}
+
 constexpr size_t smem_bytes(int passes, int bn) {
     return 1024 + (size_t)STAGES * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) + 256;
     // (1024: alignment slack of the ring; 256: barriers, TMEM slot, abort flag, counters)
@@ -351,6 +597,38 @@ int launch_tc_t(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_ti
     gemm_tc_kernel<PASSES, BNT><<<(unsigned)n_tiles, NT, sm, stream>>>(
         tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
     return check_launch("gemm_tc_kernel");
+}
+
+template <int PASSES, int BNT>
+int launch_tc_persistent_t(const tnk_gemm_task* tasks, const TcSeg* segs,
+                           const tnk_gemm_tile* tiles, int64_t n_tiles, int grid,
+                           const void* maps, void* C, int* err, cudaStream_t stream) {
+    const size_t sm = smem_bytes_p(PASSES, BNT);
+    cudaError_t e = cudaFuncSetAttribute(gemm_tc_persistent_kernel<PASSES, BNT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) {
+        set_error("tc gemm (persistent): smem attribute: %s", cudaGetErrorString(e));
+        return TNK_ERR_CUDA;
+    }
+    gemm_tc_persistent_kernel<PASSES, BNT><<<(unsigned)grid, NT_P, sm, stream>>>(
+        tasks, segs, tiles, (int)n_tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
+    return check_launch("gemm_tc_persistent_kernel");
+}
+
+int g_tc_schedule = 0;       // 0: one tile per CTA; 1: persistent CTAs when tiles exceed SMs
+
+int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            n < 1)
+            n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
 }
 
 }  // namespace
@@ -373,6 +651,18 @@ int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm
     if ((reinterpret_cast<uintptr_t>(maps) & 63) != 0) {
         set_error("tc gemm: tensor maps must be 64-byte aligned");
         return TNK_ERR_ARG;
+    }
+    const int nsm = sm_count();
+    if (g_tc_schedule == 1 && n_tiles > nsm) {
+        if (passes == 3)
+            return bn == 128 ? launch_tc_persistent_t<3, 128>(tasks, segs, tiles, n_tiles, nsm,
+                                                              maps, C, err, stream)
+                             : launch_tc_persistent_t<3, 64>(tasks, segs, tiles, n_tiles, nsm,
+                                                             maps, C, err, stream);
+        return bn == 128 ? launch_tc_persistent_t<1, 128>(tasks, segs, tiles, n_tiles, nsm, maps,
+                                                          C, err, stream)
+                         : launch_tc_persistent_t<1, 64>(tasks, segs, tiles, n_tiles, nsm, maps,
+                                                         C, err, stream);
     }
     if (passes == 3)
         return bn == 128 ? launch_tc_t<3, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
@@ -442,3 +732,12 @@ int encode_tmaps(const float* base, const int64_t* desc, int64_t n, void* out, i
 }
 
 }  // namespace tnk
+
+// Selects how every later tensor-core GEMM stage is scheduled (process-wide): 0 = one CTA per
+// tile, 1 = a persistent CTA per SM with two TMEM accumulators for stages with more tiles than
+// SMs. Other values leave it unchanged. Returns the previous setting.
+extern "C" int tnk_tc_schedule(int32_t mode) {
+    const int prev = tnk::g_tc_schedule;
+    if (mode == 0 || mode == 1) tnk::g_tc_schedule = mode;
+    return prev;
+}
