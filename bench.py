@@ -201,6 +201,10 @@ def main():
     ap.add_argument("--sweep-model", default="xxz", choices=["xxz", "hubbard"])
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--svd-method", default="gram", choices=["svd", "gram"])
+    ap.add_argument("--svd-host", default="auto", choices=["auto", "device", "never", "always"],
+                    help="with --svd-method gram: where the sectors factor (device: reduction "
+                         "and back-transformation on the GPU, tridiagonal eigenproblems on the "
+                         "host)")
     ap.add_argument("--sweep-precisions", default="f64,mixed,mixed-ff",
                     help="comma-separated among f64, ff, mixed, mixed-ff")
     ap.add_argument("--mixed-schedule", default="sweep", choices=["bond", "sweep"],
@@ -739,7 +743,8 @@ def sweep_leg(torch, args):
         make = lambda: to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
         charge = 0
     out = {"workload": f"{name}, {args.sweeps} sweeps, seed 1, expand 0, "
-                       f"truncation '{args.svd_method}', mixed schedule '{args.mixed_schedule}', "
+                       f"truncation '{args.svd_method}' (host '{args.svd_host}'), "
+                       f"mixed schedule '{args.mixed_schedule}', "
                        f"polish '{args.polish_mode}'"
                        + (f" ({args.polish_sweeps} polished sweeps)"
                           if args.mixed_schedule == "sweep" else ""),
@@ -758,7 +763,7 @@ def sweep_leg(torch, args):
         if args.sweep_warmup_chi > 0:
             dmrg(make(), min(chi, args.sweep_warmup_chi), charge=charge, seed=2, n_sweeps=2,
                  tol=0, rtol=0, expand=0, precision=prec, svd_method=args.svd_method,
-                 mixed_schedule=args.mixed_schedule, polish_sweeps=1,
+                 svd_host=args.svd_host, mixed_schedule=args.mixed_schedule, polish_sweeps=1,
                  polish_mode=args.polish_mode)
         ops._PLANS.clear()
         Wb = make()
@@ -766,7 +771,8 @@ def sweep_leg(torch, args):
         t0 = time.perf_counter()
         E, M, info = dmrg(Wb, chi, charge=charge, seed=1, n_sweeps=args.sweeps, tol=0, rtol=0,
                           expand=0, precision=prec, svd_method=args.svd_method,
-                          mixed_schedule=args.mixed_schedule, polish_sweeps=args.polish_sweeps,
+                          svd_host=args.svd_host, mixed_schedule=args.mixed_schedule,
+                          polish_sweeps=args.polish_sweeps,
                           polish_mode=args.polish_mode)
         torch.cuda.synchronize()
         rec = {"E": E, "energies": info["energies"], "sweep_s": info["sweep_s"],

@@ -419,6 +419,34 @@ int tnk_svd_gram_ws_f32(int64_t R, int64_t C, int64_t* bytes);
 int tnk_svd_gram_f32(const float* M, int64_t R, int64_t C, float* U, float* S, float* Vh,
                      void* ws, int64_t ws_bytes, double* S_host, void* stream);
 
+/* The O(n^3) steps of the same Gram eigh for all sectors of a bond at once (the per-sector eigh
+ * of tnkit/blocks.py:1345-1377 inside the truncation of tnkit/blocks.py:1380-1462), hand-written
+ * for the device: the Householder reduction of every sector's Gram matrix to tridiagonal form in
+ * one launch (one thread-block cluster of `cluster` CTAs per sector, the matrix resident in the
+ * cluster's distributed shared memory), and the back-transformation U = Q Z of the tridiagonal
+ * eigenvectors Z that the cut keeps, in one launch. Between them, the caller solves the
+ * tridiagonal eigenproblems (d, e). Sector s: order n, its Gram matrix at G + g_off (n x n,
+ * column-major; the lower triangle is read), its d, e, tau at + v_off (n entries each; e and tau
+ * use n - 1), its Z at Z + z_off (column-major n x k, ld n). On return from the reduction,
+ * column k of G holds reflector k's v in rows k+1 .. n-1 (v[k+1] = 1). The table arrays are
+ * device memory; the calls only enqueue work on `stream`. */
+typedef struct {
+    int64_t n, g_off, v_off, z_off;
+} tnk_sytrd_sector;
+typedef struct {
+    int32_t sector, col0, ncols, pad;    /* ncols <= 8 columns of one sector's Z */
+} tnk_ormtr_item;
+/* The largest order the reduction takes with clusters of `cluster` (1, 2, 4, 8, 16) CTAs on
+ * the current device; 0 when such clusters cannot be launched there. */
+int tnk_sytrd_limits(int32_t cluster, int32_t* n_max);
+/* n_max: the largest n of the batch (at most tnk_sytrd_limits(cluster)). */
+int tnk_sytrd_batched_f64(const tnk_sytrd_sector* sectors, int32_t n_sectors, int32_t n_max,
+                          int32_t cluster, double* G, double* d, double* e, double* tau,
+                          void* stream);
+int tnk_ormtr_batched_f64(const tnk_sytrd_sector* sectors, const tnk_ormtr_item* items,
+                          int32_t n_items, int32_t n_max, const double* G, const double* tau,
+                          double* Z, void* stream);
+
 /* ----------------------------------------------------------------------------------------
  * Host planner: the block tables of the one- and two-site H_eff contraction (the stage-1 /
  * stage-2 / stage-3 tables above) built natively from the layouts' sector keys, and their

@@ -1,0 +1,183 @@
+"""The device Gram route of the truncation (tnk_sytrd_batched_f64 / tnk_ormtr_batched_f64 with
+the host tridiagonal solver between them) against numpy and against the cuSOLVER route:
+tridiagonal reductions with the Gram matrix's eigenvalues, orthonormal back-transformed
+eigenvectors that reconstruct it, the same kept values, bond sectors and discarded weight as
+the per-sector cuSOLVER factorisation, and DMRG on it matching the reference's energies."""
+import ctypes as C
+import importlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tnkit_gb300 import build
+    build.build()
+    from tnkit_gb300 import linalg as LA
+    if not LA.device_gram_available():
+        pytest.fail("the device Gram route is unavailable on this device")
+
+
+def _gram(n, seed, span=30.0):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    lam = 10.0 ** (-np.linspace(0.0, span, n))
+    return (Q * lam) @ Q.T, lam
+
+
+def test_reduction_and_back_transformation():
+    """Several sectors of different orders in one launch each: T's eigenvalues are G's to FP64
+    accuracy, Q Z is orthonormal and reconstructs G."""
+    from tnkit_gb300 import _lib, hostlapack
+    from tnkit_gb300 import linalg as LA
+    lib = _lib.lib()
+    cs, nmax = LA._sytrd_limits()
+    orders = [1, 2, 3, 17, 100, 33, 522, min(nmax, 640)]
+    gs = [_gram(n, 100 + n) for n in orders]
+    tab = np.zeros((len(orders), 4), np.int64)
+    g = v = 0
+    for r, n in enumerate(orders):
+        tab[r, :3] = (n, g, v)
+        g += n * n
+        v += n
+    G = torch.as_tensor(np.concatenate([x[0].T.reshape(-1) for x in gs]), device="cuda")
+    dv = torch.zeros(3 * v, dtype=torch.float64, device="cuda")
+    tab_d = torch.as_tensor(tab, device="cuda")
+    sp = _lib.stream_ptr()
+    _lib.check(lib.tnk_sytrd_batched_f64(tab_d.data_ptr(), len(orders), max(orders), cs,
+                                         G.data_ptr(), dv.data_ptr(), dv.data_ptr() + 8 * v,
+                                         dv.data_ptr() + 16 * v, sp), "sytrd")
+    dh = dv.cpu().numpy()
+    zs, items = [], []
+    z = 0
+    lams = []
+    for r, n in enumerate(orders):
+        d, e = dh[tab[r, 2]:tab[r, 2] + n], dh[v + tab[r, 2]:v + tab[r, 2] + n]
+        lam, Z = hostlapack.tridiag_eigh(d, e)
+        lams.append(lam)
+        ref = np.linalg.eigvalsh(gs[r][0])
+        assert np.abs(lam - ref).max() <= 1e-14, n
+        tab[r, 3] = z
+        zs.append(np.asfortranarray(Z).T.reshape(-1))        # column-major n x n
+        for c0 in range(0, n, 8):
+            items.append((r, c0, min(8, n - c0), 0))
+        z += n * n
+    Zd = torch.as_tensor(np.concatenate(zs), device="cuda")
+    tab_d = torch.as_tensor(tab, device="cuda")
+    it_d = torch.as_tensor(np.asarray(items, np.int32), device="cuda")
+    _lib.check(lib.tnk_ormtr_batched_f64(tab_d.data_ptr(), it_d.data_ptr(), len(items),
+                                         max(orders), G.data_ptr(), dv.data_ptr() + 16 * v,
+                                         Zd.data_ptr(), sp), "ormtr")
+    Zh = Zd.cpu().numpy()
+    for r, n in enumerate(orders):
+        U = Zh[tab[r, 3]:tab[r, 3] + n * n].reshape(n, n).T      # columns: eigenvectors of G
+        assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-13, n
+        assert np.abs((U * lams[r]) @ U.T - gs[r][0]).max() <= 1e-14, n
+
+
+def test_sytrd_rejects_oversize_order():
+    from tnkit_gb300 import _lib
+    from tnkit_gb300 import linalg as LA
+    lib = _lib.lib()
+    cs, nmax = LA._sytrd_limits()
+    rc = lib.tnk_sytrd_batched_f64(8, 1, nmax + 64, cs, 8, 8, 8, 8, None)
+    assert rc == _lib.TNK_ERR_SIZE
+
+
+def _mid_bond_matrix(seed):
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.tensor import BlockTensor
+    th, *_ = workloads.mid_bond_problem(seed=seed, device="cuda")
+    rng = np.random.default_rng(seed)
+    x = torch.as_tensor(rng.standard_normal(th.layout.size), device="cuda")
+    mat, info = LA.fuse_matrix(BlockTensor(th.layout, x / x.norm()), 2)
+    return mat
+
+
+@pytest.mark.parametrize("scale", ["right", "left", "none"])
+def test_device_route_matches_cusolver_route(scale):
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(21)
+    a = Leg((-2, 0, 2), (60, 310, 140), 1)
+    b = Leg((-2, 0, 2), (70, 300, 150), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size) * np.repeat(10.0 ** -np.linspace(0, 3, lay.nblocks),
+                                                   [int(x) for x in lay.sizes])
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    dn = lambda t: to_dense_np(t.layout, t.data.cpu().numpy())
+    U, S, V, disc = LA.truncated_svd(m, 250, scale=scale, method="gram", host="device")
+    U0, S0, V0, disc0 = LA.truncated_svd(m, 250, scale=scale, method="gram", host="never")
+    assert U.layout.legs == U0.layout.legs and V.layout.legs == V0.layout.legs
+    assert float((S - S0).abs().max()) <= 1e-10 * float(S0.max())
+    assert abs(disc - disc0) <= 1e-9 * max(disc0, 1e-300)
+    if scale == "right":
+        iso = dn(U)
+    elif scale == "left":
+        iso = dn(V).T
+    else:
+        iso = dn(U) if dn(U).shape[0] <= dn(V).shape[1] else dn(V).T
+    assert np.abs(iso.T @ iso - np.eye(iso.shape[1])).max() <= 1e-12
+    mid = np.ones_like(S.cpu().numpy()) if scale != "none" else S.cpu().numpy()
+    assert np.abs((dn(U) * mid) @ dn(V) - (dn(U0) * mid) @ dn(V0)).max() <= 1e-10
+
+
+def test_device_route_many_matches_one_by_one():
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(5)
+    mats = []
+    for k in range(3):
+        a = Leg((-1, 1), (30 + 10 * k, 50), 1)
+        b = Leg((-1, 1), (40, 45 + 5 * k), -1)
+        lay = layout_of((a, b), 0)
+        h = rng.standard_normal(lay.size)
+        mats.append(BlockTensor(lay, torch.as_tensor(h, device="cuda"), h))
+    many = LA.truncated_svd_many([(m, 40, "right") for m in mats], method="gram", host="device")
+    for m, (U, S, V, d) in zip(mats, many):
+        U1, S1, V1, d1 = LA.truncated_svd(m, 40, scale="right", method="gram", host="device")
+        assert U.layout.legs == U1.layout.legs
+        assert torch.equal(S, S1) and torch.equal(U.data, U1.data) and torch.equal(V.data, V1.data)
+        assert d == d1
+
+
+def test_mid_bond_truncation_device_route():
+    """The chi=1024 mid-bond block (XXZ N=64 sectors, up to 522 rows): the device route keeps the
+    same values and sectors as the cuSOLVER route."""
+    from tnkit_gb300 import linalg as LA
+    mat = _mid_bond_matrix(3)
+    U, S, V, disc = LA.truncated_svd(mat, 1024, scale="right", method="gram", host="device")
+    U0, S0, V0, disc0 = LA.truncated_svd(mat, 1024, scale="right", method="gram", host="never")
+    assert U.layout.legs == U0.layout.legs
+    assert float((S**2 - S0**2).abs().max()) <= 1e-13 * float(S0.max() ** 2)
+    assert abs(disc - disc0) <= 1e-12
+
+
+@pytest.mark.parametrize("N,chi", [(12, 64), (64, 64)])
+def test_dmrg_on_device_route_matches_reference(N, chi):
+    """DMRG with the Gram truncation on the device route: the reference's exact-SVD energy to
+    1e-10 (the bar of the cuSOLVER Gram route) and every bond's sectors."""
+    D = importlib.import_module("tnkit_gb300.dmrg")
+    from tnkit_gb300 import workloads
+    from tnkit_gb300.mpo import to_block_mpo
+    ref = json.load(open(os.path.join(GOLDEN, "dmrg_small.json")))[f"xxz_n{N}_chi{chi}"]
+    Wb = to_block_mpo(workloads.xxz_mpo(N), [[1, -1]] * N)[0]
+    E, M, info = D.dmrg(Wb, chi, charge=0, seed=1, n_sweeps=len(ref["energies"]), tol=0,
+                        rtol=0, expand=0, svd_method="gram", svd_host="device")
+    assert abs(E - ref["E"]) <= 1e-10, (E, ref["E"])
+    for m, b in zip(M, ref["bonds"]):
+        assert list(m.legs[2].dims) == b["dims"] and list(m.legs[2].charges) == b["charges"]

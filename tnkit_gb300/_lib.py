@@ -144,6 +144,9 @@ _SIGS = {
     "tnk_zaxpby_f64": ([_P, _P, _I64, _P, _D, _P, _D, _P], C.c_int),
     "tnk_gemm_f64_variant": ([_I32], C.c_int),
     "tnk_tridiag_eig_f64": ([_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P], C.c_int),
+    "tnk_sytrd_limits": ([_I32, _P], C.c_int),
+    "tnk_sytrd_batched_f64": ([_P, _I32, _I32, _I32, _P, _P, _P, _P, _P], C.c_int),
+    "tnk_ormtr_batched_f64": ([_P, _P, _I32, _I32, _P, _P, _P, _P], C.c_int),
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
     "tnk_env_plan_build": ([_P, _P], C.c_int),

@@ -314,7 +314,8 @@ def dmrg_batch(mpos: Sequence, chis: Sequence[int], charges: Optional[Sequence] 
                  for lay, a, b in zip(layouts, offsets[:-1], offsets[1:])]
         facs = LA.truncated_svd_many(
             [(mat, chains[c]["chi"], "right" if chains[c]["sched"][r][1] else "left")
-             for (mat, _), c in zip(fused, act)], driver=o.svd_driver, method=o.svd_method)
+             for (mat, _), c in zip(fused, act)], driver=o.svd_driver, method=o.svd_method,
+            host=o.svd_host)
         new = []
         for (U, S, Vh, disc), (_, finfo), c in zip(facs, fused, act):
             ch = chains[c]

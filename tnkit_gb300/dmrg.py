@@ -66,6 +66,11 @@ class DMRGOptions:
     device: Any = None
     svd_driver: Optional[str] = "gesvd"   # cuSOLVER driver of the per-sector SVD (as the reference)
     svd_method: str = "svd"               # 'svd' (exact) or 'gram' (eigh of the Gram matrix)
+    svd_host: str = "auto"                # with 'gram': where the sectors factor ('device':
+                                          # reduction and back-transformation on the GPU, the
+                                          # tridiagonal eigenproblems on the host; 'never': per
+                                          # sector on cuSOLVER; 'always': host LAPACK; 'auto':
+                                          # the default route of truncated_svd)
     env_precision: str = "auto"           # 'f64', 'ff' (environment updates in float-float:
                                           # ~2x faster, ~10x larger energy error, ~1e-13) or
                                           # 'auto': float-float in the tensor-core-only sweeps
@@ -236,7 +241,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         t0 = time.perf_counter()
         mat, info = LA.fuse_matrix(x, 2)
         U, S, Vh, disc = LA.truncated_svd(mat, chi, scale="right" if right else "left",
-                                          driver=o.svd_driver, method=o.svd_method)
+                                          driver=o.svd_driver, method=o.svd_method,
+                                          host=o.svd_host)
         M[i] = LA.split_rows(U, info)
         M[i + 1] = LA.split_cols(Vh, info)
         total_disc += disc

@@ -345,6 +345,157 @@ def _svd_gram(M: torch.Tensor):
     return U[:, o].contiguous(), S, Q.mH.contiguous()
 
 
+# --- the device Gram route --------------------------------------------------------------------
+# Every sector of a bond (of several bonds: truncated_svd_many) through its canonical side's Gram
+# matrix, G = M M^T for scale 'right' (U from its eigenvectors), M^T M for 'left' (Vh from its
+# eigenvectors), the smaller one for 'none': the Gram matrices by cuBLAS, their reduction to
+# tridiagonal form in one launch (tnk_sytrd_batched_f64), the tridiagonal eigenproblems on the
+# host (hostlapack.tridiag_eigh_many, O(n^2) each), the global cut, then the back-transformation
+# of only the kept eigenvectors in one launch (tnk_ormtr_batched_f64) and the other factor as the
+# exact projection, diag(1/S) U^T M or M V diag(1/S). Sectors larger than the reduction takes
+# go through _svd_gram_native.
+_SYTRD = {"cluster": None, "n_max": 0}
+
+
+def _sytrd_limits():
+    """(cluster size, largest order) of the device reduction on the current device."""
+    if _SYTRD["cluster"] is None:
+        lib = _lib.lib()
+        _SYTRD.update(cluster=0, n_max=0)
+        for cs in (16, 8):
+            nm = C.c_int32(0)
+            _lib.check(lib.tnk_sytrd_limits(cs, C.byref(nm)), "tnk_sytrd_limits")
+            if nm.value > 0:
+                _SYTRD.update(cluster=cs, n_max=int(nm.value))
+                break
+    return _SYTRD["cluster"], _SYTRD["n_max"]
+
+
+def device_gram_available() -> bool:
+    """Whether the device Gram route can run here (a CUDA device with the cluster launch, and
+    the host tridiagonal solver)."""
+    from . import hostlapack
+    if not torch.cuda.is_available() or not hostlapack.available():
+        return False
+    return _sytrd_limits()[1] > 0
+
+
+def _gram_side(scale: str, R: int, Cc: int) -> int:
+    return 1 if scale == "right" else 2 if scale == "left" else (1 if R <= Cc else 2)
+
+
+def _gram_device_many(items):
+    """[(m, blocks, chi, scale, normalize)] -> [(U, S, Vh, disc)] by the device Gram route."""
+    from . import hostlapack
+    lib = _lib.lib()
+    cs, nmax = _sytrd_limits()
+    if nmax <= 0:
+        raise RuntimeError("the device Gram route needs thread-block clusters on a CUDA device")
+    dev = items[0][0].data.device
+    sp = _lib.stream_ptr()
+    sec = []                    # (item, block index, M, side, n)
+    for it, (m, blocks, chi, scale, normalize) in enumerate(items):
+        for b, (_, _, M) in enumerate(blocks):
+            R, Cc = M.shape
+            side = _gram_side(scale, R, Cc)
+            sec.append((it, b, M, side, R if side == 1 else Cc))
+    on_dev = sorted([i for i, s in enumerate(sec) if s[4] <= nmax], key=lambda i: -sec[i][4])
+    off_dev = [i for i, s in enumerate(sec) if s[4] > nmax]
+    # Gram matrices, packed (column-major = row-major: they are symmetric)
+    tab = np.zeros((max(len(on_dev), 1), 4), dtype=np.int64)
+    g = v = 0
+    for r, i in enumerate(on_dev):
+        n = sec[i][4]
+        tab[r, :3] = (n, g, v)
+        g += n * n
+        v += n
+    G = torch.empty(max(g, 1), dtype=torch.float64, device=dev)
+    dv = torch.empty(3 * max(v, 1), dtype=torch.float64, device=dev)
+    d, e, tau = dv[:max(v, 1)], dv[max(v, 1):2 * max(v, 1)], dv[2 * max(v, 1):]
+    for r, i in enumerate(on_dev):
+        _, _, M, side, n = sec[i]
+        Gi = G[tab[r, 1]:tab[r, 1] + n * n].view(n, n)
+        torch.matmul(M, M.mT, out=Gi) if side == 1 else torch.matmul(M.mT, M, out=Gi)
+    facs = {}
+    if on_dev:
+        tab_d = torch.from_numpy(tab).to(dev)
+        n_max = int(tab[:, 0].max())
+        _lib.check(lib.tnk_sytrd_batched_f64(tab_d.data_ptr(), len(on_dev), n_max, cs,
+                                             G.data_ptr(), d.data_ptr(), e.data_ptr(),
+                                             tau.data_ptr(), sp), "tnk_sytrd_batched_f64")
+        de = dv[:2 * max(v, 1)].cpu().numpy()
+        dh, eh = de[:max(v, 1)], de[max(v, 1):]
+    # sectors too large for the reduction, meanwhile on the GPU path
+    for i in off_dev:
+        _, _, M, side, _ = sec[i]
+        facs[i] = _svd_gram_native(M, side)
+    if on_dev:
+        eig = hostlapack.tridiag_eigh_many(
+            [(dh[tab[r, 2]:tab[r, 2] + tab[r, 0]], eh[tab[r, 2]:tab[r, 2] + tab[r, 0]])
+             for r in range(len(on_dev))], lanes=_HOST_LANES)
+    sig = {}
+    for r, i in enumerate(on_dev):
+        M = sec[i][2]
+        k = min(M.shape)
+        lam = eig[r][0][::-1][:k]
+        sig[i] = np.sqrt(np.maximum(lam, 0.0))
+    for i in off_dev:
+        sig[i] = facs[i][3]
+    # the cut of each item (the rule of _trunc_finish), then the kept eigenvectors to the device
+    kept = {}
+    for it, (m, blocks, chi, scale, normalize) in enumerate(items):
+        ids = [i for i, s in enumerate(sec) if s[0] == it]
+        s_host = np.concatenate([sig[i] for i in ids])
+        owner = np.concatenate([np.full(len(sig[i]), j) for j, i in enumerate(ids)])
+        order = np.lexsort((np.arange(s_host.size), -s_host))
+        kk = min(int(chi), s_host.size)
+        cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
+        for j, i in enumerate(ids):
+            kept[i] = int(cnt[j])
+    z = 0
+    zparts, items_orm = [], []
+    for r, i in enumerate(on_dev):
+        n, q = int(tab[r, 0]), kept[i]
+        tab[r, 3] = z
+        if q:
+            Zf = eig[r][1]
+            zparts.append(np.ascontiguousarray(Zf[:, ::-1][:, :q].T))    # (q, n): Z column-major
+            for c0 in range(0, q, 8):
+                items_orm.append((r, c0, min(8, q - c0), 0))
+            z += q * n
+    if zparts:
+        Zd = torch.from_numpy(np.concatenate([p.reshape(-1) for p in zparts])).to(dev)
+        tab_z = torch.from_numpy(tab).to(dev)
+        it_d = torch.from_numpy(np.asarray(items_orm, dtype=np.int32)).to(dev)
+        _lib.check(lib.tnk_ormtr_batched_f64(tab_z.data_ptr(), it_d.data_ptr(), len(items_orm),
+                                             int(tab[:, 0].max()), G.data_ptr(), tau.data_ptr(),
+                                             Zd.data_ptr(), sp), "tnk_ormtr_batched_f64")
+        S_all = torch.from_numpy(np.concatenate(
+            [sig[i][:kept[i]] for i in on_dev if kept[i]])).to(dev)
+    so = 0
+    for r, i in enumerate(on_dev):
+        _, _, M, side, n = sec[i]
+        q = kept[i]
+        R, Cc = M.shape
+        if not q:
+            facs[i] = (M.new_zeros((R, 0)), M.new_zeros(0), M.new_zeros((0, Cc)), sig[i])
+            continue
+        V = Zd[int(tab[r, 3]):int(tab[r, 3]) + q * n].view(q, n)   # row j: eigenvector j of G
+        S = S_all[so:so + q]
+        so += q
+        inv = torch.where(S > 0, 1.0 / torch.where(S > 0, S, torch.ones_like(S)),
+                          torch.zeros_like(S))
+        if side == 1:
+            facs[i] = (V.mT, S, (V @ M) * inv[:, None], sig[i])
+        else:
+            facs[i] = ((M @ V.mT) * inv[None, :], S, V, sig[i])
+    out = []
+    for it, (m, blocks, chi, scale, normalize) in enumerate(items):
+        ids = [i for i, s in enumerate(sec) if s[0] == it]
+        out.append(_trunc_finish(m, blocks, [facs[i] for i in ids], chi, scale, normalize))
+    return out
+
+
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
                   method: str = "svd", normalize: bool = True, host: str = "auto",
                   dtype=torch.float64, gram_qr: bool = False):
@@ -361,11 +512,22 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     not converge is redone in FP64). Inside a DMRG sweep near convergence the FP32 Gram matrix
     loses the small singular values and the environments built on its factors drift, so the
     sweep driver does not use it.
+    host='device': the device Gram route (_gram_device_many: the sectors' reductions to
+    tridiagonal form and the back-transformation of the kept vectors on the GPU, only the
+    tridiagonal eigenproblems on the host); FP64 CUDA blocks, scale as above.
     Returns U, S (device vector, normalised when scale != 'none'), Vh, disc (absolute)."""
-    if host not in ("auto", "never", "always"):
-        raise ValueError("host must be 'auto', 'never' or 'always'")
+    if host not in ("auto", "never", "always", "device"):
+        raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
+    if host == "device":
+        if method != "gram" or gram_qr or dtype != torch.float64 or not m.data.is_cuda or \
+                m.data.dtype != torch.float64:
+            raise ValueError("host='device' is the FP64 Gram route of a CUDA block matrix")
+        blocks = list(_blocks(m))
+        if not blocks:
+            raise ValueError("the matrix has no allowed blocks")
+        return _gram_device_many([(m, blocks, chi, scale, normalize)])[0]
     lr, lc = m.layout.legs
     low = dtype == torch.float32 and m.data.dtype == torch.float64
     if low and method != "gram":
@@ -437,10 +599,24 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
     chains -- given as [(m, chi, scale)], with the sectors of all of them factored in one
     concurrent pass (GPU sectors a stream each, with method='gram' the host LAPACK share
     assigned over all sectors together). Returns the list of (U, S, Vh, disc)."""
-    if host not in ("auto", "never", "always"):
-        raise ValueError("host must be 'auto', 'never' or 'always'")
+    if host not in ("auto", "never", "always", "device"):
+        raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if method not in ("svd", "gram"):
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
+    if host == "device":
+        if method != "gram":
+            raise ValueError("host='device' is the Gram route")
+        dv = []
+        for m, chi, scale in items:
+            if chi < 1:
+                raise ValueError(f"chi must be at least 1, got {chi}")
+            if not (m.data.is_cuda and m.data.dtype == torch.float64):
+                raise TypeError("truncated_svd_many takes FP64 CUDA block matrices")
+            blocks = list(_blocks(m))
+            if not blocks:
+                raise ValueError("the matrix has no allowed blocks")
+            dv.append((m, blocks, chi, scale, normalize))
+        return _gram_device_many(dv)
     per, fns, mats, shapes = [], [], [], []
     for m, chi, scale in items:
         if chi < 1:
