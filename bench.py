@@ -181,6 +181,10 @@ def main():
                          "at N=1)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the whole chi=1024 DMRG leg (FP64 against mixed-ff, ~2 minutes)")
+    ap.add_argument("--no-trunc", action="store_true",
+                    help="skip the truncation leg (the chi=1024 mid-bond cut on each route)")
+    ap.add_argument("--trunc-only", action="store_true",
+                    help="run only the truncation leg and print its record")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-chain batched local problems (sequential, batched, "
                          "graph-captured; a few seconds, run by default at N=1)")
@@ -237,6 +241,11 @@ def main():
     from tnkit_gb300 import build, ops, workloads, _lib, plan as P
     build.build()
     _lib.load()
+    if args.trunc_only:
+        if rank == 0:
+            print(json.dumps({"truncation": trunc_leg(torch, dev, measure_dgemm_peak(torch, dev),
+                                                      max(args.steps // 2, 5))}), flush=True)
+        return
     th, L, W1, W2, R = workloads.mid_bond_problem(seed=3 + rank, device=dev)
     # the schedule (FP64 inner product, stage-3 split-K, tile order) picked by the autotuner on
     # this problem; every FP64 launch of the legs below uses its inner product
@@ -453,6 +462,8 @@ def main():
     # the float-float leg: theta split, two GEMMs, combination, split-K sum when present
     line["gpu_launches_per_step"] = {"fp64": per_step, "e2e": per_step, "mixed": 4,
                                      "float_float": per_step + 1}
+    if world == 1 and not args.no_trunc:
+        line["truncation"] = trunc_leg(torch, dev, dgemm, max(args.steps // 2, 5))
     if args.sweep or (world == 1 and not args.no_sweep):
         line["sweep"] = sweep_leg(torch, args)
     if world == 1 and not args.no_batch:
@@ -470,6 +481,83 @@ def main():
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
+
+
+def trunc_block(torch, dev, seed=0):
+    """The chi=1024 mid-bond two-site block (U(1) XXZ N=64 sector dimensions) fused to a matrix,
+    with a DMRG-like spectrum: sigma_i = exp(-i / 40) over all 2048 values, dealt to the sectors
+    at random, unit norm (synthetic data of the workload's shapes)."""
+    from tnkit_gb300 import linalg as LA, workloads
+    from tnkit_gb300.tensor import BlockTensor
+    th, *_ = workloads.mid_bond_problem(seed=3, device=dev)
+    mat, _ = LA.fuse_matrix(th, 2)
+    lay = mat.layout
+    rng = np.random.default_rng(seed)
+    ks = [min(lay.shape(j)) for j in range(lay.nblocks)]
+    sig = np.exp(-np.arange(sum(ks)) / 40.0)
+    owner = np.concatenate([[j] * k for j, k in enumerate(ks)])
+    rng.shuffle(owner)
+    data = np.zeros(lay.size)
+    for j in range(lay.nblocks):
+        R, Cc = lay.shape(j)
+        k = ks[j]
+        sj = np.sort(sig[owner == j])[::-1]
+        U, _ = np.linalg.qr(rng.standard_normal((R, k)))
+        V, _ = np.linalg.qr(rng.standard_normal((Cc, k)))
+        o = int(lay.offsets[j])
+        data[o:o + R * Cc] = ((U * sj) @ V.T).reshape(-1)
+    data /= np.linalg.norm(data)
+    return BlockTensor(lay, torch.as_tensor(data, device=dev))
+
+
+def trunc_leg(torch, dev, dgemm, reps):
+    """The truncation of the chi=1024 mid bond (keep 1024 of 2048 values, scale 'right', as the
+    left-to-right sweep cuts) on each Gram route: 'device' (the sectors' reductions and the
+    back-transformation of the kept vectors on the GPU, tridiagonal problems on host threads),
+    'never' (each sector's eigh on cuSOLVER), 'auto' (the sweep's default)."""
+    from tnkit_gb300 import linalg as LA
+    m = trunc_block(torch, dev)
+    out = {"workload": "chi=1024 mid-bond truncation, U(1) XXZ N=64 sector dims (2 .. 522 "
+                       "rows), keep 1024 of 2048, sigma_i = exp(-i/40) dealt to sectors "
+                       "(synthetic), scale 'right'",
+           "sectors": [list(m.layout.shape(j)) for j in range(m.layout.nblocks)]}
+    res = {}
+    routes = ["device", "never", "auto"] if LA.device_gram_available() else ["never", "auto"]
+    for host in routes:
+        for _ in range(2):
+            r = LA.truncated_svd(m, 1024, scale="right", method="gram", host=host)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = LA.truncated_svd(m, 1024, scale="right", method="gram", host=host)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        res[host] = r
+        out[host] = {"ms_median": float(np.median(ts)) * 1e3, "ms_min": float(min(ts)) * 1e3}
+    S0 = res["never"][1]
+    for host in routes:
+        S = res[host][1]
+        out[host]["max_abs_dsigma2_vs_never"] = float((S ** 2 - S0 ** 2).abs().max())
+        out[host]["discarded"] = res[host][3]
+    if "device" in res:
+        tm = {}
+        for _ in range(reps):
+            blocks = list(LA._blocks(m))
+            LA._gram_device_many([(m, blocks, 1024, "right", True)], timing=tm)
+        ph = {k: v / reps for k, v in tm.items() if k.endswith("_ms") or k == "reduce_flops"}
+        out["device_phases_ms"] = {k: v for k, v in ph.items() if k.endswith("_ms")}
+        achieved = ph["reduce_flops"] / (ph["reduce_ms"] * 1e-3) / 1e12
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        cls = LA._sytrd_clusters(sorted((min(s) for s in out["sectors"]), reverse=True), n_sm)
+        out["roofline"] = {
+            "bound": "fp64", "kernel": "sytrd_cluster_kernel (all sectors, one launch per "
+                                       "cluster size)",
+            "achieved": achieved, "peak": dgemm, "unit": "TFLOP/s", "frac": achieved / dgemm,
+            "flops": "4/3 n^3 per sector (LAPACK dsytrd's count)",
+            "sms_used": int(sum(cls)), "clusters": cls,
+            "peak_source": "cuBLAS DGEMM 8192^3 measured in this run over all SMs"}
+    return out
 
 
 def _peaks():
@@ -778,6 +866,7 @@ def sweep_leg(torch, args):
         rec = {"E": E, "energies": info["energies"], "sweep_s": info["sweep_s"],
                "total_s": time.perf_counter() - t0, "phase_time": info["phase_time"],
                "matvecs": info["mixed_counts"], "discarded_weight": info["discarded_weight"],
+               "discarded_per_sweep": info["discarded_per_sweep"],
                "mid_bond": {"sectors": len(M[N // 2].legs[0].dims),
                             "dim": int(sum(M[N // 2].legs[0].dims)),
                             "largest_sector": int(max(M[N // 2].legs[0].dims))}}

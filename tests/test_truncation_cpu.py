@@ -35,3 +35,36 @@ def test_lane_switches():
     assert all(0 <= l < LA._HOST_LANES for l in host_only)
     assert LA._assign_sectors([(40, 40)], True) == [-1]
     assert LA._assign_sectors([(40, 40)], True, gpu_ok=False) == [0]
+
+
+def test_cut_with_factors_holding_only_the_kept_vectors():
+    """The device route hands the cut every sector's full singular values on the host but only
+    the kept columns as factors: the cut counts per sector from the full values, as when every
+    factor is complete."""
+    import numpy as np
+    import torch
+    from tnkit_gb300.layout import Leg, layout_of
+    from tnkit_gb300.tensor import BlockTensor
+    a = Leg((-1, 1), (5, 4), 1)
+    b = Leg((-1, 1), (6, 4), -1)
+    lay = layout_of((a, b), 0)
+    m = BlockTensor(lay, torch.zeros(lay.size, dtype=torch.float64))
+    blocks = list(LA._blocks(m))
+    s = [np.array([0.9, 0.5, 0.3, 0.2, 0.1]), np.array([0.8, 0.6, 0.25, 0.05])]
+    chi = 5                      # keeps 0.9, 0.8, 0.6, 0.5, 0.3: three of sector 0, two of 1
+    full, part = [], []
+    for (_, _, M), sv in zip(blocks, s):
+        R, C = M.shape
+        k = len(sv)
+        U = torch.eye(R, k, dtype=torch.float64)
+        Vh = torch.eye(k, C, dtype=torch.float64)
+        S = torch.as_tensor(sv)
+        full.append((U, S, Vh, sv))
+        q = {5: 3, 4: 2}[k]
+        part.append((U[:, :q], S[:q], Vh[:q], sv))
+    Uf, Sf, Vf, df = LA._trunc_finish(m, blocks, full, chi, "right", True)
+    Up, Sp, Vp, dp = LA._trunc_finish(m, blocks, part, chi, "right", True)
+    assert Up.layout.legs == Uf.layout.legs and Vp.layout.legs == Vf.layout.legs
+    assert torch.equal(Sp, Sf) and torch.equal(Up.data, Uf.data) and torch.equal(Vp.data, Vf.data)
+    assert dp == df and abs(df - (0.2 ** 2 + 0.1 ** 2 + 0.25 ** 2 + 0.05 ** 2)) < 1e-15
+    assert list(Up.layout.legs[1].dims) == [3, 2]

@@ -188,7 +188,7 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         if o.env_precision == "auto":
             return "ff" if tc_only_sweep() else "f64"
         return o.env_precision
-    energies, sweep_s, alphas = [], [], []
+    energies, sweep_s, alphas, disc_sweeps = [], [], [], []
     phase = {"eig": 0.0, "trunc": 0.0, "env": 0.0}
     counts = {"lo": 0, "hi": 0}
     total_disc, mv_calls = 0.0, 0
@@ -271,6 +271,7 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
         for i in range(N - 2, -1, -1):
             E = solve_block(i, False)
         energies.append(E)
+        disc_sweeps.append(total_disc - sum(disc_sweeps))
         sync()
         sweep_s.append(time.perf_counter() - ts)
         if o.verbose:
@@ -280,7 +281,8 @@ def dmrg(mpo, chi: Optional[int] = None, options=None, **kw):
             break
         prev_E = E
     info = {"sweeps": sweep + 1, "energies": energies, "backend": "b200", "blocks": block,
-            "eig": o.eig, "discarded_weight": total_disc, "matvec_calls": mv_calls,
+            "eig": o.eig, "discarded_weight": total_disc, "discarded_per_sweep": disc_sweeps,
+            "matvec_calls": mv_calls,
             "phase_time": phase, "mixed_counts": counts, "sites": 2, "expand": 0,
             "expand_alphas": alphas, "sweep_s": sweep_s, "precision": o.precision}
     return E, M, info

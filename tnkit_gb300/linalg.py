@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import ctypes as C
+import os
 import threading
 from typing import Tuple
 
@@ -354,21 +355,63 @@ def _svd_gram(M: torch.Tensor):
 # of only the kept eigenvectors in one launch (tnk_ormtr_batched_f64) and the other factor as the
 # exact projection, diag(1/S) U^T M or M V diag(1/S). Sectors larger than the reduction takes
 # go through _svd_gram_native.
-_SYTRD = {"cluster": None, "n_max": 0}
+_SYTRD = {"limits": None}
+# time model of one sector's reduction with a cluster of cs CTAs: ~n^3 FP64 FMAs shared by the
+# cluster, plus a fixed cost per column (two cluster barriers and the gathers; one CTA barrier
+# pair when cs = 1), measured on GB300
+_SY_FMA_PER_S = 3.6e9                 # FP64 FMAs per second per SM
+_SY_STEP_S = {1: 0.6e-6, 2: 1.4e-6, 4: 1.5e-6, 8: 1.6e-6, 16: 1.8e-6}
+
+
+def _sytrd_table():
+    """{cluster size: largest order} of the device reduction on the current device (0: that
+    cluster size cannot launch there)."""
+    if _SYTRD["limits"] is None:
+        lib = _lib.lib()
+        lim = {}
+        for cs in (1, 2, 4, 8, 16):
+            nm = C.c_int32(0)
+            _lib.check(lib.tnk_sytrd_limits(cs, C.byref(nm)), "tnk_sytrd_limits")
+            lim[cs] = int(nm.value)
+        _SYTRD["limits"] = lim
+    return _SYTRD["limits"]
 
 
 def _sytrd_limits():
-    """(cluster size, largest order) of the device reduction on the current device."""
-    if _SYTRD["cluster"] is None:
-        lib = _lib.lib()
-        _SYTRD.update(cluster=0, n_max=0)
-        for cs in (16, 8):
-            nm = C.c_int32(0)
-            _lib.check(lib.tnk_sytrd_limits(cs, C.byref(nm)), "tnk_sytrd_limits")
-            if nm.value > 0:
-                _SYTRD.update(cluster=cs, n_max=int(nm.value))
-                break
-    return _SYTRD["cluster"], _SYTRD["n_max"]
+    """(largest usable cluster size, its largest order) of the device reduction."""
+    lim = _sytrd_table()
+    for cs in (16, 8, 4, 2, 1):
+        if lim[cs] > 0:
+            return cs, lim[cs]
+    return 0, 0
+
+
+def _sy_time(n: int, cs: int) -> float:
+    return n ** 3 / (cs * _SY_FMA_PER_S) + n * _SY_STEP_S[cs]
+
+
+def _sytrd_clusters(ns, n_sm: int):
+    """A cluster size per sector order: each sector's fastest alone, then, while the clusters
+    need more than one wave of the SMs, the sector whose halving costs least in makespan terms
+    gets half the CTAs (throughput for many small sectors, latency for a bond's few large
+    ones)."""
+    lim = _sytrd_table()
+    ok = lambda n, c: lim.get(c, 0) >= n
+    cs = []
+    for n in ns:
+        cands = [c for c in (1, 2, 4, 8, 16) if ok(n, c)]
+        cs.append(min(cands, key=lambda c: _sy_time(n, c)) if cands else 0)
+    while sum(cs) > n_sm:
+        best, cost = None, None
+        for i, (n, c) in enumerate(zip(ns, cs)):
+            if c > 1 and ok(n, c // 2):
+                d = _sy_time(n, c // 2) - _sy_time(n, c)
+                if cost is None or d < cost:
+                    best, cost = i, d
+        if best is None:
+            break
+        cs[best] //= 2
+    return cs
 
 
 def device_gram_available() -> bool:
@@ -380,15 +423,28 @@ def device_gram_available() -> bool:
     return _sytrd_limits()[1] > 0
 
 
+# host threads for the tridiagonal eigenproblems of one pass (each O(n^2) with deflation)
+_STEDC_LANES = max(1, min(8, (os.cpu_count() or 2) // 2))
+
+
 def _gram_side(scale: str, R: int, Cc: int) -> int:
     return 1 if scale == "right" else 2 if scale == "left" else (1 if R <= Cc else 2)
 
 
-def _gram_device_many(items):
-    """[(m, blocks, chi, scale, normalize)] -> [(U, S, Vh, disc)] by the device Gram route."""
+def _gram_device_many(items, timing=None):
+    """[(m, blocks, chi, scale, normalize)] -> [(U, S, Vh, disc)] by the device Gram route.
+    With a dict `timing`, the phases' times in ms are added to it (CUDA events for the device
+    phases, host clock for the host one; the call then synchronises at its end)."""
+    import time
     from . import hostlapack
     lib = _lib.lib()
-    cs, nmax = _sytrd_limits()
+    ev = {}
+
+    def mark(name):
+        if timing is not None:
+            ev[name] = torch.cuda.Event(enable_timing=True)
+            ev[name].record()
+    cs_max, nmax = _sytrd_limits()
     if nmax <= 0:
         raise RuntimeError("the device Gram route needs thread-block clusters on a CUDA device")
     dev = items[0][0].data.device
@@ -412,17 +468,34 @@ def _gram_device_many(items):
     G = torch.empty(max(g, 1), dtype=torch.float64, device=dev)
     dv = torch.empty(3 * max(v, 1), dtype=torch.float64, device=dev)
     d, e, tau = dv[:max(v, 1)], dv[max(v, 1):2 * max(v, 1)], dv[2 * max(v, 1):]
+    mark("gram0")
     for r, i in enumerate(on_dev):
         _, _, M, side, n = sec[i]
         Gi = G[tab[r, 1]:tab[r, 1] + n * n].view(n, n)
         torch.matmul(M, M.mT, out=Gi) if side == 1 else torch.matmul(M.mT, M, out=Gi)
     facs = {}
     if on_dev:
-        tab_d = torch.from_numpy(tab).to(dev)
-        n_max = int(tab[:, 0].max())
-        _lib.check(lib.tnk_sytrd_batched_f64(tab_d.data_ptr(), len(on_dev), n_max, cs,
-                                             G.data_ptr(), d.data_ptr(), e.data_ptr(),
-                                             tau.data_ptr(), sp), "tnk_sytrd_batched_f64")
+        # one launch per cluster size, each over its sectors (largest first)
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        cls = _sytrd_clusters([int(tab[r, 0]) for r in range(len(on_dev))], n_sm)
+        main = torch.cuda.current_stream(dev)
+        mark("red0")
+        for j, c in enumerate(sorted(set(cls), reverse=True)):
+            rows = [r for r in range(len(on_dev)) if cls[r] == c]
+            sub = torch.from_numpy(np.ascontiguousarray(tab[rows])).to(dev)
+            st = main if j == 0 else _concurrent().stream(dev, 64 + j)
+            if st is not main:
+                st.wait_stream(main)
+            with torch.cuda.stream(st):
+                _lib.check(lib.tnk_sytrd_batched_f64(
+                    sub.data_ptr(), len(rows), int(tab[rows, 0].max()), c, G.data_ptr(),
+                    d.data_ptr(), e.data_ptr(), tau.data_ptr(), _lib.stream_ptr()),
+                    "tnk_sytrd_batched_f64")
+                sub.record_stream(st)
+            if st is not main:
+                main.wait_stream(st)
+        mark("red1")
+        t_host = time.perf_counter()
         de = dv[:2 * max(v, 1)].cpu().numpy()
         dh, eh = de[:max(v, 1)], de[max(v, 1):]
     # sectors too large for the reduction, meanwhile on the GPU path
@@ -432,7 +505,9 @@ def _gram_device_many(items):
     if on_dev:
         eig = hostlapack.tridiag_eigh_many(
             [(dh[tab[r, 2]:tab[r, 2] + tab[r, 0]], eh[tab[r, 2]:tab[r, 2] + tab[r, 0]])
-             for r in range(len(on_dev))], lanes=_HOST_LANES)
+             for r in range(len(on_dev))], lanes=_STEDC_LANES)
+        if timing is not None:
+            timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
     sig = {}
     for r, i in enumerate(on_dev):
         M = sec[i][2]
@@ -467,9 +542,11 @@ def _gram_device_many(items):
         Zd = torch.from_numpy(np.concatenate([p.reshape(-1) for p in zparts])).to(dev)
         tab_z = torch.from_numpy(tab).to(dev)
         it_d = torch.from_numpy(np.asarray(items_orm, dtype=np.int32)).to(dev)
+        mark("back0")
         _lib.check(lib.tnk_ormtr_batched_f64(tab_z.data_ptr(), it_d.data_ptr(), len(items_orm),
                                              int(tab[:, 0].max()), G.data_ptr(), tau.data_ptr(),
                                              Zd.data_ptr(), sp), "tnk_ormtr_batched_f64")
+        mark("back1")
         S_all = torch.from_numpy(np.concatenate(
             [sig[i][:kept[i]] for i in on_dev if kept[i]])).to(dev)
     so = 0
@@ -493,6 +570,17 @@ def _gram_device_many(items):
     for it, (m, blocks, chi, scale, normalize) in enumerate(items):
         ids = [i for i, s in enumerate(sec) if s[0] == it]
         out.append(_trunc_finish(m, blocks, [facs[i] for i in ids], chi, scale, normalize))
+    if timing is not None:
+        mark("end")
+        torch.cuda.synchronize(dev)
+        span = lambda a, b: ev[a].elapsed_time(ev[b]) if a in ev and b in ev else 0.0
+        for k, (a, b) in {"gram_ms": ("gram0", "red0"), "reduce_ms": ("red0", "red1"),
+                          "back_ms": ("back0", "back1"), "total_ms": ("gram0", "end")}.items():
+            timing[k] = timing.get(k, 0.0) + span(a, b)
+        timing["sectors"] = len(sec)
+        timing["sectors_on_device"] = len(on_dev)
+        timing["reduce_flops"] = timing.get("reduce_flops", 0.0) + sum(
+            4.0 / 3.0 * sec[i][4] ** 3 for i in on_dev)
     return out
 
 
@@ -670,11 +758,14 @@ def _trunc_finish(m: BlockTensor, blocks, facs, chi: int, scale: str, normalize:
     parts = [(r, c, U, S, Vh) for (r, c, _), (U, S, Vh, _h) in zip(blocks, facs)]
     if not parts:
         raise ValueError("the matrix has no allowed blocks")
+    # every sector's singular values on the host (the factors may hold only the kept ones)
     if all(f[3] is not None for f in facs):
         s_host = np.concatenate([f[3] for f in facs])
+        lens = [len(f[3]) for f in facs]
     else:
         s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
-    owner = np.concatenate([np.full(len(p[3]), j) for j, p in enumerate(parts)])
+        lens = [len(p[3]) for p in parts]
+    owner = np.concatenate([np.full(n, j) for j, n in enumerate(lens)])
     order = np.lexsort((np.arange(s_host.size), -s_host))
     k = min(int(chi), s_host.size)
     kept = np.bincount(owner[order[:k]], minlength=len(parts))
