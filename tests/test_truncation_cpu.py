@@ -68,3 +68,66 @@ def test_cut_with_factors_holding_only_the_kept_vectors():
     assert torch.equal(Sp, Sf) and torch.equal(Up.data, Uf.data) and torch.equal(Vp.data, Vf.data)
     assert dp == df and abs(df - (0.2 ** 2 + 0.1 ** 2 + 0.25 ** 2 + 0.05 ** 2)) < 1e-15
     assert list(Up.layout.legs[1].dims) == [3, 2]
+
+
+def _run_tiles(tables, slots, C):
+    """Only the listed tiles of each task (64 x 64, clipped), as the grouped GEMM kernel runs
+    them; entries outside every tile stay as they were."""
+    import numpy as np
+    from table_interp import _view
+    from tnkit_gb300.plan import TILE_M, TILE_N
+    tasks, segs, tiles = tables
+    for tl in tiles:
+        t = tasks[int(tl["task"])]
+        m, n = int(t["m"]), int(t["n"])
+        m0, n0 = int(tl["m0"]), int(tl["n0"])
+        rows, cols = np.arange(m0, min(m, m0 + TILE_M)), np.arange(n0, min(n, n0 + TILE_N))
+        acc = np.zeros((len(rows), len(cols)))
+        for s in segs[int(t["seg_begin"]):int(t["seg_end"])]:
+            k = int(s["k"])
+            A = _view(slots[int(s["a_buf"])], s["a_off"], (m, k), (s["a_rs"], s["a_cs"]))
+            B = _view(slots[int(s["b_buf"])], s["b_off"], (k, n), (s["b_rs"], s["b_cs"]))
+            acc += float(s["coef"]) * (A[rows] @ B[:, cols])
+        C[int(t["c_off"]) + rows[:, None] * int(t["ldc"]) + cols[None, :]] = acc
+
+
+def test_device_route_product_tables():
+    """The device route's grouped-GEMM tables, run tile by tile on the CPU: the Gram matrices'
+    tiles cover the triangle the reduction reads (the lower one of the column-major view, G[j n +
+    i] for i >= j) with M M^T or M^T M; the other factor is V M or M V^T."""
+    import numpy as np
+    rng = np.random.default_rng(4)
+    shapes = [(70, 90, 1), (130, 40, 2), (5, 3, 1), (64, 64, 2), (200, 129, 1)]
+    buf = rng.standard_normal(sum(R * C for R, C, _ in shapes) + 7)
+    secs, mo, go = [], 7, 0
+    for R, C, side in shapes:
+        secs.append((mo, R, C, side, go))
+        n = R if side == 1 else C
+        mo += R * C
+        go += n * n
+    G = np.full(go, np.nan)
+    _run_tiles(LA._product_tables(LA._gram_products(secs), upper_only=True), [buf], G)
+    for (mo, R, C, side, go), _ in zip(secs, shapes):
+        M = buf[mo:mo + R * C].reshape(R, C)
+        ref = M @ M.T if side == 1 else M.T @ M
+        n = ref.shape[0]
+        g = G[go:go + n * n]
+        lower = np.array([[g[j * n + i] for j in range(i + 1)] for i in range(n)], dtype=object)
+        for i in range(n):
+            assert np.allclose(np.asarray(lower[i], float), ref[i, :i + 1], rtol=1e-13, atol=1e-12)
+    # the other factor
+    Z = rng.standard_normal(40000)
+    osecs, po = [], 0
+    for (mo, R, C, side, _), q in zip(secs, (20, 13, 2, 64, 100)):
+        n = R if side == 1 else C
+        zo = int(rng.integers(0, 40000 - q * n))
+        osecs.append((mo, R, C, side, zo, q, po))
+        po += q * (C if side == 1 else R)
+    P = np.full(po, np.nan)
+    _run_tiles(LA._product_tables(LA._other_products(osecs)), [buf, Z], P)
+    for mo, R, C, side, zo, q, po in osecs:
+        M = buf[mo:mo + R * C].reshape(R, C)
+        n = R if side == 1 else C
+        V = Z[zo:zo + q * n].reshape(q, n)
+        ref = V @ M if side == 1 else M @ V.T
+        assert np.allclose(P[po:po + ref.size].reshape(ref.shape), ref, rtol=1e-13, atol=1e-12)

@@ -47,77 +47,70 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Sum over the CTA; every thread gets the result. red holds SY_WARPS + 1 doubles.
-__device__ double block_sum(double v, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        double s = lane < SY_WARPS ? red[lane] : 0.0;
-        s = warp_sum(s);
-        if (lane == 0) red[SY_WARPS] = s;
-    }
-    __syncthreads();
-    const double s = red[SY_WARPS];
-    __syncthreads();
-    return s;
-}
-
 // Shared-memory layout of a sector of order n on a cluster of cs CTAs (the same offsets in every
-// CTA of the cluster, so peers address each other's arrays by the local offset).
+// CTA of the cluster, so peers address each other's arrays by the local offset). Columns are
+// stored with an odd stride (ld = n | 1 doubles): threads that read one row of several
+// columns then hit distinct banks.
 struct SyShared {
-    double* A;      // ncm columns of n (the CTA's own columns, cyclic)
+    double* A;      // ncm columns of ld (the CTA's own columns, cyclic)
     double* vb;     // n: the reflector this CTA formed (read by the peers)
     double* vl;     // n: the current reflector
     double* wl;     // n: the current w
     double* pown;   // ncm: p of the own columns (read by the peers)
-    double* red;    // SY_WARPS + 1: reductions
+    double* part;   // SY_THREADS: partial column dot products
+    double* red;    // SY_WARPS: reductions
     double* scal;   // 2: tau of the reflector in vb, this CTA's share of p . v
 };
 
+__host__ __device__ inline int64_t sy_ld(int64_t n) { return n | 1; }
+
 __host__ __device__ inline int64_t sy_shared_doubles(int64_t n, int cs) {
     const int64_t ncm = (n + cs - 1) / cs;
-    return ncm * n + 3 * n + ncm + SY_WARPS + 1 + 2;
+    return ncm * sy_ld(n) + 3 * n + ncm + SY_THREADS + SY_WARPS + 2;
 }
 
 __device__ SyShared sy_layout(double* sh, int n, int ncm) {
     SyShared s;
     s.A = sh;
-    s.vb = s.A + (size_t)ncm * n;
+    s.vb = s.A + (size_t)ncm * sy_ld(n);
     s.vl = s.vb + n;
     s.wl = s.vl + n;
     s.pown = s.wl + n;
-    s.red = s.pown + ncm;
-    s.scal = s.red + SY_WARPS + 1;
+    s.part = s.pown + ncm;
+    s.red = s.part + SY_THREADS;
+    s.scal = s.red + SY_WARPS;
     return s;
 }
 
-// The reflector of column c (stored at col, rows 0 .. n-1, already updated through step c - 1):
-// H = I - tau v v^T with H [alpha; x] = [beta; 0], v = [1; x / (alpha - beta)],
-// beta = -sign(alpha) ||[alpha; x]||, tau = (beta - alpha) / beta (tau = 0, v = e_1 when x = 0).
-// Writes v to vb and to column c of the sector's G (rows c+1 .. n-1), tau to scal[0] and tau[c],
-// d[c] and e[c] = beta. The entries of a Gram matrix of a unit-norm block are at most 1 in
-// magnitude, so the sum of squares needs no scaling (it underflows only below 1e-154).
-__device__ void householder(const double* col, int c, int n, double* vb, double* gcol,
-                            double* d, double* e, double* tau, double* red, double* scal) {
-    const int tid = threadIdx.x;
+// The reflector of column c, formed by one warp (lanes over rows) from col (rows 0 .. n-1,
+// already updated through step c - 1): H = I - tau v v^T with H [alpha; x] = [beta; 0],
+// v = [1; x / (alpha - beta)], beta = -sign(alpha) ||[alpha; x]||, tau = (beta - alpha) / beta
+// (tau = 0, v = e_1 when x = 0). The scalars are computed by lane 0 alone and broadcast. Writes
+// v to vb and to column c of the sector's G (rows c+1 .. n-1), tau to scal[0] and tau[c], d[c]
+// and e[c] = beta. The entries of a Gram matrix of a unit-norm block are at most 1 in magnitude,
+// so the sum of squares needs no scaling (it underflows only below 1e-154).
+__device__ void householder_warp(const double* col, int c, int n, double* vb, double* gcol,
+                                 double* d, double* e, double* tau, double* scal) {
+    const int lane = threadIdx.x & 31;
     const double alpha = col[c + 1];
     double ss = 0.0;
-    for (int i = c + 2 + tid; i < n; i += SY_THREADS) ss = fma(col[i], col[i], ss);
-    ss = block_sum(ss, red);
+    for (int i = c + 2 + lane; i < n; i += 32) ss = fma(col[i], col[i], ss);
+    ss = warp_sum(ss);
     double beta = alpha, t = 0.0, sc = 0.0;
-    if (ss > 0.0) {
+    if (lane == 0 && ss > 0.0) {
         beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
         t = (beta - alpha) / beta;
         sc = 1.0 / (alpha - beta);
     }
-    for (int i = c + 1 + tid; i < n; i += SY_THREADS) {
+    beta = __shfl_sync(0xffffffffu, beta, 0);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    sc = __shfl_sync(0xffffffffu, sc, 0);
+    for (int i = c + 1 + lane; i < n; i += 32) {
         const double v = (i == c + 1) ? 1.0 : col[i] * sc;
         vb[i] = v;
         gcol[i] = v;
     }
-    if (tid == 0) {
+    if (lane == 0) {
         d[c] = col[c];
         e[c] = beta;
         tau[c] = t;
@@ -139,6 +132,7 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
     double* e = ev + sec[s].v_off;
     double* tau = tv + sec[s].v_off;
     const int ncm = (n + cs - 1) / cs;
+    const int ld = (int)sy_ld(n);
     const int ncl = r < n ? (n - r + cs - 1) / cs : 0;    // own columns j = r + cs * jl
     extern __shared__ double sh[];
     const SyShared S = sy_layout(sh, n, ncm);
@@ -148,10 +142,10 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
     for (int jl = 0; jl < ncl; ++jl) {
         const int j = r + cs * jl;
         for (int i = tid; i < n; i += SY_THREADS)
-            S.A[(size_t)jl * n + i] = i >= j ? Gs[(size_t)j * n + i] : Gs[(size_t)i * n + j];
+            S.A[(size_t)jl * ld + i] = i >= j ? Gs[(size_t)j * n + i] : Gs[(size_t)i * n + j];
     }
     __syncthreads();
-    if (n >= 3 && r == 0) householder(S.A, 0, n, S.vb, Gs, d, e, tau, S.red, S.scal);
+    if (n >= 3 && r == 0 && warp == 0) householder_warp(S.A, 0, n, S.vb, Gs, d, e, tau, S.scal);
 
     for (int k = 0; k + 2 < n; ++k) {
         cl.sync();                                   // reflector k is in its owner's vb
@@ -162,21 +156,44 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
         }
         const double t = *cl.map_shared_rank(S.scal, o);
         __syncthreads();
-        // p_j = t A[:, j] . v (rows k+1 ..) for the own columns j > k; this CTA's share of p . v
+        // p_j = t A[:, j] . v (rows k+1 ..) for the na own columns j > k: thread (q, c) sums
+        // the rows of chunk q of column c, then one thread per column adds the chunks
         const int jl0 = k >= r ? (k - r) / cs + 1 : 0;
-        double part = 0.0;
-        for (int jl = jl0 + warp; jl < ncl; jl += SY_WARPS) {
-            const double* col = S.A + (size_t)jl * n;
-            double acc = 0.0;
-            for (int i = k + 1 + lane; i < n; i += 32) acc = fma(col[i], S.vl[i], acc);
-            acc = warp_sum(acc) * t;
-            if (lane == 0) {
-                S.pown[jl] = acc;
-                part = fma(acc, S.vl[r + cs * jl], part);
+        const int na = ncl - jl0;
+        if (na > 0) {
+            const int nq = min(SY_WARPS, max(1, SY_THREADS / na));
+            const int m = n - k - 1;
+            const int chunk = (m + nq - 1) / nq;
+            if (tid < nq * na) {
+                const int c = tid % na, q = tid / na;
+                const double* col = S.A + (size_t)(jl0 + c) * ld;
+                const int i1 = min(n, k + 1 + (q + 1) * chunk);
+                double acc = 0.0;
+                for (int i = k + 1 + q * chunk; i < i1; ++i) acc = fma(col[i], S.vl[i], acc);
+                S.part[q * na + c] = acc;
             }
+            __syncthreads();
+            double pv = 0.0;
+            if (tid < na) {
+                double sum = 0.0;
+                for (int q = 0; q < nq; ++q) sum += S.part[q * na + tid];
+                const double p = sum * t;
+                S.pown[jl0 + tid] = p;
+                pv = p * S.vl[r + cs * (jl0 + tid)];
+            }
+            if (warp * 32 < na) {
+                pv = warp_sum(pv);
+                if (lane == 0) S.red[warp] = pv;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                double sum = 0.0;
+                for (int w = 0; w * 32 < na; ++w) sum += S.red[w];
+                S.scal[1] = sum;
+            }
+        } else if (tid == 0) {
+            S.scal[1] = 0.0;
         }
-        part = block_sum(part, S.red);
-        if (tid == 0) S.scal[1] = part;
         cl.sync();                                   // every p_j and share of p . v is written
         double pv = lane < cs ? *cl.map_shared_rank(S.scal + 1, lane) : 0.0;
         pv = warp_sum(pv);
@@ -186,37 +203,40 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
             S.wl[i] = fma(-kc, S.vl[i], p);
         }
         __syncthreads();
-        // A -= v w^T + w v^T on the own columns j > k; column k + 1 first when it is ours and
-        // still needs a reflector
+        // A -= v w^T + w v^T on the own columns j > k. When column k + 1 is ours and still
+        // needs a reflector, warp 0 updates it and forms that reflector while the other warps
+        // update the rest (look-ahead: the next step's reflector is off the critical path).
         const int c = k + 1;
-        int done = -1;
-        if (c + 2 < n && c % cs == r) {
-            done = c / cs;
-            double* col = S.A + (size_t)done * n;
+        const bool look = c + 2 < n && c % cs == r;
+        const int jc = c / cs;
+        if (look && warp == 0) {
+            double* col = S.A + (size_t)jc * ld;
             const double vj = S.vl[c], wj = S.wl[c];
-            for (int i = k + 1 + tid; i < n; i += SY_THREADS)
-                col[i] -= fma(S.vl[i], wj, S.wl[i] * vj);
-            __syncthreads();
-            householder(col, c, n, S.vb, Gs + (size_t)c * n, d, e, tau, S.red, S.scal);
-        }
-        for (int jl = jl0 + warp; jl < ncl; jl += SY_WARPS) {
-            if (jl == done) continue;
-            const int j = r + cs * jl;
-            const double vj = S.vl[j], wj = S.wl[j];
-            double* col = S.A + (size_t)jl * n;
             for (int i = k + 1 + lane; i < n; i += 32) col[i] -= fma(S.vl[i], wj, S.wl[i] * vj);
+            __syncwarp();
+            householder_warp(col, c, n, S.vb, Gs + (size_t)c * n, d, e, tau, S.scal);
+        } else {
+            const int w0 = look ? 1 : 0, nw = SY_WARPS - w0;
+            for (int jl = jl0 + warp - w0; jl < ncl; jl += nw) {
+                if (look && jl == jc) continue;
+                const int j = r + cs * jl;
+                const double vj = S.vl[j], wj = S.wl[j];
+                double* col = S.A + (size_t)jl * ld;
+                for (int i = k + 1 + lane; i < n; i += 32)
+                    col[i] -= fma(S.vl[i], wj, S.wl[i] * vj);
+            }
         }
     }
     __syncthreads();
     // the trailing 2 x 2 (or 1 x 1) block
     if (tid == 0) {
         if (n >= 2 && (n - 2) % cs == r) {
-            const double* col = S.A + (size_t)((n - 2) / cs) * n;
+            const double* col = S.A + (size_t)((n - 2) / cs) * ld;
             d[n - 2] = col[n - 2];
             e[n - 2] = col[n - 1];
             tau[n - 2] = 0.0;
         }
-        if ((n - 1) % cs == r) d[n - 1] = S.A[(size_t)((n - 1) / cs) * n + n - 1];
+        if ((n - 1) % cs == r) d[n - 1] = S.A[(size_t)((n - 1) / cs) * ld + n - 1];
     }
     cl.sync();   // no CTA leaves while a peer may still read its shared memory
 }

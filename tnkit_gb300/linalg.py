@@ -431,6 +431,92 @@ def _gram_side(scale: str, R: int, Cc: int) -> int:
     return 1 if scale == "right" else 2 if scale == "left" else (1 if R <= Cc else 2)
 
 
+_PIN = {"buf": None, "done": None}
+
+
+def _pinned(nelem: int) -> torch.Tensor:
+    """A page-locked FP64 host buffer of at least nelem entries, reused across calls (the copy
+    that last read it has finished when it is handed out again)."""
+    if _PIN["done"] is not None:
+        _PIN["done"].synchronize()
+    buf = _PIN["buf"]
+    if buf is None or buf.numel() < nelem:
+        buf = torch.empty(max(nelem, 2 * (buf.numel() if buf is not None else 0), 1 << 16),
+                          dtype=torch.float64, pin_memory=True)
+        _PIN["buf"] = buf
+    return buf
+
+
+def _product_tables(prods, upper_only=False):
+    """Task, segment and tile tables (numpy, the tnk_gemm_* layouts) of several products
+    C_p = A_p B_p with C row-major (C(i, j) at c_off + i ldc + j): prods holds per product
+    (c_off, ldc, m, n, k, (a_buf, a_off, a_rs, a_cs), (b_buf, b_off, b_rs, b_cs)). With
+    upper_only, only the tiles that hold entries with i <= j (square symmetric outputs of which
+    only that triangle is read -- the lower triangle of the column-major view). Tiles longest K
+    first."""
+    from ._lib import GEMM_SEG, GEMM_TASK, GEMM_TILE
+    from .plan import TILE_M, TILE_N
+    tasks = np.zeros(len(prods), dtype=GEMM_TASK)
+    segs = np.zeros(len(prods), dtype=GEMM_SEG)
+    tiles = []
+    for t, (c_off, ldc, m, n, k, a, b) in enumerate(prods):
+        tasks[t] = (c_off, ldc, m, n, t, t + 1, 0)
+        segs[t] = (a[1], b[1], a[2], a[3], b[2], b[3], k, a[0], b[0], 0, 0, 1.0)
+        for m0 in range(0, m, TILE_M):
+            for n0 in range(0, n, TILE_N):
+                if upper_only and m0 > n0 + TILE_N - 1:
+                    continue
+                tiles.append((k, t, m0, n0))
+    tiles.sort(key=lambda x: -x[0])
+    tl = np.zeros(len(tiles), dtype=GEMM_TILE)
+    if tiles:
+        arr = np.asarray(tiles, dtype=np.int64)
+        tl["task"], tl["m0"], tl["n0"] = arr[:, 1], arr[:, 2], arr[:, 3]
+    return tasks, segs, tl
+
+
+def _grouped_products(prods, C_out: torch.Tensor, slots, upper_only=False):
+    """One tnk_grouped_gemm_f64 launch of _product_tables(prods, upper_only) with operand slots
+    `slots` (device addresses) and output base C_out. Returns the table tensor (to be kept
+    alive until the stream has run the launch)."""
+    tasks, segs, tl = _product_tables(prods, upper_only)
+    host = np.concatenate([tasks.view(np.uint8), segs.view(np.uint8), tl.view(np.uint8)])
+    dt = torch.from_numpy(host).to(C_out.device)
+    a0, a1 = tasks.nbytes, tasks.nbytes + segs.nbytes
+    sl = list(slots) + [0] * (4 - len(slots))
+    _lib.check(_lib.lib().tnk_grouped_gemm_f64(dt.data_ptr(), dt.data_ptr() + a0,
+                                               dt.data_ptr() + a1, len(tl), sl[0], sl[1], sl[2],
+                                               sl[3], C_out.data_ptr(), _lib.stream_ptr()),
+               "tnk_grouped_gemm_f64")
+    return dt
+
+
+def _gram_products(sectors):
+    """The Gram products of the device route for [(offset of M in slot 0, R, C, side,
+    offset of G)]: G = M M^T (side 1) or M^T M (side 2), n x n."""
+    prods = []
+    for mo, R, Cc, side, go in sectors:
+        n = R if side == 1 else Cc
+        if side == 1:          # A = M (R x C), B(k, j) = M[j, k]
+            prods.append((go, n, n, n, Cc, (0, mo, Cc, 1), (0, mo, 1, Cc)))
+        else:                  # A(i, k) = M[k, i], B = M
+            prods.append((go, n, n, n, R, (0, mo, 1, Cc), (0, mo, Cc, 1)))
+    return prods
+
+
+def _other_products(sectors):
+    """The other factor's products for [(offset of M in slot 0, R, C, side, offset of V in
+    slot 1, q kept, offset of the output)]: side 1: V (q x R) M, q x C; side 2: M V^T
+    (V q x C), R x q."""
+    prods = []
+    for mo, R, Cc, side, zo, q, po in sectors:
+        if side == 1:
+            prods.append((po, Cc, q, Cc, R, (1, zo, R, 1), (0, mo, Cc, 1)))
+        else:
+            prods.append((po, q, R, q, Cc, (0, mo, Cc, 1), (1, zo, 1, Cc)))
+    return prods
+
+
 def _gram_device_many(items, timing=None):
     """[(m, blocks, chi, scale, normalize)] -> [(U, S, Vh, disc)] by the device Gram route.
     With a dict `timing`, the phases' times in ms are added to it (CUDA events for the device
@@ -449,6 +535,7 @@ def _gram_device_many(items, timing=None):
         raise RuntimeError("the device Gram route needs thread-block clusters on a CUDA device")
     dev = items[0][0].data.device
     sp = _lib.stream_ptr()
+    keep = []                   # tables and buffers the stream still reads
     sec = []                    # (item, block index, M, side, n)
     for it, (m, blocks, chi, scale, normalize) in enumerate(items):
         for b, (_, _, M) in enumerate(blocks):
@@ -457,7 +544,10 @@ def _gram_device_many(items, timing=None):
             sec.append((it, b, M, side, R if side == 1 else Cc))
     on_dev = sorted([i for i, s in enumerate(sec) if s[4] <= nmax], key=lambda i: -sec[i][4])
     off_dev = [i for i, s in enumerate(sec) if s[4] > nmax]
-    # Gram matrices, packed (column-major = row-major: they are symmetric)
+    base = min(s[2].data_ptr() for s in sec)          # operand slot 0: the blocks' buffers
+    moff = {i: (s[2].data_ptr() - base) // 8 for i, s in enumerate(sec)}
+    # Gram matrices, packed; the reduction reads the lower triangle of the column-major view,
+    # which is the upper one of the row-major products written here
     tab = np.zeros((max(len(on_dev), 1), 4), dtype=np.int64)
     g = v = 0
     for r, i in enumerate(on_dev):
@@ -469,10 +559,10 @@ def _gram_device_many(items, timing=None):
     dv = torch.empty(3 * max(v, 1), dtype=torch.float64, device=dev)
     d, e, tau = dv[:max(v, 1)], dv[max(v, 1):2 * max(v, 1)], dv[2 * max(v, 1):]
     mark("gram0")
-    for r, i in enumerate(on_dev):
-        _, _, M, side, n = sec[i]
-        Gi = G[tab[r, 1]:tab[r, 1] + n * n].view(n, n)
-        torch.matmul(M, M.mT, out=Gi) if side == 1 else torch.matmul(M.mT, M, out=Gi)
+    prods = _gram_products([(moff[i], sec[i][2].shape[0], sec[i][2].shape[1], sec[i][3],
+                             int(tab[r, 1])) for r, i in enumerate(on_dev)])
+    if prods:
+        keep.append(_grouped_products(prods, G, [base], upper_only=True))
     facs = {}
     if on_dev:
         # one launch per cluster size, each over its sectors (largest first)
@@ -506,8 +596,6 @@ def _gram_device_many(items, timing=None):
         eig = hostlapack.tridiag_eigh_many(
             [(dh[tab[r, 2]:tab[r, 2] + tab[r, 0]], eh[tab[r, 2]:tab[r, 2] + tab[r, 0]])
              for r in range(len(on_dev))], lanes=_STEDC_LANES)
-        if timing is not None:
-            timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
     sig = {}
     for r, i in enumerate(on_dev):
         M = sec[i][2]
@@ -527,28 +615,64 @@ def _gram_device_many(items, timing=None):
         cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
         for j, i in enumerate(ids):
             kept[i] = int(cnt[j])
-    z = 0
-    zparts, items_orm = [], []
+    z = ns = 0
+    items_orm = []
     for r, i in enumerate(on_dev):
         n, q = int(tab[r, 0]), kept[i]
         tab[r, 3] = z
         if q:
-            Zf = eig[r][1]
-            zparts.append(np.ascontiguousarray(Zf[:, ::-1][:, :q].T))    # (q, n): Z column-major
             for c0 in range(0, q, 8):
                 items_orm.append((r, c0, min(8, q - c0), 0))
             z += q * n
-    if zparts:
-        Zd = torch.from_numpy(np.concatenate([p.reshape(-1) for p in zparts])).to(dev)
+            ns += q
+    if z:
+        # kept eigenvectors (descending) and their S through one page-locked buffer
+        pin = _pinned(z + ns)
+        hz = pin.numpy()
+        so = z
+        for r, i in enumerate(on_dev):
+            n, q = int(tab[r, 0]), kept[i]
+            if q:
+                Zf = eig[r][1]
+                o = int(tab[r, 3])
+                hz[o:o + q * n].reshape(q, n)[:] = Zf[:, n - q:][:, ::-1].T
+                hz[so:so + q] = sig[i][:q]
+                so += q
+        up = torch.empty(z + ns, dtype=torch.float64, device=dev)
+        up.copy_(pin[:z + ns], non_blocking=True)
+        _PIN["done"] = torch.cuda.Event()
+        _PIN["done"].record()
+        if timing is not None:
+            timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
+        Zd, S_all = up[:z], up[z:]
         tab_z = torch.from_numpy(tab).to(dev)
         it_d = torch.from_numpy(np.asarray(items_orm, dtype=np.int32)).to(dev)
+        keep += [tab_z, it_d]
         mark("back0")
         _lib.check(lib.tnk_ormtr_batched_f64(tab_z.data_ptr(), it_d.data_ptr(), len(items_orm),
                                              int(tab[:, 0].max()), G.data_ptr(), tau.data_ptr(),
                                              Zd.data_ptr(), sp), "tnk_ormtr_batched_f64")
         mark("back1")
-        S_all = torch.from_numpy(np.concatenate(
-            [sig[i][:kept[i]] for i in on_dev if kept[i]])).to(dev)
+        inv_all = torch.where(S_all > 0, 1.0 / torch.where(S_all > 0, S_all,
+                                                            torch.ones_like(S_all)),
+                              torch.zeros_like(S_all))
+        # the other factor of every sector in one launch: diag(1/S) V M or M V^T diag(1/S)
+        osec, poff, p = [], {}, 0
+        for r, i in enumerate(on_dev):
+            _, _, M, side, n = sec[i]
+            q = kept[i]
+            if not q:
+                continue
+            R, Cc = M.shape
+            poff[i] = p
+            osec.append((moff[i], R, Cc, side, int(tab[r, 3]), q, p))
+            p += q * (Cc if side == 1 else R)
+        prods = _other_products(osec)
+        P_all = torch.empty(max(p, 1), dtype=torch.float64, device=dev)
+        keep.append(_grouped_products(prods, P_all, [base, Zd.data_ptr()]))
+        mark("other1")
+    elif on_dev and timing is not None:
+        timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
     so = 0
     for r, i in enumerate(on_dev):
         _, _, M, side, n = sec[i]
@@ -558,14 +682,16 @@ def _gram_device_many(items, timing=None):
             facs[i] = (M.new_zeros((R, 0)), M.new_zeros(0), M.new_zeros((0, Cc)), sig[i])
             continue
         V = Zd[int(tab[r, 3]):int(tab[r, 3]) + q * n].view(q, n)   # row j: eigenvector j of G
-        S = S_all[so:so + q]
+        S, inv = S_all[so:so + q], inv_all[so:so + q]
         so += q
-        inv = torch.where(S > 0, 1.0 / torch.where(S > 0, S, torch.ones_like(S)),
-                          torch.zeros_like(S))
         if side == 1:
-            facs[i] = (V.mT, S, (V @ M) * inv[:, None], sig[i])
+            Vh = P_all[poff[i]:poff[i] + q * Cc].view(q, Cc)
+            Vh.mul_(inv[:, None])
+            facs[i] = (V.mT, S, Vh, sig[i])
         else:
-            facs[i] = ((M @ V.mT) * inv[None, :], S, V, sig[i])
+            U = P_all[poff[i]:poff[i] + R * q].view(R, q)
+            U.mul_(inv[None, :])
+            facs[i] = (U, S, V, sig[i])
     out = []
     for it, (m, blocks, chi, scale, normalize) in enumerate(items):
         ids = [i for i, s in enumerate(sec) if s[0] == it]
@@ -575,7 +701,8 @@ def _gram_device_many(items, timing=None):
         torch.cuda.synchronize(dev)
         span = lambda a, b: ev[a].elapsed_time(ev[b]) if a in ev and b in ev else 0.0
         for k, (a, b) in {"gram_ms": ("gram0", "red0"), "reduce_ms": ("red0", "red1"),
-                          "back_ms": ("back0", "back1"), "total_ms": ("gram0", "end")}.items():
+                          "back_ms": ("back0", "back1"), "other_ms": ("back1", "other1"),
+                          "total_ms": ("gram0", "end")}.items():
             timing[k] = timing.get(k, 0.0) + span(a, b)
         timing["sectors"] = len(sec)
         timing["sectors_on_device"] = len(on_dev)
@@ -590,8 +717,10 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     """U, S, Vh, disc of a two-leg block matrix, keeping the `chi` largest singular values over
     all sectors. `scale` folds S into the kept factor ('right': rows of Vh, 'left': columns of U,
     'none'), with S normalised to unit norm first, as the sweep does (tnkit/_dmrg.py:705-714).
-    With method='gram', `host` chooses where the sectors are factored: 'auto' (split between the
-    GPU and host LAPACK by cost), 'never' (GPU only) or 'always' (host only). For scale
+    With method='gram', `host` chooses where the sectors are factored: 'device' (below; what
+    'auto' means for FP64 CUDA blocks with scale 'right' / 'left' where the device supports it),
+    'auto' otherwise (split between cuSOLVER and host LAPACK by cost), 'never' (each sector on
+    cuSOLVER) or 'always' (host LAPACK only). For scale
     'right' / 'left' the side the sweep keeps canonical (U / Vh) of a near-square sector comes
     straight from its own Gram matrix and the other is the exact projection, with S the square
     roots of the Gram eigenvalues; gram_qr=True keeps the reference's form (the smaller Gram
@@ -608,6 +737,10 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
         raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
+    if host == "auto" and method == "gram" and not gram_qr and dtype == torch.float64 and \
+            scale in ("right", "left") and m.data.is_cuda and m.data.dtype == torch.float64 \
+            and device_gram_available():
+        host = "device"
     if host == "device":
         if method != "gram" or gram_qr or dtype != torch.float64 or not m.data.is_cuda or \
                 m.data.dtype != torch.float64:
@@ -691,6 +824,10 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
         raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if method not in ("svd", "gram"):
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
+    if host == "auto" and method == "gram" and all(sc in ("right", "left") for _, _, sc in items) \
+            and all(m.data.is_cuda and m.data.dtype == torch.float64 for m, _, _ in items) \
+            and device_gram_available():
+        host = "device"
     if host == "device":
         if method != "gram":
             raise ValueError("host='device' is the Gram route")
