@@ -615,14 +615,19 @@ def _gram_device_many(items, timing=None):
         cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
         for j, i in enumerate(ids):
             kept[i] = int(cnt[j])
+    # back-transformation items: column chunks of up to 8 (one warp each); a bond whose kept
+    # columns would not give every SM two CTAs gets chunks of 2, so its largest sectors spread
+    # over more SMs (the work is FP64-bound, ~n^2 FMAs per column)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    chunk = 8 if sum((kept[i] + 7) // 8 for i in on_dev) >= 2 * n_sm else 2
     z = ns = 0
     items_orm = []
     for r, i in enumerate(on_dev):
         n, q = int(tab[r, 0]), kept[i]
         tab[r, 3] = z
         if q:
-            for c0 in range(0, q, 8):
-                items_orm.append((r, c0, min(8, q - c0), 0))
+            for c0 in range(0, q, chunk):
+                items_orm.append((r, c0, min(chunk, q - c0), 0))
             z += q * n
             ns += q
     if z:
