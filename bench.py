@@ -777,14 +777,16 @@ def batch_dmrg_leg(torch, args):
     def mk(m, g, N):
         return workloads.tfim_mpo(N, g) if m == "tfim" else \
             to_block_mpo(workloads.xxz_mpo(N, g), [[1, -1]] * N)[0]
-    kw = dict(n_sweeps=args.batch_sweeps, tol=0, rtol=0, expand=0)
+    kw = dict(n_sweeps=args.batch_sweeps, tol=0, rtol=0, expand=0, svd_method=args.svd_method,
+              svd_host=args.svd_host)
     dmrg_batch([mk("tfim", 1.0, 8), mk("xxz", 1.0, 8)], [16, 16], charges=[None, 0],
                **dict(kw, n_sweeps=1))
     dmrg(mk("xxz", 1.0, 8), 16, charge=0, **dict(kw, n_sweeps=1))
     torch.cuda.synchronize()
     out = {"workload": f"DMRG of {len(sel)} chains (the first {half} transverse-field Ising and "
                        f"first {half} U(1) XXZ chains of the 64-chain seed-2 draws), "
-                       f"{args.batch_sweeps} sweeps each, seeds 0..{len(sel) - 1}",
+                       f"{args.batch_sweeps} sweeps each, seeds 0..{len(sel) - 1}, "
+                       f"truncation '{args.svd_method}' (host '{args.svd_host}')",
            "chains": [list(d) for d in sel]}
     for prec in ("f64", "ff", "mixed"):
         t0 = time.perf_counter()

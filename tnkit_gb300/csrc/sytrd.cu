@@ -58,7 +58,6 @@ struct SyShared {
     double* wl;     // n: the current w
     double* pown;   // ncm: p of the own columns (read by the peers)
     double* part;   // SY_THREADS: partial column dot products
-    double* red;    // SY_WARPS: reductions
     double* scal;   // 2: tau of the reflector in vb, this CTA's share of p . v
 };
 
@@ -66,7 +65,7 @@ __host__ __device__ inline int64_t sy_ld(int64_t n) { return n | 1; }
 
 __host__ __device__ inline int64_t sy_shared_doubles(int64_t n, int cs) {
     const int64_t ncm = (n + cs - 1) / cs;
-    return ncm * sy_ld(n) + 3 * n + ncm + SY_THREADS + SY_WARPS + 2;
+    return ncm * sy_ld(n) + 3 * n + ncm + SY_THREADS + 2;
 }
 
 __device__ SyShared sy_layout(double* sh, int n, int ncm) {
@@ -77,8 +76,7 @@ __device__ SyShared sy_layout(double* sh, int n, int ncm) {
     s.wl = s.vl + n;
     s.pown = s.wl + n;
     s.part = s.pown + ncm;
-    s.red = s.part + SY_THREADS;
-    s.scal = s.red + SY_WARPS;
+    s.scal = s.part + SY_THREADS;
     return s;
 }
 
@@ -150,11 +148,12 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
     for (int k = 0; k + 2 < n; ++k) {
         cl.sync();                                   // reflector k is in its owner's vb
         const int o = k % cs;
+        // the reflector and its tau from the owner (independent remote loads, issued together)
+        const double t = *cl.map_shared_rank(S.scal, o);
         {
             const double* rv = cl.map_shared_rank(S.vb, o);
             for (int i = k + 1 + tid; i < n; i += SY_THREADS) S.vl[i] = rv[i];
         }
-        const double t = *cl.map_shared_rank(S.scal, o);
         __syncthreads();
         // p_j = t A[:, j] . v (rows k+1 ..) for the na own columns j > k: thread (q, c) sums
         // the rows of chunk q of column c, then one thread per column adds the chunks
@@ -173,34 +172,49 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
                 S.part[q * na + c] = acc;
             }
             __syncthreads();
-            double pv = 0.0;
-            if (tid < na) {
-                double sum = 0.0;
-                for (int q = 0; q < nq; ++q) sum += S.part[q * na + tid];
-                const double p = sum * t;
-                S.pown[jl0 + tid] = p;
-                pv = p * S.vl[r + cs * (jl0 + tid)];
-            }
-            if (warp * 32 < na) {
+            // warp 0 adds the chunks of every column (lanes c, c + 32), forms p_j and this CTA's
+            // share of p . v; the cluster barrier below publishes them
+            if (warp == 0) {
+                double pv = 0.0;
+                for (int c = lane; c < na; c += 32) {
+                    double sum = 0.0;
+                    for (int q = 0; q < nq; ++q) sum += S.part[q * na + c];
+                    const double p = sum * t;
+                    S.pown[jl0 + c] = p;
+                    pv = fma(p, S.vl[r + cs * (jl0 + c)], pv);
+                }
                 pv = warp_sum(pv);
-                if (lane == 0) S.red[warp] = pv;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                double sum = 0.0;
-                for (int w = 0; w * 32 < na; ++w) sum += S.red[w];
-                S.scal[1] = sum;
+                if (lane == 0) S.scal[1] = pv;
             }
         } else if (tid == 0) {
             S.scal[1] = 0.0;
         }
         cl.sync();                                   // every p_j and share of p . v is written
+        // the shares of p . v and this thread's p entries from the peers, loaded together
         double pv = lane < cs ? *cl.map_shared_rank(S.scal + 1, lane) : 0.0;
+        constexpr int PG = 4;                        // p entries per thread per pass
+        double pg[PG];
+        int i0 = k + 1 + tid;
+#pragma unroll
+        for (int u = 0; u < PG; ++u) {
+            const int i = i0 + u * SY_THREADS;
+            pg[u] = i < n ? cl.map_shared_rank(S.pown, i % cs)[i / cs] : 0.0;
+        }
         pv = warp_sum(pv);
         const double kc = 0.5 * t * pv;
-        for (int i = k + 1 + tid; i < n; i += SY_THREADS) {
-            const double p = cl.map_shared_rank(S.pown, i % cs)[i / cs];
-            S.wl[i] = fma(-kc, S.vl[i], p);
+        for (;;) {
+#pragma unroll
+            for (int u = 0; u < PG; ++u) {
+                const int i = i0 + u * SY_THREADS;
+                if (i < n) S.wl[i] = fma(-kc, S.vl[i], pg[u]);
+            }
+            i0 += PG * SY_THREADS;
+            if (i0 >= n) break;
+#pragma unroll
+            for (int u = 0; u < PG; ++u) {
+                const int i = i0 + u * SY_THREADS;
+                pg[u] = i < n ? cl.map_shared_rank(S.pown, i % cs)[i / cs] : 0.0;
+            }
         }
         __syncthreads();
         // A -= v w^T + w v^T on the own columns j > k. When column k + 1 is ours and still
@@ -212,7 +226,8 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
         if (look && warp == 0) {
             double* col = S.A + (size_t)jc * ld;
             const double vj = S.vl[c], wj = S.wl[c];
-            for (int i = k + 1 + lane; i < n; i += 32) col[i] -= fma(S.vl[i], wj, S.wl[i] * vj);
+            for (int i = k + 1 + lane; i < n; i += 32)
+                col[i] = fma(-S.vl[i], wj, fma(-S.wl[i], vj, col[i]));
             __syncwarp();
             householder_warp(col, c, n, S.vb, Gs + (size_t)c * n, d, e, tau, S.scal);
         } else {
@@ -223,7 +238,7 @@ __global__ void __launch_bounds__(SY_THREADS, 1)
                 const double vj = S.vl[j], wj = S.wl[j];
                 double* col = S.A + (size_t)jl * ld;
                 for (int i = k + 1 + lane; i < n; i += 32)
-                    col[i] -= fma(S.vl[i], wj, S.wl[i] * vj);
+                    col[i] = fma(-S.vl[i], wj, fma(-S.wl[i], vj, col[i]));
             }
         }
     }

@@ -8,11 +8,15 @@ SVD with the global cut across sectors, the per-block LQ of the initial canonica
                           (-sigma, position), new bond sectors labelled by the row charge
   lq                      tnkit/blocks.py:1465-1495 (right=True)
 
-The per-sector factorisations run on cuSOLVER/cuBLAS, FP64 on the GPU, from a thread pool with one
-stream per sector: method='gram' on real blocks is one library call per sector
-(tnk_svd_gram_f64, which releases the interpreter lock and hands back S on the host), 'svd' and
-complex blocks go through torch.linalg. Only the singular values cross to the host, once per
-bond.
+Factorisations. method='gram' on FP64 CUDA blocks cut the way a sweep cuts (scale 'right' /
+'left') takes the device route (_gram_device_many): every sector's Gram matrix, Householder
+reduction to tridiagonal form, back-transformation of the kept vectors and other factor on the
+GPU in a handful of launches for the whole bond (csrc/sytrd.cu, grouped GEMMs), the tridiagonal
+eigenproblems on host threads (hostlapack.py, O(n^2) each), the cut on the host. Otherwise the
+Gram route is one library call per sector (tnk_svd_gram_f64 on cuSOLVER, from a thread pool
+with one stream per sector, optionally with a host LAPACK share); 'svd' and complex blocks go
+through torch.linalg. Only the singular values (and, on the device route, the tridiagonals and
+the kept tridiagonal eigenvectors) cross between host and device, once per bond.
 """
 from __future__ import annotations
 
@@ -187,7 +191,8 @@ def _svd_gram_native(M: torch.Tensor, orth: int = 0):
     return U, S, Vh, s_host
 
 
-# --- host co-processing of the truncation -----------------------------------------------------
+# --- host co-processing of the per-sector route ------------------------------------------------
+# (host='auto' where the device route does not apply, and host='always')
 # A chi=1024 bond's largest sectors (~520 rows) are latency-bound in cuSOLVER: one Gram
 # factorisation takes ~17 ms, and calls on several streams do not overlap (the GPU path is one
 # lane). The host's cores are idle during the truncation, and host LAPACK calls from several
