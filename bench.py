@@ -515,7 +515,8 @@ def trunc_leg(torch, dev, dgemm, reps):
     left-to-right sweep cuts) on each Gram route: 'device' (the sectors' reductions and the
     back-transformation of the kept vectors on the GPU, tridiagonal problems on host threads),
     'never' (each sector's eigh on cuSOLVER), 'always' (each sector's eigh on host LAPACK,
-    sectors over host threads). The spectra are compared sorted: below ~1e-8 of the largest
+    sectors over host threads); and the exact route (method='svd', the reference's default) on
+    the device against torch.linalg.svd per sector. The spectra are compared sorted: below ~1e-8 of the largest
     value the Gram route resolves nothing, so which sector a value that small lands in is
     rounding, and the routes' bonds may differ there."""
     from tnkit_gb300 import linalg as LA
@@ -543,6 +544,31 @@ def trunc_leg(torch, dev, dgemm, reps):
         S = torch.sort(res[host][1], descending=True).values
         out[host]["max_abs_dsigma2_vs_never"] = float((S ** 2 - S0 ** 2).abs().max())
         out[host]["discarded"] = res[host][3]
+    # the exact route (method='svd', the reference's default): device bidiagonalisation against
+    # torch.linalg.svd per sector
+    if LA.device_svd_available():
+        ex = {}
+        for host in ("device", "never"):
+            for _ in range(2):
+                r = LA.truncated_svd(m, 1024, scale="right", method="svd", host=host)
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(max(3, reps // 3) if host == "never" else reps):
+                t0 = time.perf_counter()
+                r = LA.truncated_svd(m, 1024, scale="right", method="svd", host=host)
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            ex[host] = r
+            out[f"svd_{host}"] = {"ms_median": float(np.median(ts)) * 1e3,
+                                  "ms_min": float(min(ts)) * 1e3, "discarded": r[3]}
+        Sa = torch.sort(ex["device"][1], descending=True).values
+        Sb = torch.sort(ex["never"][1], descending=True).values
+        out["svd_device"]["max_abs_dsigma_vs_torch"] = float((Sa - Sb).abs().max())
+        tm = {}
+        for _ in range(reps):
+            blocks = list(LA._blocks(m))
+            LA._svd_device_many([(m, blocks, 1024, "right", True)], timing=tm)
+        out["svd_device_phases_ms"] = {k: v / reps for k, v in tm.items() if k.endswith("_ms")}
     if "device" in res:
         tm = {}
         for _ in range(reps):

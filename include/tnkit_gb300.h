@@ -447,6 +447,38 @@ int tnk_ormtr_batched_f64(const tnk_sytrd_sector* sectors, const tnk_ormtr_item*
                           int32_t n_items, int32_t n_max, const double* G, const double* tau,
                           double* Z, void* stream);
 
+/* The O(n^3) steps of the exact per-sector SVD of the truncation (method='svd', the reference's
+ * default, tnkit/blocks.py:1310-1344 inside :1380-1462) for all sectors of a bond at once: the
+ * Householder bidiagonalisation A = Q_L B Q_R^T of every sector's m x n working matrix (m >= n:
+ * the block, or its transpose) in one launch (one thread-block cluster per sector, the matrix
+ * resident in the cluster's distributed shared memory), and the back-transformations of the
+ * singular vectors the cut keeps (tnk_ormqr_batched_f64). Between them, the caller solves the
+ * bidiagonal SVDs (d, e). Sector s: A(i, j) = M[a_off + i a_rs + j a_cs]; its left reflectors
+ * (column k: u_k in rows k .. m-1, u_k[k] = 1) into the m x n column-major matrix at
+ * UL + ul_off, its right reflectors (column k: v_k in rows k+1 .. n-1, v_k[k+1] = 1) into the
+ * n x n column-major matrix at VR + vr_off, and d (n), e (n - 1), tau_u (n), tau_v (n - 2) at
+ * vec + v_off + {0, n, 2n, 3n}. Tables are device memory; the calls only enqueue work. */
+typedef struct {
+    int64_t m, n, a_off, ul_off, vr_off, v_off, spare;
+    int32_t a_rs, a_cs;
+} tnk_gebrd_sector;                  /* 64 bytes */
+/* Z <- H_0 H_1 ... H_{nrefl-1} Z: reflector k in column k of the rows x nrefl column-major
+ * matrix at R + r_off, from row k + shift (that entry 1) to rows - 1, its tau at
+ * tau + tau_off + k; Z column-major rows x (columns named by the items), at Z + z_off. */
+typedef struct {
+    int64_t rows, nrefl, r_off, tau_off, z_off;
+    int32_t shift, pad;
+} tnk_refl_set;                      /* 48 bytes */
+/* The largest m (with n <= m) the bidiagonalisation takes with clusters of `cluster` CTAs on
+ * the current device; 0 when such clusters cannot be launched there. */
+int tnk_gebrd_limits(int32_t cluster, int32_t* m_max);
+int tnk_gebrd_batched_f64(const tnk_gebrd_sector* sectors, int32_t n_sectors, int32_t m_max,
+                          int32_t n_max, int32_t cluster, const double* M, double* UL,
+                          double* VR, double* vec, void* stream);
+int tnk_ormqr_batched_f64(const tnk_refl_set* sets, const tnk_ormtr_item* items,
+                          int32_t n_items, int32_t rows_max, const double* R, const double* tau,
+                          double* Z, void* stream);
+
 /* ----------------------------------------------------------------------------------------
  * Host planner: the block tables of the one- and two-site H_eff contraction (the stage-1 /
  * stage-2 / stage-3 tables above) built natively from the layouts' sector keys, and their

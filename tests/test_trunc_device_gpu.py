@@ -186,3 +186,128 @@ def test_dmrg_on_device_route_matches_reference(N, chi):
     assert abs(E - ref["E"]) <= 1e-10, (E, ref["E"])
     for m, b in zip(M, ref["bonds"]):
         assert list(m.legs[2].dims) == b["dims"] and list(m.legs[2].charges) == b["charges"]
+
+
+# ---- the exact route (method='svd') ---------------------------------------------------------
+
+def _graded(R, C, seed, span=12.0):
+    rng = np.random.default_rng(seed)
+    k = min(R, C)
+    U, _ = np.linalg.qr(rng.standard_normal((R, k)))
+    V, _ = np.linalg.qr(rng.standard_normal((C, k)))
+    s = 10.0 ** (-np.linspace(0.0, span, k))
+    return (U * s) @ V.T, s
+
+
+@pytest.mark.parametrize("cs", [1, 4, 16])
+def test_bidiagonalisation_and_back_transformation(cs):
+    """Blocks of several shapes (tall, wide through the transpose, square, one row/column) in one
+    launch: B's singular values are the block's to FP64 accuracy, the back-transformed vectors
+    are orthonormal and reconstruct the block."""
+    from tnkit_gb300 import _lib, hostlapack
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300._lib import GEBRD_SECTOR, REFL_SET
+    lib = _lib.lib()
+    mmax = LA._gebrd_table()[cs]
+    if mmax == 0:
+        pytest.skip(f"clusters of {cs} cannot launch here")
+    shapes = [(s0, s1) for s0, s1 in ((1, 1), (5, 1), (1, 4), (3, 3), (40, 17), (17, 40),
+                                      (130, 100), (300, 300), (mmax, mmax - 7))
+              if max(s0, s1) <= mmax]
+    mats = [_graded(R, C, 7 + R + 3 * C)[0] for R, C in shapes]
+    buf = np.concatenate([M.reshape(-1) for M in mats])
+    Md = torch.as_tensor(buf, device="cuda")
+    tab = np.zeros(len(shapes), dtype=GEBRD_SECTOR)
+    a = refl = vo = 0
+    for r, (R, C) in enumerate(shapes):
+        tr = R < C
+        mm, nn = max(R, C), min(R, C)
+        tab[r] = (mm, nn, a, refl, refl + mm * nn, vo, 0, 1 if tr else C, C if tr else 1)
+        a += R * C
+        refl += mm * nn + nn * nn
+        vo += 4 * nn
+    RF = torch.zeros(refl, dtype=torch.float64, device="cuda")
+    vec = torch.zeros(vo, dtype=torch.float64, device="cuda")
+    tab_d = torch.as_tensor(tab.view(np.uint8), device="cuda")
+    sp = _lib.stream_ptr()
+    _lib.check(lib.tnk_gebrd_batched_f64(tab_d.data_ptr(), len(shapes), int(tab["m"].max()),
+                                         int(tab["n"].max()), cs, Md.data_ptr(), RF.data_ptr(),
+                                         RF.data_ptr(), vec.data_ptr(), sp), "gebrd")
+    vh = vec.cpu().numpy()
+    sets, items, zs, z = [], [], [], 0
+    res = []
+    for r, (R, C) in enumerate(shapes):
+        mm, nn, v0 = int(tab[r]["m"]), int(tab[r]["n"]), int(tab[r]["v_off"])
+        s, Ub, VTb = hostlapack.bidiag_svd(vh[v0:v0 + nn], vh[v0 + nn:v0 + 2 * nn])
+        ref = np.linalg.svd(mats[r], compute_uv=False)
+        assert np.abs(s - ref).max() <= 1e-13 * ref[0], (R, C)
+        res.append(s)
+        zl = np.zeros((nn, mm))
+        zl[:, :nn] = Ub.T
+        zs += [zl.reshape(-1), np.ascontiguousarray(VTb).reshape(-1)]
+        sets.append((mm, nn, int(tab[r]["ul_off"]), v0 + 2 * nn, z, 0, 0))
+        sets.append((nn, max(nn - 2, 0), int(tab[r]["vr_off"]), v0 + 3 * nn, z + mm * nn, 1, 0))
+        for si in (len(sets) - 2, len(sets) - 1):
+            for c0 in range(0, nn, 8):
+                items.append((si, c0, min(8, nn - c0), 0))
+        z += (mm + nn) * nn
+    st = np.zeros(len(sets), dtype=REFL_SET)
+    arr = np.asarray(sets, dtype=np.int64)
+    for f, name in enumerate(("rows", "nrefl", "r_off", "tau_off", "z_off", "shift", "pad")):
+        st[name] = arr[:, f]
+    Zd = torch.as_tensor(np.concatenate(zs), device="cuda")
+    st_d = torch.as_tensor(st.view(np.uint8), device="cuda")
+    it_d = torch.as_tensor(np.asarray(items, np.int32), device="cuda")
+    _lib.check(lib.tnk_ormqr_batched_f64(st_d.data_ptr(), it_d.data_ptr(), len(items),
+                                         int(st["rows"].max()), RF.data_ptr(), vec.data_ptr(),
+                                         Zd.data_ptr(), sp), "ormqr")
+    Zh = Zd.cpu().numpy()
+    for r, (R, C) in enumerate(shapes):
+        mm, nn = int(tab[r]["m"]), int(tab[r]["n"])
+        zl, zr = int(st[2 * r]["z_off"]), int(st[2 * r + 1]["z_off"])
+        Lq = Zh[zl:zl + mm * nn].reshape(nn, mm).T
+        Rq = Zh[zr:zr + nn * nn].reshape(nn, nn).T
+        U, V = (Lq, Rq) if R >= C else (Rq, Lq)
+        assert np.abs(U.T @ U - np.eye(nn)).max() <= 1e-13, (R, C)
+        assert np.abs(V.T @ V - np.eye(nn)).max() <= 1e-13, (R, C)
+        assert np.abs((U * res[r]) @ V.T - mats[r]).max() <= 1e-13, (R, C)
+
+
+@pytest.mark.parametrize("scale", ["right", "left", "none"])
+def test_exact_device_route_matches_torch_svd(scale):
+    """truncated_svd(method='svd') on the device route against torch.linalg.svd per sector:
+    the same kept values (1e-13 of the largest), bond, discarded weight (1e-12 of the total) and
+    truncated matrix; orthonormal factors."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(31)
+    a = Leg((-2, 0, 2), (60, 310, 140), 1)
+    b = Leg((-2, 0, 2), (70, 300, 150), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size) * np.repeat(10.0 ** -np.linspace(0, 3, lay.nblocks),
+                                                   [int(x) for x in lay.sizes])
+    h /= np.linalg.norm(h)
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    dn = lambda t: to_dense_np(t.layout, t.data.cpu().numpy())
+    U, S, V, disc = LA.truncated_svd(m, 250, scale=scale, method="svd", host="device")
+    U0, S0, V0, disc0 = LA.truncated_svd(m, 250, scale=scale, method="svd", host="never")
+    assert U.layout.legs == U0.layout.legs and V.layout.legs == V0.layout.legs
+    assert float((S - S0).abs().max()) <= 1e-13 * float(S0.max())
+    assert abs(disc - disc0) <= 1e-12
+    mid = np.ones_like(S.cpu().numpy()) if scale != "none" else S.cpu().numpy()
+    assert np.abs((dn(U) * mid) @ dn(V) - (dn(U0) * mid) @ dn(V0)).max() <= 1e-12
+    iso = dn(U) if scale != "left" else dn(V).T
+    assert np.abs(iso.T @ iso - np.eye(iso.shape[1])).max() <= 1e-12
+
+
+def test_exact_device_route_mid_bond():
+    """The chi=1024 mid-bond block on the exact device route: the same spectrum as
+    torch.linalg.svd per sector to 1e-14 of the largest value."""
+    from tnkit_gb300 import linalg as LA
+    mat = _mid_bond_matrix(5)
+    U, S, V, disc = LA.truncated_svd(mat, 1024, scale="right", method="svd", host="device")
+    U0, S0, V0, disc0 = LA.truncated_svd(mat, 1024, scale="right", method="svd", host="never")
+    assert U.layout.legs == U0.layout.legs
+    assert float((S - S0).abs().max()) <= 1e-14 * float(S0.max()) * 10
+    assert abs(disc - disc0) <= 1e-12

@@ -38,6 +38,11 @@ GEMM_SEG = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("a_rs", "<i4"), ("a_cs
                      ("b_rs", "<i4"), ("b_cs", "<i4"), ("k", "<i4"), ("a_buf", "<i2"),
                      ("b_buf", "<i2"), ("conj", "<i4"), ("pad", "<i4"), ("coef", "<f8")])
 GEMM_TILE = np.dtype([("task", "<i4"), ("m0", "<i4"), ("n0", "<i4"), ("pad", "<i4")])
+GEBRD_SECTOR = np.dtype([("m", "<i8"), ("n", "<i8"), ("a_off", "<i8"), ("ul_off", "<i8"),
+                         ("vr_off", "<i8"), ("v_off", "<i8"), ("spare", "<i8"), ("a_rs", "<i4"),
+                         ("a_cs", "<i4")])
+REFL_SET = np.dtype([("rows", "<i8"), ("nrefl", "<i8"), ("r_off", "<i8"), ("tau_off", "<i8"),
+                     ("z_off", "<i8"), ("shift", "<i4"), ("pad", "<i4")])
 COMB_TASK = np.dtype([("dst_off", "<i8"), ("rows", "<i4"), ("cols", "<i4"), ("dst_ld", "<i4"),
                       ("dst_cs", "<i4"), ("term_begin", "<i4"), ("term_end", "<i4")])
 COMB_TERM = np.dtype([("src_off", "<i8"), ("src_ld", "<i4"), ("src_cs", "<i4"),
@@ -147,6 +152,9 @@ _SIGS = {
     "tnk_sytrd_limits": ([_I32, _P], C.c_int),
     "tnk_sytrd_batched_f64": ([_P, _I32, _I32, _I32, _P, _P, _P, _P, _P], C.c_int),
     "tnk_ormtr_batched_f64": ([_P, _P, _I32, _I32, _P, _P, _P, _P], C.c_int),
+    "tnk_gebrd_limits": ([_I32, _P], C.c_int),
+    "tnk_gebrd_batched_f64": ([_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P], C.c_int),
+    "tnk_ormqr_batched_f64": ([_P, _P, _I32, _I32, _P, _P, _P, _P], C.c_int),
     "tnk_apply_plan_build": ([_P, _P], C.c_int),
     "tnk_plan_tc_build": ([_P, _I64, _P, _P, _I64, _P, _I64, _P, _P], C.c_int),
     "tnk_env_plan_build": ([_P, _P], C.c_int),

@@ -13,6 +13,10 @@ static_assert(sizeof(tnk_gemm_tile) == 16, "tnk_gemm_tile layout");
 static_assert(sizeof(tnk_comb_task) == 32, "tnk_comb_task layout");
 static_assert(sizeof(tnk_comb_term) == 24, "tnk_comb_term layout");
 static_assert(sizeof(tnk_comb_item) == 16, "tnk_comb_item layout");
+static_assert(sizeof(tnk_sytrd_sector) == 32, "tnk_sytrd_sector layout");
+static_assert(sizeof(tnk_ormtr_item) == 16, "tnk_ormtr_item layout");
+static_assert(sizeof(tnk_gebrd_sector) == 64, "tnk_gebrd_sector layout");
+static_assert(sizeof(tnk_refl_set) == 48, "tnk_refl_set layout");
 
 namespace tnk {
 

@@ -721,6 +721,242 @@ def _gram_device_many(items, timing=None):
     return out
 
 
+# --- the device exact route --------------------------------------------------------------------
+# Every sector's exact SVD (the reference's default method='svd') as LAPACK's dgesdd computes
+# it: the Householder bidiagonalisation of the block (or its transpose, m >= n) in one launch per
+# cluster size (tnk_gebrd_batched_f64), the bidiagonal SVDs on host threads
+# (hostlapack.bidiag_svd_many, O(n^2) each), the global cut, then the back-transformation of the
+# kept left and right singular vectors in one launch (tnk_ormqr_batched_f64). Sectors larger
+# than the reduction takes go through torch.linalg.svd.
+_GEBRD = {"limits": None}
+_GB_STEP_S = {1: 1.0e-6, 2: 2.6e-6, 4: 2.7e-6, 8: 2.8e-6, 16: 3.0e-6}
+
+
+def _gebrd_table():
+    if _GEBRD["limits"] is None:
+        lib = _lib.lib()
+        lim = {}
+        for cs in (1, 2, 4, 8, 16):
+            nm = C.c_int32(0)
+            _lib.check(lib.tnk_gebrd_limits(cs, C.byref(nm)), "tnk_gebrd_limits")
+            lim[cs] = int(nm.value)
+        _GEBRD["limits"] = lim
+    return _GEBRD["limits"]
+
+
+def device_svd_available() -> bool:
+    """Whether the device exact route can run here."""
+    from . import hostlapack
+    if not torch.cuda.is_available() or not hostlapack.available():
+        return False
+    return max(_gebrd_table().values()) > 0
+
+
+def _gebrd_clusters(shapes, n_sm: int):
+    """A cluster size per (m, n) block (m >= n), as _sytrd_clusters chooses them: each block's
+    fastest alone by a time model (~4 m n^2 FP64 FMAs over the cluster, four cluster barriers
+    per column), then halvings while the clusters need more than one wave of the SMs."""
+    lim = _gebrd_table()
+    ok = lambda m, c: lim.get(c, 0) >= m
+    t = lambda m, n, c: 4.0 * (m * n * n - n ** 3 / 3.0) / (c * _SY_FMA_PER_S) + n * _GB_STEP_S[c]
+    cs = []
+    for m, n in shapes:
+        cands = [c for c in (1, 2, 4, 8, 16) if ok(m, c)]
+        cs.append(min(cands, key=lambda c: t(m, n, c)) if cands else 0)
+    while sum(cs) > n_sm:
+        best, cost = None, None
+        for i, ((m, n), c) in enumerate(zip(shapes, cs)):
+            if c > 1 and ok(m, c // 2):
+                dlt = t(m, n, c // 2) - t(m, n, c)
+                if cost is None or dlt < cost:
+                    best, cost = i, dlt
+        if best is None:
+            break
+        cs[best] //= 2
+    return cs
+
+
+def _svd_device_many(items, timing=None):
+    """[(m, blocks, chi, scale, normalize)] -> [(U, S, Vh, disc)] by the device exact route
+    (see above). With a dict `timing`, phase times in ms are added to it."""
+    import time
+    from . import hostlapack
+    from ._lib import GEBRD_SECTOR, REFL_SET
+    lib = _lib.lib()
+    ev = {}
+
+    def mark(name):
+        if timing is not None:
+            ev[name] = torch.cuda.Event(enable_timing=True)
+            ev[name].record()
+    lim = _gebrd_table()
+    mmax_dev = max(lim.values())
+    if mmax_dev <= 0:
+        raise RuntimeError("the device exact route needs thread-block clusters on a CUDA device")
+    dev = items[0][0].data.device
+    sp = _lib.stream_ptr()
+    keep = []
+    sec = []                    # (item, block index, M, transposed, m, n)
+    for it, (mt, blocks, chi, scale, normalize) in enumerate(items):
+        for b, (_, _, M) in enumerate(blocks):
+            R, Cc = M.shape
+            tr = R < Cc
+            sec.append((it, b, M, tr, max(R, Cc), min(R, Cc)))
+    on_dev = sorted([i for i, s in enumerate(sec) if s[4] <= mmax_dev],
+                    key=lambda i: -(sec[i][4] * sec[i][5] ** 2))
+    off_dev = [i for i, s in enumerate(sec) if s[4] > mmax_dev]
+    base = min(s[2].data_ptr() for s in sec)
+    tab = np.zeros(max(len(on_dev), 1), dtype=GEBRD_SECTOR)
+    refl = vo = 0
+    for r, i in enumerate(on_dev):
+        _, _, M, tr, mm, nn = sec[i]
+        Cc = M.shape[1]
+        tab[r] = (mm, nn, (M.data_ptr() - base) // 8, refl, refl + mm * nn, vo, 0,
+                  1 if tr else Cc, Cc if tr else 1)
+        refl += mm * nn + nn * nn
+        vo += 4 * nn
+    RF = torch.empty(max(refl, 1), dtype=torch.float64, device=dev)
+    vec = torch.zeros(max(vo, 1), dtype=torch.float64, device=dev)
+    facs = {}
+    if on_dev:
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        cls = _gebrd_clusters([(int(tab[r]["m"]), int(tab[r]["n"])) for r in range(len(on_dev))],
+                              n_sm)
+        main = torch.cuda.current_stream(dev)
+        mark("red0")
+        for j, c in enumerate(sorted(set(cls), reverse=True)):
+            rows = [r for r in range(len(on_dev)) if cls[r] == c]
+            sub_h = np.ascontiguousarray(tab[rows])
+            sub = torch.from_numpy(sub_h.view(np.uint8)).to(dev)
+            st = main if j == 0 else _concurrent().stream(dev, 80 + j)
+            if st is not main:
+                st.wait_stream(main)
+            with torch.cuda.stream(st):
+                _lib.check(lib.tnk_gebrd_batched_f64(
+                    sub.data_ptr(), len(rows), int(sub_h["m"].max()), int(sub_h["n"].max()), c,
+                    base, RF.data_ptr(), RF.data_ptr(), vec.data_ptr(), _lib.stream_ptr()),
+                    "tnk_gebrd_batched_f64")
+                sub.record_stream(st)
+            if st is not main:
+                main.wait_stream(st)
+        mark("red1")
+        t_host = time.perf_counter()
+        vh = vec.cpu().numpy()
+    for i in off_dev:
+        M = sec[i][2]
+        U, S, Vh = torch.linalg.svd(M, full_matrices=False)
+        facs[i] = (U, S, Vh, S.cpu().numpy().astype(np.float64))
+    if on_dev:
+        res = hostlapack.bidiag_svd_many(
+            [(vh[int(tab[r]["v_off"]):int(tab[r]["v_off"]) + int(tab[r]["n"])],
+              vh[int(tab[r]["v_off"]) + int(tab[r]["n"]):int(tab[r]["v_off"]) + 2 * int(tab[r]["n"])])
+             for r in range(len(on_dev))], lanes=_STEDC_LANES)
+    sig = {}
+    for r, i in enumerate(on_dev):
+        sig[i] = np.maximum(res[r][0], 0.0)
+    for i in off_dev:
+        sig[i] = facs[i][3]
+    kept = {}
+    for it, (mt, blocks, chi, scale, normalize) in enumerate(items):
+        ids = [i for i, s in enumerate(sec) if s[0] == it]
+        s_host = np.concatenate([sig[i] for i in ids])
+        owner = np.concatenate([np.full(len(sig[i]), j) for j, i in enumerate(ids)])
+        order = np.lexsort((np.arange(s_host.size), -s_host))
+        kk = min(int(chi), s_host.size)
+        cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
+        for j, i in enumerate(ids):
+            kept[i] = int(cnt[j])
+    # kept vectors of B: left (m rows, zero below n), right (n rows); two reflector sets each
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    chunk = 8 if sum((kept[i] + 7) // 8 for i in on_dev) * 2 >= 2 * n_sm else 2
+    sets, items_q, zoff = [], [], {}
+    z = 0
+    for r, i in enumerate(on_dev):
+        q = kept[i]
+        if not q:
+            continue
+        mm, nn = int(tab[r]["m"]), int(tab[r]["n"])
+        vo_r = int(tab[r]["v_off"])
+        zl, zr = z, z + mm * q
+        zoff[i] = (zl, zr)
+        z += (mm + nn) * q
+        sets.append((mm, nn, int(tab[r]["ul_off"]), vo_r + 2 * nn, zl, 0, 0))
+        sets.append((nn, max(nn - 2, 0), int(tab[r]["vr_off"]), vo_r + 3 * nn, zr, 1, 0))
+        for sidx in (len(sets) - 2, len(sets) - 1):
+            for c0 in range(0, q, chunk):
+                items_q.append((sidx, c0, min(chunk, q - c0), 0))
+    if z:
+        ns = sum(kept[i] for i in on_dev)
+        pin = _pinned(z + ns)
+        hz = pin.numpy()
+        hz[:z] = 0.0
+        so = z
+        for r, i in enumerate(on_dev):
+            q = kept[i]
+            if not q:
+                continue
+            mm, nn = int(tab[r]["m"]), int(tab[r]["n"])
+            s_, Ub, VTb = res[r]
+            zl, zr = zoff[i]
+            hz[zl:zl + mm * q].reshape(q, mm)[:, :nn] = Ub[:, :q].T
+            hz[zr:zr + nn * q].reshape(q, nn)[:] = VTb[:q, :]
+            hz[so:so + q] = sig[i][:q]
+            so += q
+        up = torch.empty(z + ns, dtype=torch.float64, device=dev)
+        up.copy_(pin[:z + ns], non_blocking=True)
+        _PIN["done"] = torch.cuda.Event()
+        _PIN["done"].record()
+        if timing is not None:
+            timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
+        Zd, S_all = up[:z], up[z:]
+        st_h = np.asarray(sets, dtype=np.int64)
+        st_arr = np.zeros(len(sets), dtype=REFL_SET)
+        for f, name in enumerate(("rows", "nrefl", "r_off", "tau_off", "z_off", "shift", "pad")):
+            st_arr[name] = st_h[:, f]
+        st_d = torch.from_numpy(st_arr.view(np.uint8)).to(dev)
+        it_d = torch.from_numpy(np.asarray(items_q, dtype=np.int32)).to(dev)
+        keep += [st_d, it_d]
+        mark("back0")
+        _lib.check(lib.tnk_ormqr_batched_f64(st_d.data_ptr(), it_d.data_ptr(), len(items_q),
+                                             int(st_arr["rows"].max()), RF.data_ptr(),
+                                             vec.data_ptr(), Zd.data_ptr(), sp),
+                   "tnk_ormqr_batched_f64")
+        mark("back1")
+    elif on_dev and timing is not None:
+        timing["host_ms"] = timing.get("host_ms", 0.0) + (time.perf_counter() - t_host) * 1e3
+    so = 0
+    for r, i in enumerate(on_dev):
+        _, _, M, tr, mm, nn = sec[i]
+        q = kept[i]
+        R, Cc = M.shape
+        if not q:
+            facs[i] = (M.new_zeros((R, 0)), M.new_zeros(0), M.new_zeros((0, Cc)), sig[i])
+            continue
+        zl, zr = zoff[i]
+        Lq = Zd[zl:zl + mm * q].view(q, mm)        # row j: left singular vector j of A
+        Rq = Zd[zr:zr + nn * q].view(q, nn)        # row j: right singular vector j of A
+        S = S_all[so:so + q]
+        so += q
+        if not tr:          # A = M: U = Q_L U_B, V = Q_R V_B
+            facs[i] = (Lq.mT, S, Rq, sig[i])
+        else:               # A = M^T = U_A S V_A^T: M = V_A S U_A^T
+            facs[i] = (Rq.mT, S, Lq, sig[i])
+    out = []
+    for it, (mt, blocks, chi, scale, normalize) in enumerate(items):
+        ids = [i for i, s in enumerate(sec) if s[0] == it]
+        out.append(_trunc_finish(mt, blocks, [facs[i] for i in ids], chi, scale, normalize))
+    if timing is not None:
+        mark("end")
+        torch.cuda.synchronize(dev)
+        span = lambda a, b: ev[a].elapsed_time(ev[b]) if a in ev and b in ev else 0.0
+        for k, (a, b) in {"reduce_ms": ("red0", "red1"), "back_ms": ("back0", "back1"),
+                          "total_ms": ("red0", "end")}.items():
+            timing[k] = timing.get(k, 0.0) + span(a, b)
+        timing["sectors"] = len(sec)
+        timing["sectors_on_device"] = len(on_dev)
+    return out
+
+
 def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
                   method: str = "svd", normalize: bool = True, host: str = "auto",
                   dtype=torch.float64, gram_qr: bool = False):
@@ -741,20 +977,29 @@ def truncated_svd(m: BlockTensor, chi: int, scale: str = "none", driver=None,
     sweep driver does not use it.
     host='device': the device Gram route (_gram_device_many: the sectors' reductions to
     tridiagonal form and the back-transformation of the kept vectors on the GPU, only the
-    tridiagonal eigenproblems on the host); FP64 CUDA blocks, scale as above.
+    tridiagonal eigenproblems on the host); FP64 CUDA blocks, scale as above. With
+    method='svd', host 'auto' / 'device' takes the device exact route on FP64 CUDA blocks
+    (_svd_device_many: bidiagonalisation and back-transformations on the GPU, the bidiagonal
+    SVDs on the host), 'never' keeps torch.linalg.svd per sector.
     Returns U, S (device vector, normalised when scale != 'none'), Vh, disc (absolute)."""
     if host not in ("auto", "never", "always", "device"):
         raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if chi < 1:
         raise ValueError(f"chi must be at least 1, got {chi}")
-    if host == "auto" and method == "gram" and not gram_qr and dtype == torch.float64 and \
-            scale in ("right", "left") and m.data.is_cuda and m.data.dtype == torch.float64 \
-            and device_gram_available():
+    real_cuda = m.data.is_cuda and m.data.dtype == torch.float64 and dtype == torch.float64
+    if method == "svd" and host in ("auto", "device") and real_cuda and \
+            (host == "device" or device_svd_available()):
+        blocks = list(_blocks(m))
+        if not blocks:
+            raise ValueError("the matrix has no allowed blocks")
+        return _svd_device_many([(m, blocks, chi, scale, normalize)])[0]
+    if host == "auto" and method == "gram" and not gram_qr and real_cuda and \
+            scale in ("right", "left") and device_gram_available():
         host = "device"
     if host == "device":
-        if method != "gram" or gram_qr or dtype != torch.float64 or not m.data.is_cuda or \
-                m.data.dtype != torch.float64:
-            raise ValueError("host='device' is the FP64 Gram route of a CUDA block matrix")
+        if method != "gram" or gram_qr or not real_cuda:
+            raise ValueError("host='device' is the FP64 Gram or exact route of a CUDA block "
+                             "matrix")
         blocks = list(_blocks(m))
         if not blocks:
             raise ValueError("the matrix has no allowed blocks")
@@ -834,6 +1079,18 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
         raise ValueError("host must be 'auto', 'never', 'always' or 'device'")
     if method not in ("svd", "gram"):
         raise ValueError(f"unknown method {method!r}; expected 'svd' or 'gram'")
+    if method == "svd" and host in ("auto", "device") and \
+            all(m.data.is_cuda and m.data.dtype == torch.float64 for m, _, _ in items) and \
+            (host == "device" or device_svd_available()):
+        dv = []
+        for m, chi, scale in items:
+            if chi < 1:
+                raise ValueError(f"chi must be at least 1, got {chi}")
+            blocks = list(_blocks(m))
+            if not blocks:
+                raise ValueError("the matrix has no allowed blocks")
+            dv.append((m, blocks, chi, scale, normalize))
+        return _svd_device_many(dv)
     if host == "auto" and method == "gram" and all(sc in ("right", "left") for _, _, sc in items) \
             and all(m.data.is_cuda and m.data.dtype == torch.float64 for m, _, _ in items) \
             and device_gram_available():
