@@ -61,3 +61,43 @@ def test_cluster_choice():
         assert LA._sytrd_clusters([700], 152) == [0]
     finally:
         LA._SYTRD["limits"] = saved
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 50, 300])
+def test_bidiag_svd(n):
+    """dbdsdc through the Cython export: singular values against numpy (descending), orthonormal
+    vectors, B = U diag(s) VT."""
+    rng = np.random.default_rng(n)
+    d = rng.standard_normal(n) * 10.0 ** -np.linspace(0, 8, n)
+    e = rng.standard_normal(max(n - 1, 0)) * 10.0 ** -np.linspace(0, 8, max(n - 1, 0))
+    B = np.diag(d) + (np.diag(e, 1) if n > 1 else 0)
+    s, U, VT = hostlapack.bidiag_svd(d, e)
+    ref = np.linalg.svd(B, compute_uv=False)
+    assert np.all(np.diff(s) <= 0) and np.all(s >= 0)
+    assert np.abs(s - ref).max() <= 1e-14 * max(ref[0], 1e-300)
+    assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-13
+    assert np.abs(VT @ VT.T - np.eye(n)).max() <= 1e-13
+    assert np.abs((U * s) @ VT - B).max() <= 1e-14 * max(ref[0], 1e-300)
+
+
+def test_bidiag_svd_many_equals_one_by_one():
+    rng = np.random.default_rng(3)
+    probs = [(rng.standard_normal(n), rng.standard_normal(max(n - 1, 0))) for n in (7, 90, 1, 33)]
+    many = hostlapack.bidiag_svd_many(probs, lanes=3)
+    for (d, e), (s, U, VT) in zip(probs, many):
+        s1, U1, VT1 = hostlapack.bidiag_svd(d, e)
+        assert np.array_equal(s, s1) and np.array_equal(U, U1) and np.array_equal(VT, VT1)
+
+
+def test_exact_route_cluster_choice():
+    from tnkit_gb300 import linalg as LA
+    saved = LA._GEBRD["limits"]
+    LA._GEBRD["limits"] = {1: 160, 2: 228, 4: 322, 8: 450, 16: 630}
+    try:
+        shapes = [(522, 519), (344, 344), (142, 142), (31, 31), (2, 2)]
+        cs = LA._gebrd_clusters(shapes, 152)
+        assert all(LA._GEBRD["limits"][c] >= m for (m, _), c in zip(shapes, cs))
+        assert cs[0] == 16 and sum(cs) <= 152
+        assert LA._gebrd_clusters([(700, 10)], 152) == [0]
+    finally:
+        LA._GEBRD["limits"] = saved
