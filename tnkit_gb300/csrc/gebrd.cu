@@ -262,8 +262,13 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         }
         cl.sync();                                   // (3) every part of y is written
         for (int i = k + 1 + r + cs * tid; i < m; i += cs * GB_THREADS) {
+            // the peers' parts, all loads in flight at once, then summed in rank order
+            double part[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) part[q] = q < cs ? cl.map_shared_rank(S.yp, q)[i] : 0.0;
             double acc = 0.0;
-            for (int q = 0; q < cs; ++q) acc += cl.map_shared_rank(S.yp, q)[i];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc += part[q];
             S.yr[i] = acc;
         }
         cl.sync();                                   // (4) y is summed, by residue class
