@@ -181,10 +181,15 @@ def main():
                          "at N=1)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the whole chi=1024 DMRG leg (FP64 against mixed-ff, ~2 minutes)")
+    ap.add_argument("--no-sweep-exact", action="store_true",
+                    help="skip the second sweep record (the exact truncation, FP64 and mixed)")
     ap.add_argument("--no-trunc", action="store_true",
                     help="skip the truncation leg (the chi=1024 mid-bond cut on each route)")
     ap.add_argument("--trunc-only", action="store_true",
                     help="run only the truncation leg and print its record")
+    ap.add_argument("--trunc-routes", default="gram,svd",
+                    help="routes of the truncation leg: 'gram' (device, cuSOLVER, host LAPACK), "
+                         "'svd' (exact: device, torch), 'gram-device', 'svd-device'")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-chain batched local problems (sequential, batched, "
                          "graph-captured; a few seconds, run by default at N=1)")
@@ -244,7 +249,8 @@ def main():
     if args.trunc_only:
         if rank == 0:
             print(json.dumps({"truncation": trunc_leg(torch, dev, measure_dgemm_peak(torch, dev),
-                                                      max(args.steps // 2, 5))}), flush=True)
+                                                      max(args.steps // 2, 5),
+                                                      args.trunc_routes)}), flush=True)
         return
     th, L, W1, W2, R = workloads.mid_bond_problem(seed=3 + rank, device=dev)
     # the schedule (FP64 inner product, stage-3 split-K, tile order) picked by the autotuner on
@@ -463,9 +469,15 @@ def main():
     line["gpu_launches_per_step"] = {"fp64": per_step, "e2e": per_step, "mixed": 4,
                                      "float_float": per_step + 1}
     if world == 1 and not args.no_trunc:
-        line["truncation"] = trunc_leg(torch, dev, dgemm, max(args.steps // 2, 5))
+        line["truncation"] = trunc_leg(torch, dev, dgemm, max(args.steps // 2, 5),
+                                       args.trunc_routes)
     if args.sweep or (world == 1 and not args.no_sweep):
         line["sweep"] = sweep_leg(torch, args)
+        if not args.no_sweep_exact and args.svd_method == "gram" and args.sweep_model == "xxz":
+            # the same DMRG with the reference's default exact truncation, FP64 and mixed
+            ex = argparse.Namespace(**vars(args))
+            ex.svd_method, ex.sweep_precisions = "svd", "f64,mixed"
+            line["sweep_exact"] = sweep_leg(torch, ex)
     if world == 1 and not args.no_batch:
         line["batch"] = batch_leg(torch, dev, flush, max(args.steps, 5))
     if args.batch_dmrg:
@@ -510,7 +522,7 @@ def trunc_block(torch, dev, seed=0):
     return BlockTensor(lay, torch.as_tensor(data, device=dev))
 
 
-def trunc_leg(torch, dev, dgemm, reps):
+def trunc_leg(torch, dev, dgemm, reps, routes_arg="gram,svd"):
     """The truncation of the chi=1024 mid bond (keep 1024 of 2048 values, scale 'right', as the
     left-to-right sweep cuts) on each Gram route: 'device' (the sectors' reductions and the
     back-transformation of the kept vectors on the GPU, tridiagonal problems on host threads),
@@ -526,7 +538,12 @@ def trunc_leg(torch, dev, dgemm, reps):
                        "(synthetic), scale 'right'",
            "sectors": [list(m.layout.shape(j)) for j in range(m.layout.nblocks)]}
     res = {}
-    routes = ["device", "never", "always"] if LA.device_gram_available() else ["never", "always"]
+    want = set(routes_arg.split(","))
+    routes = []
+    if want & {"gram", "gram-device"} and LA.device_gram_available():
+        routes.append("device")
+    if "gram" in want:
+        routes += ["never", "always"]
     for host in routes:
         for _ in range(2):
             r = LA.truncated_svd(m, 1024, scale="right", method="gram", host=host)
@@ -539,16 +556,17 @@ def trunc_leg(torch, dev, dgemm, reps):
             ts.append(time.perf_counter() - t0)
         res[host] = r
         out[host] = {"ms_median": float(np.median(ts)) * 1e3, "ms_min": float(min(ts)) * 1e3}
-    S0 = torch.sort(res["never"][1], descending=True).values
-    for host in routes:
-        S = torch.sort(res[host][1], descending=True).values
-        out[host]["max_abs_dsigma2_vs_never"] = float((S ** 2 - S0 ** 2).abs().max())
-        out[host]["discarded"] = res[host][3]
+    if "never" in res:
+        S0 = torch.sort(res["never"][1], descending=True).values
+        for host in routes:
+            S = torch.sort(res[host][1], descending=True).values
+            out[host]["max_abs_dsigma2_vs_never"] = float((S ** 2 - S0 ** 2).abs().max())
+            out[host]["discarded"] = res[host][3]
     # the exact route (method='svd', the reference's default): device bidiagonalisation against
     # torch.linalg.svd per sector
-    if LA.device_svd_available():
+    if want & {"svd", "svd-device"} and LA.device_svd_available():
         ex = {}
-        for host in ("device", "never"):
+        for host in (("device", "never") if "svd" in want else ("device",)):
             for _ in range(2):
                 r = LA.truncated_svd(m, 1024, scale="right", method="svd", host=host)
             torch.cuda.synchronize()
@@ -561,9 +579,10 @@ def trunc_leg(torch, dev, dgemm, reps):
             ex[host] = r
             out[f"svd_{host}"] = {"ms_median": float(np.median(ts)) * 1e3,
                                   "ms_min": float(min(ts)) * 1e3, "discarded": r[3]}
-        Sa = torch.sort(ex["device"][1], descending=True).values
-        Sb = torch.sort(ex["never"][1], descending=True).values
-        out["svd_device"]["max_abs_dsigma_vs_torch"] = float((Sa - Sb).abs().max())
+        if "never" in ex:
+            Sa = torch.sort(ex["device"][1], descending=True).values
+            Sb = torch.sort(ex["never"][1], descending=True).values
+            out["svd_device"]["max_abs_dsigma_vs_torch"] = float((Sa - Sb).abs().max())
         tm = {}
         for _ in range(reps):
             blocks = list(LA._blocks(m))

@@ -16,12 +16,13 @@
 //   right: row k's entries right of the diagonal are spread over the CTAs: each publishes the
 //          sum of squares of its own entries (the owner of column k+1 also its alpha), every
 //          CTA forms the reflector G_k = I - tau_v v v^T (columns k+1 .. n-1, e_k = beta) from
-//          the same numbers in the same order, keeps v for its own columns, computes its part
-//          of y = A[k+1:, k+1:] v, the cluster sums y (each CTA one residue class of rows, then
-//          every CTA gathers the whole y), and every CTA applies A -= tau_v y v^T to its columns;
+//          the same numbers in the same order and keeps v for its own columns; y = A[k+1:, k+1:] v
+//          is summed over the cluster from unscaled parts published with the row norms (each CTA
+//          one residue class of rows, then every CTA gathers the whole y), and every CTA
+//          applies A -= tau_v y v^T to its columns;
 //   the owner of column k + 1 applies both to that column first and forms H_{k+1} with one
 //          warp while its other warps update (look-ahead).
-// Four cluster barriers per step; no flag waits (every CTA of a cluster reaches every barrier
+// Three cluster barriers per step; no flag waits (every CTA of a cluster reaches every barrier
 // the same number of times: the loop counts depend only on the sector's shape). Outputs: d, e,
 // tau_u, tau_v per sector; reflector k's u (u[k] = 1 stored) in column k, rows k .. m-1, of the
 // sector's m x n left-reflector matrix, v (v[k+1] = 1) in column k, rows k+1 .. n-1, of its
@@ -53,7 +54,7 @@ __host__ __device__ inline int64_t gb_ld(int64_t m) { return m | 1; }
 
 __host__ __device__ inline int64_t gb_shared_doubles(int64_t m, int64_t n, int cs) {
     const int64_t ncm = (n + cs - 1) / cs;
-    return ncm * gb_ld(m) + 5 * m + 2 * ncm + GB_THREADS + 6;
+    return ncm * gb_ld(m) + 7 * m + 2 * ncm + GB_THREADS + 6;
 }
 
 struct GbShared {
@@ -63,6 +64,8 @@ struct GbShared {
     double* yp;     // m: this CTA's part of y (read by the peers)
     double* yr;     // m: y summed over the cluster on this CTA's rows (read by the peers)
     double* yf;     // m: the whole y
+    double* yc;     // m: column k + 1 when this CTA owns it (read by the peers)
+    double* ycl;    // m: the owner's column k + 1 on this CTA's rows
     double* sown;   // ncm: the own columns' left dot products
     double* vown;   // ncm: the own entries of the right reflector
     double* part;   // GB_THREADS: partial column dot products
@@ -78,7 +81,9 @@ __device__ GbShared gb_layout(double* sh, int m, int ncm) {
     s.yp = s.ul + m;
     s.yr = s.yp + m;
     s.yf = s.yr + m;
-    s.sown = s.yf + m;
+    s.yc = s.yf + m;
+    s.ycl = s.yc + m;
+    s.sown = s.ycl + m;
     s.vown = s.sown + ncm;
     s.part = s.vown + ncm;
     s.scal = s.part + GB_THREADS;
@@ -207,7 +212,11 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             }
             continue;                                // next step: barrier (1), left only
         }
-        // right: own sum of squares of row k over columns > k + 1, and alpha = A[k][k+1]
+        // right: G_k's vector is v = sc x + e_{k+1} with x the row k entries right of column
+        // k + 1 and sc known only once the row's norm is, so y = A v is gathered unscaled: each
+        // CTA's x part yp (own columns j > k + 1) and, from the owner of column k + 1, that
+        // column yc; y = sc sum(yp) + yc. Here: own sum of squares of x, alpha = A[k][k+1], yp,
+        // and yc (owner of k + 1).
         if (warp == 0) {
             double ss = 0.0;
             for (int jl = jl0 + lane; jl < ncl; jl += 32) {
@@ -221,7 +230,18 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                 if ((k + 1) % cs == r) S.scal[2] = S.A[(size_t)((k + 1) / cs) * ld + k];
             }
         }
-        cl.sync();                                   // (2) the row's shares are published
+        {
+            const bool own1 = (k + 1) % cs == r;
+            const int j1 = own1 ? (k + 1) / cs : -1;
+            for (int i = k + 1 + tid; i < m; i += GB_THREADS) {
+                double acc = 0.0;
+                for (int jl = jl0; jl < ncl; ++jl)
+                    if (jl != j1) acc = fma(S.A[(size_t)jl * ld + i], S.A[(size_t)jl * ld + k], acc);
+                S.yp[i] = acc;
+                if (own1) S.yc[i] = S.A[(size_t)j1 * ld + i];
+            }
+        }
+        cl.sync();                                   // (2) row norms and y parts are published
         if (warp == 0) {
             // every CTA forms the same reflector from the same numbers in the same order
             double ss = lane < cs ? *cl.map_shared_rank(S.scal + 1, lane) : 0.0;
@@ -242,36 +262,31 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                 S.scal[4] = sc;
             }
         }
-        __syncthreads();
-        const double tv = S.scal[3];
-        {
-            const double sc = S.scal[4];
-            for (int jl = jl0 + tid; jl < ncl; jl += GB_THREADS) {
-                const int j = r + cs * jl;
-                const double v = (j == k + 1) ? 1.0 : S.A[(size_t)jl * ld + k] * sc;
-                S.vown[jl] = v;
-                VRs[(size_t)k * n + j] = v;
-            }
-        }
-        __syncthreads();
-        // this CTA's part of y = A[k+1:, k+1:] v (one row per thread over the own columns)
-        for (int i = k + 1 + tid; i < m; i += GB_THREADS) {
-            double acc = 0.0;
-            for (int jl = jl0; jl < ncl; ++jl) acc = fma(S.A[(size_t)jl * ld + i], S.vown[jl], acc);
-            S.yp[i] = acc;
-        }
-        cl.sync();                                   // (3) every part of y is written
+        // meanwhile the unscaled sums of this CTA's residue class of rows (all peers' loads in
+        // flight at once, summed in rank order) and the owner's column k + 1 there
         for (int i = k + 1 + r + cs * tid; i < m; i += cs * GB_THREADS) {
-            // the peers' parts, all loads in flight at once, then summed in rank order
             double part[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) part[q] = q < cs ? cl.map_shared_rank(S.yp, q)[i] : 0.0;
+            const double c1 = cl.map_shared_rank(S.yc, (k + 1) % cs)[i];
             double acc = 0.0;
 #pragma unroll
             for (int q = 0; q < 16; ++q) acc += part[q];
             S.yr[i] = acc;
+            S.ycl[i] = c1;
         }
-        cl.sync();                                   // (4) y is summed, by residue class
+        __syncthreads();
+        const double tv = S.scal[3];
+        const double sc = S.scal[4];
+        for (int i = k + 1 + r + cs * tid; i < m; i += cs * GB_THREADS)
+            S.yr[i] = fma(sc, S.yr[i], S.ycl[i]);
+        for (int jl = jl0 + tid; jl < ncl; jl += GB_THREADS) {
+            const int j = r + cs * jl;
+            const double v = (j == k + 1) ? 1.0 : S.A[(size_t)jl * ld + k] * sc;
+            S.vown[jl] = v;
+            VRs[(size_t)k * n + j] = v;
+        }
+        cl.sync();                                   // (3) y is summed, by residue class
         for (int i = k + 1 + tid; i < m; i += GB_THREADS)
             S.yf[i] = cl.map_shared_rank(S.yr, (i - k - 1) % cs)[i];
         __syncthreads();
