@@ -54,7 +54,7 @@ __host__ __device__ inline int64_t gb_ld(int64_t m) { return m | 1; }
 
 __host__ __device__ inline int64_t gb_shared_doubles(int64_t m, int64_t n, int cs) {
     const int64_t ncm = (n + cs - 1) / cs;
-    return ncm * gb_ld(m) + 7 * m + 2 * ncm + GB_THREADS + 6;
+    return ncm * gb_ld(m) + 7 * m + 3 * ncm + GB_THREADS + 6;
 }
 
 struct GbShared {
@@ -68,6 +68,7 @@ struct GbShared {
     double* ycl;    // m: the owner's column k + 1 on this CTA's rows
     double* sown;   // ncm: the own columns' left dot products
     double* vown;   // ncm: the own entries of the right reflector
+    double* xk;     // ncm: row k of the own columns, zero in column k + 1
     double* part;   // GB_THREADS: partial column dot products
     double* scal;   // 6: tau_u of ub, own sum of squares of row k, alpha of row k, tau_v, the
                     // right reflector's scale, spare
@@ -85,7 +86,8 @@ __device__ GbShared gb_layout(double* sh, int m, int ncm) {
     s.ycl = s.yc + m;
     s.sown = s.ycl + m;
     s.vown = s.sown + ncm;
-    s.part = s.vown + ncm;
+    s.xk = s.vown + ncm;
+    s.part = s.xk + ncm;
     s.scal = s.part + GB_THREADS;
     return s;
 }
@@ -217,29 +219,28 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         // CTA's x part yp (own columns j > k + 1) and, from the owner of column k + 1, that
         // column yc; y = sc sum(yp) + yc. Here: own sum of squares of x, alpha = A[k][k+1], yp,
         // and yc (owner of k + 1).
+        const bool own1 = (k + 1) % cs == r;
+        const int j1 = own1 ? (k + 1) / cs : -1;
         if (warp == 0) {
             double ss = 0.0;
             for (int jl = jl0 + lane; jl < ncl; jl += 32) {
-                const int j = r + cs * jl;
                 const double a = S.A[(size_t)jl * ld + k];
-                if (j > k + 1) ss = fma(a, a, ss);
+                const double x = jl == j1 ? 0.0 : a;         // x: row k without column k + 1
+                S.xk[jl] = x;
+                ss = fma(x, x, ss);
             }
             ss = warp_sum_d(ss);
             if (lane == 0) {
                 S.scal[1] = ss;
-                if ((k + 1) % cs == r) S.scal[2] = S.A[(size_t)((k + 1) / cs) * ld + k];
+                if (own1) S.scal[2] = S.A[(size_t)j1 * ld + k];
             }
         }
-        {
-            const bool own1 = (k + 1) % cs == r;
-            const int j1 = own1 ? (k + 1) / cs : -1;
-            for (int i = k + 1 + tid; i < m; i += GB_THREADS) {
-                double acc = 0.0;
-                for (int jl = jl0; jl < ncl; ++jl)
-                    if (jl != j1) acc = fma(S.A[(size_t)jl * ld + i], S.A[(size_t)jl * ld + k], acc);
-                S.yp[i] = acc;
-                if (own1) S.yc[i] = S.A[(size_t)j1 * ld + i];
-            }
+        __syncthreads();
+        for (int i = k + 1 + tid; i < m; i += GB_THREADS) {
+            double acc = 0.0;
+            for (int jl = jl0; jl < ncl; ++jl) acc = fma(S.A[(size_t)jl * ld + i], S.xk[jl], acc);
+            S.yp[i] = acc;
+            if (own1) S.yc[i] = S.A[(size_t)j1 * ld + i];
         }
         cl.sync();                                   // (2) row norms and y parts are published
         if (warp == 0) {
@@ -250,9 +251,19 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             if (lane == 0) {
                 double beta = alpha, tv = 0.0, sc = 0.0;
                 if (ss > 0.0) {
+                    // one division: q = 1 / (beta (alpha - beta)) gives 1/beta = (alpha - beta) q
+                    // and 1/(alpha - beta) = beta q
                     beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
-                    tv = (beta - alpha) / beta;
-                    sc = 1.0 / (alpha - beta);
+                    const double am = alpha - beta;
+                    const double ba = beta * am;
+                    if (fabs(ba) > 1e-290) {
+                        const double q = 1.0 / ba;
+                        tv = -am * am * q;
+                        sc = beta * q;
+                    } else {                                 // (entries below ~1e-145)
+                        tv = (beta - alpha) / beta;
+                        sc = 1.0 / am;
+                    }
                 }
                 if (r == 0) {
                     e[k] = beta;
