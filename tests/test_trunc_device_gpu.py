@@ -311,3 +311,57 @@ def test_exact_device_route_mid_bond():
     assert U.layout.legs == U0.layout.legs
     assert float((S - S0).abs().max()) <= 1e-14 * float(S0.max()) * 10
     assert abs(disc - disc0) <= 1e-12
+
+
+@pytest.mark.parametrize("method", ["gram", "svd"])
+def test_sectors_above_the_cluster_limit_take_the_library_route(method, monkeypatch):
+    """With the cluster kernels' order limit lowered below the largest sector, that sector goes
+    through the per-sector library route (cuSOLVER Gram / torch SVD) and the rest through the
+    device kernels, in one cut: the same values and bond as the all-library route."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(17)
+    a = Leg((-1, 1, 3), (20, 90, 40), 1)
+    b = Leg((-1, 1, 3), (25, 80, 45), -1)
+    lay = layout_of((a, b), 0)
+    h = rng.standard_normal(lay.size)
+    h /= np.linalg.norm(h)
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    if method == "gram":
+        lim = dict(LA._sytrd_table())
+        monkeypatch.setitem(LA._SYTRD, "limits", {c: (min(v, 60) if v else 0) for c, v in lim.items()})
+    else:
+        lim = dict(LA._gebrd_table())
+        monkeypatch.setitem(LA._GEBRD, "limits", {c: (min(v, 60) if v else 0) for c, v in lim.items()})
+    U, S, V, d = LA.truncated_svd(m, 100, scale="right", method=method, host="device")
+    U0, S0, V0, d0 = LA.truncated_svd(m, 100, scale="right", method=method, host="never")
+    assert U.layout.legs == U0.layout.legs
+    assert float((S - S0).abs().max()) <= 1e-12 * float(S0.max())
+    dn = lambda t: to_dense_np(t.layout, t.data.cpu().numpy())
+    assert np.abs(dn(U) @ dn(V) - dn(U0) @ dn(V0)).max() <= 1e-11
+
+
+def test_rank_deficient_and_zero_sectors():
+    """Exact zeros: a zero sector and a rank-1 sector on both device routes -- finite factors,
+    the zero singular values, an orthonormal kept side."""
+    from tnkit_gb300 import linalg as LA
+    from tnkit_gb300.layout import Leg, layout_of, to_dense_np
+    from tnkit_gb300.tensor import BlockTensor
+    rng = np.random.default_rng(23)
+    a = Leg((-1, 1, 3), (6, 30, 12), 1)
+    b = Leg((-1, 1, 3), (5, 28, 14), -1)
+    lay = layout_of((a, b), 0)
+    h = np.zeros(lay.size)
+    o = [int(x) for x in lay.offsets]
+    h[o[1]:o[1] + 30 * 28] = np.outer(rng.standard_normal(30), rng.standard_normal(28)).ravel()
+    h[o[2]:o[2] + 12 * 14] = rng.standard_normal(12 * 14) * 1e-3
+    h /= np.linalg.norm(h)
+    m = BlockTensor(lay, torch.as_tensor(h, device="cuda"), h)
+    for method in ("gram", "svd"):
+        U, S, V, d = LA.truncated_svd(m, 12, scale="right", method=method, host="device")
+        U0, S0, V0, d0 = LA.truncated_svd(m, 12, scale="right", method=method, host="never")
+        assert torch.isfinite(U.data).all() and torch.isfinite(V.data).all()
+        assert torch.allclose(torch.sort(S).values, torch.sort(S0).values, rtol=0, atol=1e-10)
+        Ud = to_dense_np(U.layout, U.data.cpu().numpy())
+        assert np.abs(Ud.T @ Ud - np.eye(Ud.shape[1])).max() <= 1e-12
