@@ -75,36 +75,52 @@ __global__ void __launch_bounds__(NT)
 comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __restrict__ terms,
                 const tnk_comb_item* __restrict__ items, const float* __restrict__ src,
                 float* __restrict__ dst, int64_t lo_off, int split) {
+    constexpr int EPT = 4;                      // elements per thread per pass (loads in flight)
     __shared__ tnk_comb_term st[TERMS_SMEM];
     const tnk_comb_item item = items[blockIdx.x];
     const tnk_comb_task t = tasks[item.task];
     const int cols = t.cols;
     const int64_t nel = (int64_t)(item.row1 - item.row0) * cols;
     const int nterm = t.term_end - t.term_begin;
-    // accumulate in FP32 registers per element over all terms (chunks of TERMS_SMEM)
-    for (int64_t e0 = 0; e0 < nel; e0 += NT) {
-        const int64_t e = e0 + threadIdx.x;
-        const bool live = e < nel;
-        const int r = live ? item.row0 + (int)(e / cols) : 0;
-        const int c = live ? (int)(e % cols) : 0;
-        float acc = 0.f;
+    // accumulate in FP32 registers per element over all terms (chunks of TERMS_SMEM), the terms
+    // in order, so each element's sum is the same whatever the pass structure
+    for (int64_t e0 = 0; e0 < nel; e0 += EPT * NT) {
+        int r[EPT], c[EPT];
+        bool live[EPT];
+        float acc[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+            const int64_t e = e0 + u * NT + (int)threadIdx.x;
+            live[u] = e < nel;
+            const int rr = live[u] ? (int)(e / cols) : 0;
+            r[u] = item.row0 + rr;
+            c[u] = live[u] ? (int)(e - (int64_t)rr * cols) : 0;
+            acc[u] = 0.f;
+        }
         for (int t0 = 0; t0 < nterm; t0 += TERMS_SMEM) {
             const int nt = min(TERMS_SMEM, nterm - t0);
             __syncthreads();
-            if (threadIdx.x < nt) st[threadIdx.x] = terms[t.term_begin + t0 + threadIdx.x];
+            if ((int)threadIdx.x < nt) st[threadIdx.x] = terms[t.term_begin + t0 + threadIdx.x];
             __syncthreads();
-            if (live)
-                for (int q = 0; q < nt; ++q)
-                    acc = fmaf((float)st[q].coef,
-                               src[st[q].src_off + (int64_t)r * st[q].src_ld +
-                                   (int64_t)c * st[q].src_cs],
-                               acc);
+            for (int q = 0; q < nt; ++q) {
+                const tnk_comb_term tq = st[q];
+                float x[EPT];
+#pragma unroll
+                for (int u = 0; u < EPT; ++u)
+                    x[u] = live[u] ? src[tq.src_off + (int64_t)r[u] * tq.src_ld +
+                                         (int64_t)c[u] * tq.src_cs]
+                                   : 0.f;
+#pragma unroll
+                for (int u = 0; u < EPT; ++u) acc[u] = fmaf((float)tq.coef, x[u], acc[u]);
+            }
         }
-        if (live) {
-            const int64_t o = t.dst_off + (int64_t)r * t.dst_ld + (int64_t)c * t.dst_cs;
-            const float h = split ? tf32_hi(acc) : acc;
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+            if (!live[u]) continue;
+            const int64_t o = t.dst_off + (int64_t)r[u] * t.dst_ld + (int64_t)c[u] * t.dst_cs;
+            const float h = split ? tf32_hi(acc[u]) : acc[u];
             dst[o] = h;
-            if (split) dst[lo_off + o] = tf32_hi(acc - h);
+            if (split) dst[lo_off + o] = tf32_hi(acc[u] - h);
         }
     }
 }
