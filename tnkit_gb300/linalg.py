@@ -613,11 +613,7 @@ def _gram_device_many(items, timing=None):
     kept = {}
     for it, (m, blocks, chi, scale, normalize) in enumerate(items):
         ids = [i for i, s in enumerate(sec) if s[0] == it]
-        s_host = np.concatenate([sig[i] for i in ids])
-        owner = np.concatenate([np.full(len(sig[i]), j) for j, i in enumerate(ids)])
-        order = np.lexsort((np.arange(s_host.size), -s_host))
-        kk = min(int(chi), s_host.size)
-        cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
+        cnt = _cut([sig[i] for i in ids], chi)[0]
         for j, i in enumerate(ids):
             kept[i] = int(cnt[j])
     # back-transformation items: column chunks of up to 8 (one warp each); a bond whose kept
@@ -859,11 +855,7 @@ def _svd_device_many(items, timing=None):
     kept = {}
     for it, (mt, blocks, chi, scale, normalize) in enumerate(items):
         ids = [i for i, s in enumerate(sec) if s[0] == it]
-        s_host = np.concatenate([sig[i] for i in ids])
-        owner = np.concatenate([np.full(len(sig[i]), j) for j, i in enumerate(ids)])
-        order = np.lexsort((np.arange(s_host.size), -s_host))
-        kk = min(int(chi), s_host.size)
-        cnt = np.bincount(owner[order[:kk]], minlength=len(ids))
+        cnt = _cut([sig[i] for i in ids], chi)[0]
         for j, i in enumerate(ids):
             kept[i] = int(cnt[j])
     # kept vectors of B: left (m rows, zero below n), right (n rows); two reflector sets each
@@ -1154,6 +1146,19 @@ def truncated_svd_many(items, driver=None, method: str = "svd", normalize: bool 
             for m, chi, scale, blocks, b in per]
 
 
+def _cut(svals, chi: int):
+    """The global cut over the sectors' singular values (each sector's descending): the chi
+    largest in the stable order of (-sigma, position) (the reference's order,
+    tnkit/blocks.py:1427). Returns (kept count per sector, the order over the concatenated
+    values, the number kept)."""
+    s_host = np.concatenate(svals) if svals else np.zeros(0)
+    owner = np.concatenate([np.full(len(x), j) for j, x in enumerate(svals)]) if svals else \
+        np.zeros(0, dtype=np.int64)
+    order = np.lexsort((np.arange(s_host.size), -s_host))
+    k = min(int(chi), s_host.size)
+    return np.bincount(owner[order[:k]], minlength=len(svals)), order, k
+
+
 def _trunc_finish(m: BlockTensor, blocks, facs, chi: int, scale: str, normalize: bool):
     """The global cut over all sectors' singular values (descending, stable: the reference's
     order, tnkit/blocks.py:1427), the new bond leg, S normalised and folded into the kept
@@ -1169,10 +1174,8 @@ def _trunc_finish(m: BlockTensor, blocks, facs, chi: int, scale: str, normalize:
     else:
         s_host = torch.cat([p[3] for p in parts]).cpu().numpy().astype(np.float64)
         lens = [len(p[3]) for p in parts]
-    owner = np.concatenate([np.full(n, j) for j, n in enumerate(lens)])
-    order = np.lexsort((np.arange(s_host.size), -s_host))
-    k = min(int(chi), s_host.size)
-    kept = np.bincount(owner[order[:k]], minlength=len(parts))
+    kept, order, k = _cut([s_host[a:a + n] for a, n in zip(np.cumsum([0] + lens[:-1]), lens)],
+                          chi)
     disc = float(np.sum(s_host[order[k:]] ** 2))
     norm = float(np.sqrt(np.sum(s_host[order[:k]] ** 2))) or 1.0
     new = [(_row_label(lr, r), r, c, U[:, :n], S[:n], Vh[:n])
