@@ -618,21 +618,23 @@ def _peaks():
 
 
 def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps, ms64):
-    """The same matvec on the tensor cores (tcgen05, split TF32, FP32 accumulation), under both
-    GEMM schedules (tnk_tc_schedule: one CTA per tile, or persistent CTAs with two TMEM
-    accumulators for stages with more tiles than SMs); the faster one is the leg's result."""
+    """The same matvec on the tensor cores (tcgen05, split TF32, FP32 accumulation) in each
+    form: TF32 hi/lo parts staged (passes 3) under both GEMM schedules (tnk_tc_schedule: one CTA
+    per tile, or persistent CTAs with two TMEM accumulators for stages with more tiles than
+    SMs), and the parts formed in shared memory by the GEMM (passes 4, one CTA per tile); the
+    fastest form is the leg's result."""
     from tnkit_gb300 import _lib
     from tnkit_gb300.mixed import TwoSiteOperatorTC
     lib = _lib.lib()
-    op = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=3)
+    ops_tc = {p: TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=p) for p in (3, 4)}
     x = th.data
     y = torch.empty_like(x)
     stream = torch.cuda.current_stream()
-    c = op.c
     sp = _lib.stream_ptr()
     nrep = max(5, steps // 2)
 
-    def measure(sched):
+    def measure(op, sched):
+        c = op.c
         prev = lib.tnk_tc_schedule(sched)
         try:
             for _ in range(3):
@@ -655,14 +657,15 @@ def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps,
                 e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
                 e[0].record(stream)
                 _lib.check(lib.tnk_grouped_gemm_tc(c.t1, c.s1, c.tiles1, c.n_tiles1, c.maps,
-                                                   c.y32, c.err, 3, sp), "tc1")
+                                                   c.y32, c.err, op.passes, sp), "tc1")
                 e[1].record(stream)
                 _lib.check(lib.tnk_combine_f32(c.t2, c.c2, c.items2, c.n_items2, c.y32,
-                                               c.stage, c.lo_off, 1, sp), "comb32")
+                                               c.stage, c.lo_off, 1 if op.passes == 3 else 0,
+                                               sp), "comb32")
                 e[2].record(stream)
                 _lib.check(lib.tnk_grouped_gemm_tc_bn(c.t3, c.s3, c.tiles3, c.n_tiles3, c.maps,
-                                                      y.data_ptr(), c.err, 3, c.bn3 or 128, sp),
-                           "tc3")
+                                                      y.data_ptr(), c.err, op.passes,
+                                                      c.bn3 or 128, sp), "tc3")
                 e[3].record(stream)
                 torch.cuda.synchronize()
                 t1 += e[0].elapsed_time(e[1]) / 1e3
@@ -673,19 +676,22 @@ def mixed_leg(torch, dev, th, L, W1, W2, R, y64, flush, flops_ref, parts, steps,
             return t / steps, tg / nrep, t1 / nrep, err
         finally:
             lib.tnk_tc_schedule(prev)
-    runs = {name: measure(k) for name, k in (("one_tile_per_cta", 0), ("persistent", 1))}
+    forms = {"staged_one_tile_per_cta": (3, 0), "staged_persistent": (3, 1),
+             "smem_split_one_tile_per_cta": (4, 0)}
+    runs = {name: measure(ops_tc[p], k) for name, (p, k) in forms.items()}
     best = min(runs, key=lambda k: runs[k][1])
     t, tg, _, err = runs[best]
+    c = ops_tc[forms[best][0]].c
     bf16, src = _peaks()
     tf32_peak = bf16 / 2.0
     alg = 2 * (parts[0] + parts[3]) / tg / 1e12
     mms = t * 1e3
     return {"value": flops_ref / t / 1e9, "unit": "GFLOP/s", "ms_per_step": mms,
             "speedup_vs_fp64": ms64 / mms, "max_rel_err_vs_fp64": err, "dtype": "tf32x3/f32",
-            "schedule": best,
-            "schedules": {k: {"ms_per_step": v[0] * 1e3, "gemm_ms": v[1] * 1e3,
-                              "stage1_ms": v[2] * 1e3, "max_rel_err_vs_fp64": v[3]}
-                          for k, v in runs.items()},
+            "form": best,
+            "forms": {k: {"ms_per_step": v[0] * 1e3, "gemm_ms": v[1] * 1e3,
+                          "stage1_ms": v[2] * 1e3, "max_rel_err_vs_fp64": v[3]}
+                      for k, v in runs.items()},
             "tiles": {"stage1": int(c.n_tiles1), "stage3": int(c.n_tiles3),
                       "stage3_tile": f"128x{c.bn3 or 128}"},
             "roofline": {"bound": "tensor", "kernel": "gemm_tc_kernel (tcgen05 kind::tf32, "

@@ -211,7 +211,8 @@ int tnk_combine_f64(const tnk_comb_task* tasks, const tnk_comb_term* terms,
  * accumulation in TMEM), FP64 in and out. Replaces, for the bulk Lanczos iterations, the
  * low-precision matvec of tnkit/_dmrg.py:691-695 (eig='lanczos-mixed', there complex64 einsums).
  * passes = 3 splits every operand into TF32 hi/lo parts (~1e-6 relative error); passes = 1 is
- * plain TF32 (~1e-3).
+ * plain TF32 (~1e-3); passes = 4 is passes 3 with the operands staged once as FP32 and the hi/lo
+ * parts formed in shared memory inside the GEMM (half the operand traffic, the same results).
  * ---------------------------------------------------------------------------------------- */
 
 /* A tensor-core GEMM segment: operand tensor maps (hi parts at index 2*map, lo at 2*map+1). */

@@ -75,6 +75,28 @@ def test_tc_persistent_schedule_equals_one_tile_per_cta(passes):
         assert _rel(b, ref) <= 1e-4
 
 
+def test_tc_shared_memory_split_equals_staged_split():
+    """passes=4 (operands staged once as FP32, the TF32 hi/lo parts formed in shared memory by
+    the GEMM) gives the staged split's (passes=3) results bit for bit -- the chi=1024 mid bond
+    (128 x 128 and 128 x 64 tiles) and a 48-chain batched plan."""
+    from tnkit_gb300 import batch as B, workloads
+    from tnkit_gb300.mixed import TwoSiteOperatorTC
+    th, L, W1, W2, R = workloads.mid_bond_problem(seed=41)
+    a = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=3)(th.data)
+    op4 = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=4)
+    b = op4(th.data)
+    probs = B.batch_problems(48, seed=2)
+    p3 = B.BatchedTwoSiteOperator(probs, precision="tc")
+    xb = torch.randn(p3.n, dtype=torch.float64, device="cuda")
+    ab = p3(xb)
+    p4 = B.BatchedTwoSiteOperator(probs, precision="tc", tc_passes=4)
+    bb = p4(xb)
+    torch.cuda.synchronize()
+    op4.check_device_error()
+    p4.tc.check_device_error()
+    assert torch.equal(a, b) and torch.equal(ab, bb)
+
+
 def test_tc_matvec_golden_problem(golden):
     """The reference's own (converged-state) XXZ N=12 local problem."""
     from tnkit_gb300 import BlockTensor, Leg, layout_of

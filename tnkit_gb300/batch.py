@@ -30,6 +30,11 @@ from .tensor import BlockTensor
 from . import workloads
 
 
+
+# split-TF32 form of the tensor-core batches: 3 (hi/lo parts staged) or 4 (formed in shared
+# memory by the GEMM; the same results)
+TC_PASSES = 3
+
 class _Extent:
     """Stand-in output layout of a batched plan: only its size is read."""
 
@@ -99,7 +104,8 @@ class BatchedTwoSiteOperator:
     (the tensor-core split-TF32 operator of the same batched plan: operands staged once in FP32,
     one tcgen05 grouped-GEMM launch per GEMM stage for all problems; ~1e-6 relative)."""
 
-    def __init__(self, problems: Sequence[Problem], precision: str = "f64", tune: bool = False):
+    def __init__(self, problems: Sequence[Problem], precision: str = "f64", tune: bool = False,
+                 tc_passes: int = TC_PASSES):
         if precision not in ("f64", "ff", "tc"):
             raise ValueError("precision must be 'f64', 'ff' or 'tc'")
         if not problems:
@@ -137,7 +143,8 @@ class BatchedTwoSiteOperator:
         self.Lx, self.Rx = self.L, self.R
         if precision == "tc":
             from .mixed import TwoSiteOperatorTC
-            self.tc = TwoSiteOperatorTC.from_host_plan(hp, self.L, self.R, self.n)
+            self.tc = TwoSiteOperatorTC.from_host_plan(hp, self.L, self.R, self.n,
+                                                       passes=tc_passes)
         # the FP64 / float-float launches can drop converged problems' tiles (set_active); the
         # tensor-core operator computes every problem on every call
         self.supports_mask = precision != "tc"

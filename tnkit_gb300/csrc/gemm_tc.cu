@@ -11,7 +11,11 @@
 //
 // PASSES = 3 is the split-precision product A*B ~ Ah*Bh + Ah*Bl + Al*Bh of TF32 "hi" and "lo"
 // parts (each operand stored twice: hi = tf32(x), lo = tf32(x - hi)), accurate to ~1e-6
-// relative with FP32 accumulation; PASSES = 1 is plain TF32.
+// relative with FP32 accumulation; PASSES = 1 is plain TF32. PASSES = 4 is the same product as
+// PASSES = 3 with the operands staged once, as FP32: each ring slot's tiles arrive raw and six
+// splitter warps write the hi part in place and the lo part beside it before the MMAs read them
+// (half the bytes from L2 per K step, the stages being bound by that traffic; the same hi and
+// lo values, so the same results bit for bit).
 //
 // Every mbarrier wait is bounded; on a timeout the CTA records an error code in `err`, skips
 // the rest of its work, waits (bounded) for its own issued operations and frees its TMEM.
@@ -32,8 +36,15 @@ namespace {
 constexpr int BM = 128, BK = 32;
 constexpr int STAGES = 3;
 constexpr int NT = 128;
+constexpr int NT4 = 256;                    // PASSES = 4: two more roles of warps (splitters)
 constexpr int TILE_BYTES = BM * BK * 4;     // 16 KiB: one A tile (and a B tile of 128 rows)
 constexpr unsigned WAIT_LIMIT = 1u << 26;   // tries per mbarrier wait (well over a second)
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -146,7 +157,7 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parit
 // consecutive columns per store instruction. BNT is the tile width (128, or 64 for stages with
 // few, long tasks: twice the CTAs at half the work each), with B tiles of BNT rows.
 template <int PASSES, int BNT>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(PASSES == 4 ? NT4 : NT, 1)
 gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict__ segs,
                const tnk_gemm_tile* __restrict__ tiles, const CUtensorMap* __restrict__ maps,
                void* __restrict__ Cout, int* __restrict__ err) {
@@ -154,7 +165,10 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     constexpr int A_BYTES = TILE_BYTES;                 // 128 x 32 FP32
     constexpr int B_BYTES = BNT * BK * 4;               // BNT x 32 FP32 (a multiple of 1 KiB)
     constexpr int PAIR = A_BYTES + B_BYTES;
-    constexpr int STAGE_BYTES = (PASSES == 3) ? 2 * PAIR : PAIR;  // Ah, Bh (, Al, Bl)
+    constexpr int STAGE_BYTES = (PASSES >= 3) ? 2 * PAIR : PAIR;  // Ah, Bh (, Al, Bl)
+    constexpr bool SPLIT = PASSES == 4;                 // hi/lo formed in shared memory
+    constexpr int LOAD_BYTES = SPLIT ? PAIR : STAGE_BYTES;
+    constexpr int NSPLIT_W = (NT4 - 64) / 32;           // splitter warps 2 .. 7
     constexpr int LDS = BNT + 1;                        // staging row stride (floats)
     static_assert(BM * LDS * 4 <= STAGES * STAGE_BYTES, "staging tile fits the ring");
     static_assert(B_BYTES % 1024 == 0, "B tiles keep the 1 KiB swizzle alignment");
@@ -164,7 +178,8 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
     uint64_t* empty = full + STAGES;
     uint64_t* done = empty + STAGES;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    uint64_t* splitb = done + 1;                        // PASSES = 4: STAGES split barriers
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(splitb + STAGES);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* counts = const_cast<int*>(abort_flag) + 1;     // [0] issued loads, [1] consumed
 
@@ -183,6 +198,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
+            if (SPLIT) mbar_init(&splitb[s], NSPLIT_W);
         }
         mbar_init(done, 1);
         *abort_flag = 0;
@@ -220,7 +236,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                 }
             }
             uint8_t* st = stage_mem + slot * STAGE_BYTES;
-            mbar_expect_tx(&full[slot], STAGE_BYTES);
+            mbar_expect_tx(&full[slot], LOAD_BYTES);
             tma_load_2d(st, &maps[2 * g.a_map], &full[slot], lk, tile.m0);
             tma_load_2d(st + A_BYTES, &maps[2 * g.b_map], &full[slot], lk, tile.n0);
             if (PASSES == 3) {
@@ -232,12 +248,48 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
             ++issued;
         }
         counts[0] = issued;
+    } else if (SPLIT && threadIdx.x >= 64 && nk > 0) {
+        // splitters (warps 2 .. 7): the raw FP32 tiles of a slot -> hi in place, lo beside them
+        // (the same swizzled positions), then a proxy fence so the tensor core sees the writes
+        const int t = threadIdx.x - 64;
+        for (int i = 0; i < nk; ++i) {
+            const int slot = i % STAGES;
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait_or_abort(&full[slot], (i / STAGES) & 1, abort_flag);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) {
+                if (lane == 0) {
+                    if (!*abort_flag) atomicExch(err, 4);
+                    *abort_flag = 1;
+                }
+                break;
+            }
+            float4* hi = reinterpret_cast<float4*>(stage_mem + slot * STAGE_BYTES);
+            float4* lo = reinterpret_cast<float4*>(stage_mem + slot * STAGE_BYTES + PAIR);
+            for (int e = t; e < PAIR / 16; e += NSPLIT_W * 32) {
+                const float4 x = hi[e];
+                float4 h, l;
+                h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
+                h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
+                h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
+                h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+                hi[e] = h;
+                lo[e] = l;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                 smem_u32(&splitb[slot]))
+                             : "memory");
+        }
     } else if (threadIdx.x == 32 && nk > 0) {
         // MMA issuer
         int consumed = 0;
         for (int i = 0; i < nk; ++i) {
             const int slot = i % STAGES;
-            if (!mbar_wait_or_abort(&full[slot], (i / STAGES) & 1, abort_flag)) {
+            if (!mbar_wait_or_abort(SPLIT ? &splitb[slot] : &full[slot], (i / STAGES) & 1,
+                                    abort_flag)) {
                 if (!*abort_flag) atomicExch(err, 1);
                 *abort_flag = 1;
                 break;
@@ -249,7 +301,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                 const uint64_t ah = smem_desc(st + kk * 32);
                 const uint64_t bh = smem_desc(st + A_BYTES + kk * 32);
                 mma_tf32<BNT>(tmem, ah, bh, (i > 0 || kk > 0) ? 1u : 0u);
-                if (PASSES == 3) {
+                if (PASSES >= 3) {
                     const uint64_t al = smem_desc(st + PAIR + kk * 32);
                     const uint64_t bl = smem_desc(st + PAIR + A_BYTES + kk * 32);
                     mma_tf32<BNT>(tmem, ah, bl, 1u);
@@ -277,10 +329,10 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     // CTA-uniform: TMEM loads are .sync.aligned and must be issued by whole warps
     const int bad = __syncthreads_or((*abort_flag != 0) || !acc_ready);
 
-    // epilogue: warp w owns accumulator rows 32w..32w+31 (its TMEM lane quarter)
+    // epilogue: warp w < 4 owns accumulator rows 32w..32w+31 (its TMEM lane quarter)
     float* stg = reinterpret_cast<float*>(stage_mem);
     const int rloc = warp * 32 + lane;
-    for (int c0 = 0; c0 < BNT; c0 += 32) {
+    for (int c0 = 0; c0 < BNT && warp < 4; c0 += 32) {
         uint32_t v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0u;
@@ -303,7 +355,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
         for (int j = 0; j < 32; ++j) stg[rloc * LDS + c0 + j] = __uint_as_float(v[j]);
     }
     __syncwarp();
-    if (!bad) {
+    if (!bad && warp < 4) {
         const bool f64 = (task.flags & 2) != 0;
         const int rows = min(32, task.m - (tile.m0 + warp * 32));
         const int cols = min(BNT, task.n - tile.n0);
@@ -580,7 +632,7 @@ constexpr size_t smem_bytes_p(int passes, int bn) {
 }
 
 constexpr size_t smem_bytes(int passes, int bn) {
-    return 1024 + (size_t)STAGES * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) + 256;
+    return 1024 + (size_t)STAGES * ((passes >= 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) + 256;
     // (1024: alignment slack of the ring; 256: barriers, TMEM slot, abort flag, counters)
 }
 
@@ -594,7 +646,7 @@ int launch_tc_t(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_ti
         set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
         return TNK_ERR_CUDA;
     }
-    gemm_tc_kernel<PASSES, BNT><<<(unsigned)n_tiles, NT, sm, stream>>>(
+    gemm_tc_kernel<PASSES, BNT><<<(unsigned)n_tiles, PASSES == 4 ? NT4 : NT, sm, stream>>>(
         tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
     return check_launch("gemm_tc_kernel");
 }
@@ -637,7 +689,7 @@ int sm_count() {
 int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
                    int64_t n_tiles, const void* maps, void* C, int* err, int passes, int bn,
                    cudaStream_t stream) {
-    if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3) ||
+    if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3 && passes != 4) ||
         (bn != 128 && bn != 64)) {
         set_error("tc gemm: bad tile count %lld, passes %d or tile width %d", (long long)n_tiles,
                   passes, bn);
@@ -653,7 +705,7 @@ int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm
         return TNK_ERR_ARG;
     }
     const int nsm = sm_count();
-    if (g_tc_schedule == 1 && n_tiles > nsm) {
+    if (g_tc_schedule == 1 && n_tiles > nsm && passes != 4) {
         if (passes == 3)
             return bn == 128 ? launch_tc_persistent_t<3, 128>(tasks, segs, tiles, n_tiles, nsm,
                                                               maps, C, err, stream)
@@ -664,6 +716,9 @@ int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm
                          : launch_tc_persistent_t<1, 64>(tasks, segs, tiles, n_tiles, nsm, maps,
                                                          C, err, stream);
     }
+    if (passes == 4)
+        return bn == 128 ? launch_tc_t<4, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
+                         : launch_tc_t<4, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
     if (passes == 3)
         return bn == 128 ? launch_tc_t<3, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
                          : launch_tc_t<3, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);

@@ -50,8 +50,9 @@ class TwoSiteOperatorTC:
         return self
 
     def _setup(self, tc, L_data: torch.Tensor, R_data: torch.Tensor, n: int, passes: int):
-        if passes not in (1, 3):
-            raise ValueError("passes must be 1 (TF32) or 3 (split TF32)")
+        if passes not in (1, 3, 4):
+            raise ValueError("passes must be 1 (TF32), 3 (split TF32, parts staged) or 4 (split "
+                             "TF32, parts formed in shared memory)")
         dev = L_data.device
         self.device = dev
         self.passes = passes
