@@ -75,13 +75,16 @@ def test_tc_persistent_schedule_equals_one_tile_per_cta(passes):
         assert _rel(b, ref) <= 1e-4
 
 
-def test_tc_shared_memory_split_equals_staged_split():
+def test_tc_shared_memory_split_matches_staged_split():
     """passes=4 (operands staged once as FP32, the TF32 hi/lo parts formed in shared memory by
-    the GEMM) gives the staged split's (passes=3) results bit for bit -- the chi=1024 mid bond
-    (128 x 128 and 128 x 64 tiles) and a 48-chain batched plan."""
-    from tnkit_gb300 import batch as B, workloads
+    the GEMM) is as accurate as the staged split (passes=3) against the FP64 matvec -- the
+    chi=1024 mid bond (128 x 128 and 128 x 64 tiles) and a 48-chain batched plan. The two differ
+    in the lo parts of FP64-sourced operands (the staged split rounds the FP64 residual x - hi,
+    the shared-memory split the FP32 one), at ~1e-7 of the result."""
+    from tnkit_gb300 import batch as B, ops, workloads
     from tnkit_gb300.mixed import TwoSiteOperatorTC
     th, L, W1, W2, R = workloads.mid_bond_problem(seed=41)
+    ref = ops.TwoSiteOperator(th.layout, L, W1, W2, R)(th.data)
     a = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=3)(th.data)
     op4 = TwoSiteOperatorTC(th.layout, L, W1, W2, R, passes=4)
     b = op4(th.data)
@@ -91,10 +94,13 @@ def test_tc_shared_memory_split_equals_staged_split():
     ab = p3(xb)
     p4 = B.BatchedTwoSiteOperator(probs, precision="tc", tc_passes=4)
     bb = p4(xb)
+    bref = B.BatchedTwoSiteOperator(probs, precision="f64")(xb)
     torch.cuda.synchronize()
     op4.check_device_error()
     p4.tc.check_device_error()
-    assert torch.equal(a, b) and torch.equal(ab, bb)
+    assert _rel(b, ref) <= 1e-4 and _rel(bb, bref) <= 1e-4
+    assert _rel(b, ref) <= 2 * _rel(a, ref) + 1e-7
+    assert _rel(b, a) <= 1e-5 and _rel(bb, ab) <= 1e-5
 
 
 def test_tc_matvec_golden_problem(golden):
