@@ -212,7 +212,7 @@ int tnk_combine_f64(const tnk_comb_task* tasks, const tnk_comb_term* terms,
  * low-precision matvec of tnkit/_dmrg.py:691-695 (eig='lanczos-mixed', there complex64 einsums).
  * passes = 3 splits every operand into TF32 hi/lo parts (~1e-6 relative error); passes = 1 is
  * plain TF32 (~1e-3); passes = 4 is passes 3 with the operands staged once as FP32 and the hi/lo
- * parts formed in shared memory inside the GEMM (half the operand traffic, the same results).
+ * parts formed in shared memory inside the GEMM (half the operand traffic, the same accuracy).
  * ---------------------------------------------------------------------------------------- */
 
 /* A tensor-core GEMM segment: operand tensor maps (hi parts at index 2*map, lo at 2*map+1). */

@@ -32,7 +32,7 @@ from . import workloads
 
 
 # split-TF32 form of the tensor-core batches: 3 (hi/lo parts staged) or 4 (formed in shared
-# memory by the GEMM; the same results)
+# memory by the GEMM; the same accuracy)
 TC_PASSES = 3
 
 class _Extent:

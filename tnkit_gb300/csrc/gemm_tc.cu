@@ -14,8 +14,10 @@
 // relative with FP32 accumulation; PASSES = 1 is plain TF32. PASSES = 4 is the same product as
 // PASSES = 3 with the operands staged once, as FP32: each ring slot's tiles arrive raw and six
 // splitter warps write the hi part in place and the lo part beside it before the MMAs read them
-// (half the bytes from L2 per K step, the stages being bound by that traffic; the same hi and
-// lo values, so the same results bit for bit).
+// (half the bytes from L2 per K step, the stages being bound by that traffic). The parts are
+// those of the FP32 value: for FP64-sourced operands (theta, L, R) the staged split rounds the
+// FP64 residual x - hi instead, so the two forms differ in the last bit of some lo parts
+// (~1e-7 of the result); both are ~1e-6 from FP64.
 //
 // Every mbarrier wait is bounded; on a timeout the CTA records an error code in `err`, skips
 // the rest of its work, waits (bounded) for its own issued operations and frees its TMEM.
