@@ -79,11 +79,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     return false;
 }
 
-// Start fetching a tensor map into the descriptor cache (a hint; no ordering).
-__device__ __forceinline__ void tmap_prefetch(const CUtensorMap* map) {
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
-}
-
 // Make host-written tensor maps in global memory visible to the tensor-map proxy.
 __device__ __forceinline__ void tmap_acquire(const CUtensorMap* map) {
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
@@ -222,16 +217,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     for (int s = task.seg_begin; s < task.seg_end; ++s) nk += (segs[s].k + BK - 1) / BK;
 
     if (threadIdx.x == 0 && nk > 0) {
-        // TMA producer: cursor over (segment, k0); the tile's tensor maps are fetched into the
-        // descriptor cache up front, so later segments' first loads do not wait for them
-        for (int q = task.seg_begin; q < task.seg_end; ++q) {
-            tmap_prefetch(&maps[2 * segs[q].a_map]);
-            tmap_prefetch(&maps[2 * segs[q].b_map]);
-            if (PASSES == 3) {
-                tmap_prefetch(&maps[2 * segs[q].a_map + 1]);
-                tmap_prefetch(&maps[2 * segs[q].b_map + 1]);
-            }
-        }
+        // TMA producer: cursor over (segment, k0)
         int ls = task.seg_begin, lk = 0, issued = 0;
         for (int i = 0; i < nk; ++i) {
             const int slot = i % STAGES;
@@ -480,18 +466,6 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
             const tnk_gemm_task task = tasks[tile.task];
             int ls = task.seg_begin, lk = 0;
             const int nk = ksteps(task);
-            // this tile's and the next tile's tensor maps into the descriptor cache
-            for (int tt = t; tt < n_tiles && tt < t + 2 * (int)gridDim.x; tt += gridDim.x) {
-                const tnk_gemm_task tk = tasks[tiles[tt].task];
-                for (int q = tk.seg_begin; q < tk.seg_end; ++q) {
-                    tmap_prefetch(&maps[2 * segs[q].a_map]);
-                    tmap_prefetch(&maps[2 * segs[q].b_map]);
-                    if (PASSES == 3) {
-                        tmap_prefetch(&maps[2 * segs[q].a_map + 1]);
-                        tmap_prefetch(&maps[2 * segs[q].b_map + 1]);
-                    }
-                }
-            }
             for (int i = 0; i < nk; ++i, ++g) {
                 const int slot = g % STAGES;
                 if (g >= STAGES &&
