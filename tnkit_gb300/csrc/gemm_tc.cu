@@ -334,7 +334,8 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     // epilogue: warp w < 4 owns accumulator rows 32w..32w+31 (its TMEM lane quarter)
     float* stg = reinterpret_cast<float*>(stage_mem);
     const int rloc = warp * 32 + lane;
-    for (int c0 = 0; c0 < BNT && warp < 4; c0 += 32) {
+    const int tile_cols = min(BNT, task.n - tile.n0);   // chunks past the task's width hold 0
+    for (int c0 = 0; c0 < BNT && c0 < tile_cols && warp < 4; c0 += 32) {
         uint32_t v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0u;
@@ -361,7 +362,23 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
         const bool f64 = (task.flags & 2) != 0;
         const int rows = min(32, task.m - (tile.m0 + warp * 32));
         const int cols = min(BNT, task.n - tile.n0);
-        for (int r = 0; r < rows; ++r) {
+        // a tile that spans its task's whole width over rows of stride ldc == n writes one
+        // contiguous run: stream it flat, 32 consecutive elements per store, instead of row by
+        // row (thin blocks -- 2, 29, 113 columns -- make every row store a short, unaligned one)
+        const bool flat = tile.n0 == 0 && task.n <= BNT && task.ldc == task.n;
+        if (flat && rows > 0) {
+            const int64_t fbase = task.c_off + (int64_t)(tile.m0 + warp * 32) * cols;
+            const int tot = rows * cols;
+            for (int e = lane; e < tot; e += 32) {
+                const int r = e / cols, cc = e - r * cols;
+                const float x = stg[(warp * 32 + r) * LDS + cc];
+                if (f64)
+                    reinterpret_cast<double*>(Cout)[fbase + e] = (double)x;
+                else
+                    reinterpret_cast<float*>(Cout)[fbase + e] = x;
+            }
+        }
+        for (int r = 0; r < (flat ? 0 : rows); ++r) {
             const int row = tile.m0 + warp * 32 + r;
             const int64_t rbase = task.c_off + (int64_t)row * task.ldc + tile.n0;
             const float* src = stg + (warp * 32 + r) * LDS;
@@ -566,7 +583,10 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
             const bool f64 = (task.flags & 2) != 0;
             const int rows = min(32, task.m - (tile.m0 + q * 32));
             const int cols = min(BNT, task.n - tile.n0);
-            for (int c0 = 0; c0 < BNT; c0 += 32) {
+            // one chunk holds the whole row when the task is at most 32 wide: then its rows are
+            // one contiguous run (ldc == n) and are streamed flat (see gemm_tc_kernel)
+            const bool flat = tile.n0 == 0 && task.n <= 32 && task.ldc == task.n;
+            for (int c0 = 0; c0 < BNT && c0 < cols; c0 += 32) {
                 uint32_t v[32];
 #pragma unroll
                 for (int x = 0; x < 32; ++x) v[x] = 0u;
@@ -590,7 +610,18 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
 #pragma unroll
                 for (int x = 0; x < 32; ++x) stg[lane * LDW + x] = __uint_as_float(v[x]);
                 __syncwarp();
-                for (int r = 0; r < rows; ++r) {
+                if (flat && rows > 0) {
+                    const int64_t fbase = task.c_off + (int64_t)(tile.m0 + q * 32) * cols;
+                    for (int e = lane; e < rows * cols; e += 32) {
+                        const int r = e / cols, cc = e - r * cols;
+                        const float xv = stg[r * LDW + cc];
+                        if (f64)
+                            reinterpret_cast<double*>(Cout)[fbase + e] = (double)xv;
+                        else
+                            reinterpret_cast<float*>(Cout)[fbase + e] = xv;
+                    }
+                }
+                for (int r = 0; r < (flat ? 0 : rows); ++r) {
                     const int row = tile.m0 + q * 32 + r;
                     const int col = c0 + lane;
                     if (col < cols) {
