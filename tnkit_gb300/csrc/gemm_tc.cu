@@ -150,13 +150,38 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parit
     return false;
 }
 
+// One warp's share of an epilogue: `rows` (<= 32) staged rows of NQ * 32 columns at src (row
+// stride lds floats, all 32 rows readable) go to C[base + r * ldc + c] for c < cols. Rows go in
+// batches of 32 / NQ: a batch's shared-memory loads all issue before its global stores, so the
+// warp waits one load latency per batch rather than one per store (the row-at-a-time loop
+// spent ~15 k cycles of a 128 x 128 tile's epilogue on that chain, ~5 k batched).
+template <int NQ, typename T>
+__device__ __forceinline__ void store_rows(T* __restrict__ C, int64_t base, int64_t ldc,
+                                           const float* __restrict__ src, int lds, int rows,
+                                           int cols, int lane) {
+    constexpr int RB = 32 / NQ;
+    for (int r0 = 0; r0 < rows; r0 += RB) {
+        float x[RB][NQ];
+#pragma unroll
+        for (int i = 0; i < RB; ++i)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) x[i][q] = src[(r0 + i) * lds + q * 32 + lane];
+#pragma unroll
+        for (int i = 0; i < RB; ++i)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q)
+                if (r0 + i < rows && q * 32 + lane < cols)
+                    C[base + (int64_t)(r0 + i) * ldc + q * 32 + lane] = (T)x[i][q];
+    }
+}
+
 // Warp roles: warp 0 lane 0 streams the operand tiles by TMA into the STAGES-deep ring (waiting
 // for the MMA issuer to release a slot before refilling it), warp 1 lane 0 issues the MMAs as
 // tiles land and releases each slot with tcgen05.commit, so loads run STAGES - 1 K steps ahead
 // of the tensor core without either thread waiting on its own work. After the last MMA all four
 // warps move the accumulator out: TMEM -> registers (32 columns per tcgen05.ld) -> a padded
-// shared-memory tile (the operand ring, idle by then) -> global memory row by row, 32
-// consecutive columns per store instruction. BNT is the tile width (128, or 64 for stages with
+// shared-memory tile (the operand ring, idle by then) -> global memory in batches of rows
+// (store_rows), 32 consecutive columns per store instruction. BNT is the tile width (128, or 64 for stages with
 // few, long tasks: twice the CTAs at half the work each), with B tiles of BNT rows.
 template <int PASSES, int BNT>
 __global__ void __launch_bounds__(PASSES == 4 ? NT4 : NT, 1)
@@ -361,39 +386,14 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     if (!bad && warp < 4) {
         const bool f64 = (task.flags & 2) != 0;
         const int rows = min(32, task.m - (tile.m0 + warp * 32));
-        const int cols = min(BNT, task.n - tile.n0);
-        // a tile that spans its task's whole width over rows of stride ldc == n writes one
-        // contiguous run: stream it flat, 32 consecutive elements per store, instead of row by
-        // row (thin blocks -- 2, 29, 113 columns -- make every row store a short, unaligned one)
-        const bool flat = tile.n0 == 0 && task.n <= BNT && task.ldc == task.n;
-        if (flat && rows > 0) {
-            const int64_t fbase = task.c_off + (int64_t)(tile.m0 + warp * 32) * cols;
-            const int tot = rows * cols;
-            for (int e = lane; e < tot; e += 32) {
-                const int r = e / cols, cc = e - r * cols;
-                const float x = stg[(warp * 32 + r) * LDS + cc];
-                if (f64)
-                    reinterpret_cast<double*>(Cout)[fbase + e] = (double)x;
-                else
-                    reinterpret_cast<float*>(Cout)[fbase + e] = x;
-            }
-        }
-        for (int r = 0; r < (flat ? 0 : rows); ++r) {
-            const int row = tile.m0 + warp * 32 + r;
-            const int64_t rbase = task.c_off + (int64_t)row * task.ldc + tile.n0;
-            const float* src = stg + (warp * 32 + r) * LDS;
-#pragma unroll
-            for (int q = 0; q < BNT / 32; ++q) {
-                const int col = q * 32 + lane;
-                if (col < cols) {
-                    const float x = src[col];
-                    if (f64)
-                        reinterpret_cast<double*>(Cout)[rbase + col] = (double)x;
-                    else
-                        reinterpret_cast<float*>(Cout)[rbase + col] = x;
-                }
-            }
-        }
+        const int64_t base = task.c_off + (int64_t)(tile.m0 + warp * 32) * task.ldc + tile.n0;
+        const float* src = stg + warp * 32 * LDS;
+        if (f64)
+            store_rows<BNT / 32>(reinterpret_cast<double*>(Cout), base, task.ldc, src, LDS, rows,
+                                 tile_cols, lane);
+        else
+            store_rows<BNT / 32>(reinterpret_cast<float*>(Cout), base, task.ldc, src, LDS, rows,
+                                 tile_cols, lane);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -583,9 +583,6 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
             const bool f64 = (task.flags & 2) != 0;
             const int rows = min(32, task.m - (tile.m0 + q * 32));
             const int cols = min(BNT, task.n - tile.n0);
-            // one chunk holds the whole row when the task is at most 32 wide: then its rows are
-            // one contiguous run (ldc == n) and are streamed flat (see gemm_tc_kernel)
-            const bool flat = tile.n0 == 0 && task.n <= 32 && task.ldc == task.n;
             for (int c0 = 0; c0 < BNT && c0 < cols; c0 += 32) {
                 uint32_t v[32];
 #pragma unroll
@@ -610,29 +607,14 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
 #pragma unroll
                 for (int x = 0; x < 32; ++x) stg[lane * LDW + x] = __uint_as_float(v[x]);
                 __syncwarp();
-                if (flat && rows > 0) {
-                    const int64_t fbase = task.c_off + (int64_t)(tile.m0 + q * 32) * cols;
-                    for (int e = lane; e < rows * cols; e += 32) {
-                        const int r = e / cols, cc = e - r * cols;
-                        const float xv = stg[r * LDW + cc];
-                        if (f64)
-                            reinterpret_cast<double*>(Cout)[fbase + e] = (double)xv;
-                        else
-                            reinterpret_cast<float*>(Cout)[fbase + e] = xv;
-                    }
-                }
-                for (int r = 0; r < (flat ? 0 : rows); ++r) {
-                    const int row = tile.m0 + q * 32 + r;
-                    const int col = c0 + lane;
-                    if (col < cols) {
-                        const int64_t o = task.c_off + (int64_t)row * task.ldc + tile.n0 + col;
-                        const float xv = stg[r * LDW + lane];
-                        if (f64)
-                            reinterpret_cast<double*>(Cout)[o] = (double)xv;
-                        else
-                            reinterpret_cast<float*>(Cout)[o] = xv;
-                    }
-                }
+                const int64_t base =
+                    task.c_off + (int64_t)(tile.m0 + q * 32) * task.ldc + tile.n0 + c0;
+                if (f64)
+                    store_rows<1>(reinterpret_cast<double*>(Cout), base, task.ldc, stg, LDW,
+                                  rows, cols - c0, lane);
+                else
+                    store_rows<1>(reinterpret_cast<float*>(Cout), base, task.ldc, stg, LDW, rows,
+                                  cols - c0, lane);
                 __syncwarp();
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
