@@ -70,21 +70,30 @@ cvt_split_kernel(const CvtTask* __restrict__ tasks, const CvtItem* __restrict__ 
 
 constexpr int NT = 256;
 constexpr int TERMS_SMEM = 64;
+constexpr int YSPLIT = 4;       // CTAs per item (gridDim.y): each takes every YSPLIT-th pass
 
+// grid: (items, YSPLIT); each pass covers EPT * NT consecutive elements of the item's row range.
+// An element's sum runs over the task's terms in order whatever the split, so the result does not
+// depend on the grid; the loads of TB terms are issued together before their FMAs, so a pass waits
+// for about one load latency per TB terms rather than one per term.
 __global__ void __launch_bounds__(NT)
 comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __restrict__ terms,
                 const tnk_comb_item* __restrict__ items, const float* __restrict__ src,
                 float* __restrict__ dst, int64_t lo_off, int split) {
-    constexpr int EPT = 4;                      // elements per thread per pass (loads in flight)
+    constexpr int EPT = 4;                      // elements per thread per pass
+    constexpr int TB = 4;                       // terms whose loads are in flight together
     __shared__ tnk_comb_term st[TERMS_SMEM];
     const tnk_comb_item item = items[blockIdx.x];
     const tnk_comb_task t = tasks[item.task];
     const int cols = t.cols;
     const int64_t nel = (int64_t)(item.row1 - item.row0) * cols;
+    const bool nel32 = nel <= 0x7fffffff;       // element indices fit 32-bit division
     const int nterm = t.term_end - t.term_begin;
-    // accumulate in FP32 registers per element over all terms (chunks of TERMS_SMEM), the terms
-    // in order, so each element's sum is the same whatever the pass structure
-    for (int64_t e0 = 0; e0 < nel; e0 += EPT * NT) {
+    const bool resident = nterm <= TERMS_SMEM;  // terms staged once for every pass
+    if (resident && (int)threadIdx.x < nterm) st[threadIdx.x] = terms[t.term_begin + threadIdx.x];
+    __syncthreads();
+    for (int64_t e0 = (int64_t)blockIdx.y * EPT * NT; e0 < nel;
+         e0 += (int64_t)gridDim.y * EPT * NT) {
         int r[EPT], c[EPT];
         bool live[EPT];
         float acc[EPT];
@@ -92,26 +101,48 @@ comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __
         for (int u = 0; u < EPT; ++u) {
             const int64_t e = e0 + u * NT + (int)threadIdx.x;
             live[u] = e < nel;
-            const int rr = live[u] ? (int)(e / cols) : 0;
+            int rr = 0, cc = 0;
+            if (live[u]) {
+                if (nel32) {
+                    const int e32 = (int)e;
+                    rr = e32 / cols;
+                    cc = e32 - rr * cols;
+                } else {
+                    rr = (int)(e / cols);
+                    cc = (int)(e - (int64_t)rr * cols);
+                }
+            }
             r[u] = item.row0 + rr;
-            c[u] = live[u] ? (int)(e - (int64_t)rr * cols) : 0;
+            c[u] = cc;
             acc[u] = 0.f;
         }
         for (int t0 = 0; t0 < nterm; t0 += TERMS_SMEM) {
             const int nt = min(TERMS_SMEM, nterm - t0);
-            __syncthreads();
-            if ((int)threadIdx.x < nt) st[threadIdx.x] = terms[t.term_begin + t0 + threadIdx.x];
-            __syncthreads();
-            for (int q = 0; q < nt; ++q) {
-                const tnk_comb_term tq = st[q];
-                float x[EPT];
+            if (!resident) {
+                __syncthreads();
+                if ((int)threadIdx.x < nt) st[threadIdx.x] = terms[t.term_begin + t0 + threadIdx.x];
+                __syncthreads();
+            }
+            for (int q0 = 0; q0 < nt; q0 += TB) {
+                float x[TB][EPT];
 #pragma unroll
-                for (int u = 0; u < EPT; ++u)
-                    x[u] = live[u] ? src[tq.src_off + (int64_t)r[u] * tq.src_ld +
-                                         (int64_t)c[u] * tq.src_cs]
-                                   : 0.f;
+                for (int j = 0; j < TB; ++j) {
+                    const bool on = q0 + j < nt;
+                    const tnk_comb_term tq = st[on ? q0 + j : q0];
 #pragma unroll
-                for (int u = 0; u < EPT; ++u) acc[u] = fmaf((float)tq.coef, x[u], acc[u]);
+                    for (int u = 0; u < EPT; ++u)
+                        x[j][u] = (on && live[u]) ? src[tq.src_off + (int64_t)r[u] * tq.src_ld +
+                                                        (int64_t)c[u] * tq.src_cs]
+                                                  : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < TB; ++j) {
+                    if (q0 + j < nt) {
+                        const float coef = (float)st[q0 + j].coef;
+#pragma unroll
+                        for (int u = 0; u < EPT; ++u) acc[u] = fmaf(coef, x[j][u], acc[u]);
+                    }
+                }
             }
         }
 #pragma unroll
@@ -156,8 +187,8 @@ int launch_comb_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
         set_error("combine f32: null argument");
         return TNK_ERR_ARG;
     }
-    comb_f32_kernel<<<(unsigned)n_items, NT, 0, stream>>>(tasks, terms, items, src, dst, lo_off,
-                                                          split);
+    comb_f32_kernel<<<dim3((unsigned)n_items, YSPLIT), NT, 0, stream>>>(tasks, terms, items, src,
+                                                                        dst, lo_off, split);
     return check_launch("comb_f32_kernel");
 }
 
