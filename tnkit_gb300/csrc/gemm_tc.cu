@@ -210,6 +210,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* counts = const_cast<int*>(abort_flag) + 1;     // [0] issued loads, [1] consumed
 
+    pdl_trigger();
     const tnk_gemm_tile tile = tiles[blockIdx.x];
     const tnk_gemm_task task = tasks[tile.task];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -236,6 +237,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    pdl_wait();     // the operands (and C's previous readers) belong to the kernels before
 
     // total K steps over all segments
     int nk = 0;
@@ -441,6 +443,7 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* counts = const_cast<int*>(abort_flag) + 1;       // [0] issued loads, [1] consumed
 
+    pdl_trigger();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -467,6 +470,7 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    pdl_wait();     // the operands (and C's previous readers) belong to the kernels before
 
     auto ksteps = [&](const tnk_gemm_task& task) {
         int nk = 0;
@@ -653,7 +657,8 @@ constexpr size_t smem_bytes(int passes, int bn) {
 
 template <int PASSES, int BNT>
 int launch_tc_t(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
-                int64_t n_tiles, const void* maps, void* C, int* err, cudaStream_t stream) {
+                int64_t n_tiles, const void* maps, void* C, int* err, cudaStream_t stream,
+                bool pdl) {
     const size_t sm = smem_bytes(PASSES, BNT);
     cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<PASSES, BNT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -661,15 +666,15 @@ int launch_tc_t(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_ti
         set_error("tc gemm: smem attribute: %s", cudaGetErrorString(e));
         return TNK_ERR_CUDA;
     }
-    gemm_tc_kernel<PASSES, BNT><<<(unsigned)n_tiles, PASSES == 4 ? NT4 : NT, sm, stream>>>(
-        tasks, segs, tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
-    return check_launch("gemm_tc_kernel");
+    return launch_k("gemm_tc_kernel", gemm_tc_kernel<PASSES, BNT>, dim3((unsigned)n_tiles),
+                    dim3(PASSES == 4 ? NT4 : NT), sm, stream, pdl, tasks, segs, tiles,
+                    reinterpret_cast<const CUtensorMap*>(maps), C, err);
 }
 
 template <int PASSES, int BNT>
 int launch_tc_persistent_t(const tnk_gemm_task* tasks, const TcSeg* segs,
                            const tnk_gemm_tile* tiles, int64_t n_tiles, int grid,
-                           const void* maps, void* C, int* err, cudaStream_t stream) {
+                           const void* maps, void* C, int* err, cudaStream_t stream, bool pdl) {
     const size_t sm = smem_bytes_p(PASSES, BNT);
     cudaError_t e = cudaFuncSetAttribute(gemm_tc_persistent_kernel<PASSES, BNT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -677,9 +682,9 @@ int launch_tc_persistent_t(const tnk_gemm_task* tasks, const TcSeg* segs,
         set_error("tc gemm (persistent): smem attribute: %s", cudaGetErrorString(e));
         return TNK_ERR_CUDA;
     }
-    gemm_tc_persistent_kernel<PASSES, BNT><<<(unsigned)grid, NT_P, sm, stream>>>(
-        tasks, segs, tiles, (int)n_tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
-    return check_launch("gemm_tc_persistent_kernel");
+    return launch_k("gemm_tc_persistent_kernel", gemm_tc_persistent_kernel<PASSES, BNT>,
+                    dim3((unsigned)grid), dim3(NT_P), sm, stream, pdl, tasks, segs, tiles,
+                    (int)n_tiles, reinterpret_cast<const CUtensorMap*>(maps), C, err);
 }
 
 int g_tc_schedule = 0;       // 0: one tile per CTA; 1: persistent CTAs when tiles exceed SMs
@@ -701,9 +706,10 @@ int sm_count() {
 }  // namespace
 
 // bn: the tile width of this stage, 128 or 64; the B operand maps must have boxes of bn rows.
+// pdl: launch as a programmatic dependent of the stream's previous kernel (launch_k).
 int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm_tile* tiles,
                    int64_t n_tiles, const void* maps, void* C, int* err, int passes, int bn,
-                   cudaStream_t stream) {
+                   cudaStream_t stream, bool pdl) {
     if (n_tiles < 0 || n_tiles > 0x7fffffff || (passes != 1 && passes != 3 && passes != 4) ||
         (bn != 128 && bn != 64)) {
         set_error("tc gemm: bad tile count %lld, passes %d or tile width %d", (long long)n_tiles,
@@ -723,22 +729,24 @@ int launch_gemm_tc(const tnk_gemm_task* tasks, const TcSeg* segs, const tnk_gemm
     if (g_tc_schedule == 1 && n_tiles > nsm && passes != 4) {
         if (passes == 3)
             return bn == 128 ? launch_tc_persistent_t<3, 128>(tasks, segs, tiles, n_tiles, nsm,
-                                                              maps, C, err, stream)
+                                                              maps, C, err, stream, pdl)
                              : launch_tc_persistent_t<3, 64>(tasks, segs, tiles, n_tiles, nsm,
-                                                             maps, C, err, stream);
+                                                             maps, C, err, stream, pdl);
         return bn == 128 ? launch_tc_persistent_t<1, 128>(tasks, segs, tiles, n_tiles, nsm, maps,
-                                                          C, err, stream)
+                                                          C, err, stream, pdl)
                          : launch_tc_persistent_t<1, 64>(tasks, segs, tiles, n_tiles, nsm, maps,
-                                                         C, err, stream);
+                                                         C, err, stream, pdl);
     }
     if (passes == 4)
-        return bn == 128 ? launch_tc_t<4, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
-                         : launch_tc_t<4, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
+        return bn == 128
+                   ? launch_tc_t<4, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl)
+                   : launch_tc_t<4, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl);
     if (passes == 3)
-        return bn == 128 ? launch_tc_t<3, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
-                         : launch_tc_t<3, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
-    return bn == 128 ? launch_tc_t<1, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream)
-                     : launch_tc_t<1, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream);
+        return bn == 128
+                   ? launch_tc_t<3, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl)
+                   : launch_tc_t<3, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl);
+    return bn == 128 ? launch_tc_t<1, 128>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl)
+                     : launch_tc_t<1, 64>(tasks, segs, tiles, n_tiles, maps, C, err, stream, pdl);
 }
 
 // --------------------------------------------------------------------------------------------

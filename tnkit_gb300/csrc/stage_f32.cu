@@ -37,9 +37,11 @@ cvt_split_kernel(const CvtTask* __restrict__ tasks, const CvtItem* __restrict__ 
                  const double* __restrict__ src, float* __restrict__ dst, int64_t lo_off,
                  int split) {
     __shared__ double tile[32][33];
+    pdl_trigger();
     const CvtItem it = items[blockIdx.x];
     const CvtTask t = tasks[it.task];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    pdl_wait();
     // load 32 x 32 source tile (rows r0.., cols c0..), coalesced along columns
     for (int i = ty; i < 32; i += 8) {
         const int r = it.r0 + i, c = it.c0 + tx;
@@ -83,6 +85,7 @@ comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __
     constexpr int EPT = 4;                      // elements per thread per pass
     constexpr int TB = 4;                       // terms whose loads are in flight together
     __shared__ tnk_comb_term st[TERMS_SMEM];
+    pdl_trigger();
     const tnk_comb_item item = items[blockIdx.x];
     const tnk_comb_task t = tasks[item.task];
     const int cols = t.cols;
@@ -92,6 +95,7 @@ comb_f32_kernel(const tnk_comb_task* __restrict__ tasks, const tnk_comb_term* __
     const bool resident = nterm <= TERMS_SMEM;  // terms staged once for every pass
     if (resident && (int)threadIdx.x < nterm) st[threadIdx.x] = terms[t.term_begin + threadIdx.x];
     __syncthreads();
+    pdl_wait();     // src is the previous kernel's output
     for (int64_t e0 = (int64_t)blockIdx.y * EPT * NT; e0 < nel;
          e0 += (int64_t)gridDim.y * EPT * NT) {
         int r[EPT], c[EPT];
@@ -177,7 +181,7 @@ int launch_cvt_split(const CvtTask* tasks, const CvtItem* items, int64_t n_items
 
 int launch_comb_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
                     const tnk_comb_item* items, int64_t n_items, const float* src, float* dst,
-                    int64_t lo_off, int split, cudaStream_t stream) {
+                    int64_t lo_off, int split, cudaStream_t stream, bool pdl) {
     if (n_items < 0 || n_items > 0x7fffffff) {
         set_error("combine f32: bad item count");
         return TNK_ERR_ARG;
@@ -187,9 +191,8 @@ int launch_comb_f32(const tnk_comb_task* tasks, const tnk_comb_term* terms,
         set_error("combine f32: null argument");
         return TNK_ERR_ARG;
     }
-    comb_f32_kernel<<<dim3((unsigned)n_items, YSPLIT), NT, 0, stream>>>(tasks, terms, items, src,
-                                                                        dst, lo_off, split);
-    return check_launch("comb_f32_kernel");
+    return launch_k("comb_f32_kernel", comb_f32_kernel, dim3((unsigned)n_items, YSPLIT), dim3(NT),
+                    0, stream, pdl, tasks, terms, items, src, dst, lo_off, split);
 }
 
 }  // namespace tnk

@@ -49,4 +49,38 @@ inline int check_launch(const char* what) {
     return TNK_OK;
 }
 
+// Programmatic dependent launch. A kernel launched by launch_k with pdl = true may be scheduled
+// while its predecessor in the stream still runs -- once every CTA of the predecessor has called
+// pdl_trigger or exited -- and must call pdl_wait before it touches memory the predecessor (or
+// anything before it) writes or reads; pdl_wait returns when the predecessor has completed and
+// its writes are visible. For a kernel launched plainly both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch k<<<grid, block, smem, stream>>>(args...), with programmatic stream serialisation
+// when pdl.
+template <typename... KArgs, typename... Args>
+inline int launch_k(const char* what, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                    cudaStream_t stream, bool pdl, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k, args...);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_error("%s: %s", what, cudaGetErrorString(e));
+        return TNK_ERR_CUDA;
+    }
+    return check_launch(what);
+}
+
 }  // namespace tnk
