@@ -36,7 +36,10 @@ static_assert(sizeof(TcSeg) == 16, "TcSeg layout");
 namespace {
 
 constexpr int BM = 128, BK = 32;
-constexpr int STAGES = 3;
+// Depth of the operand ring: three slots of 64 KB for 128-wide tiles; four of 48 KB for 64-wide
+// ones, whose long K loops (stage 3: ~27 K steps per tile) otherwise wait on TMA latency that
+// three slots do not cover.
+__host__ __device__ constexpr int stages_for(int bnt) { return bnt == 64 ? 4 : 3; }
 constexpr int NT = 128;
 constexpr int NT4 = 256;                    // PASSES = 4: two more roles of warps (splitters)
 constexpr int TILE_BYTES = BM * BK * 4;     // 16 KiB: one A tile (and a B tile of 128 rows)
@@ -189,6 +192,7 @@ gemm_tc_kernel(const tnk_gemm_task* __restrict__ tasks, const TcSeg* __restrict_
                const tnk_gemm_tile* __restrict__ tiles, const CUtensorMap* __restrict__ maps,
                void* __restrict__ Cout, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
+    constexpr int STAGES = stages_for(BNT);
     constexpr int A_BYTES = TILE_BYTES;                 // 128 x 32 FP32
     constexpr int B_BYTES = BNT * BK * 4;               // BNT x 32 FP32 (a multiple of 1 KiB)
     constexpr int PAIR = A_BYTES + B_BYTES;
@@ -425,6 +429,7 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
                           int n_tiles, const CUtensorMap* __restrict__ maps,
                           void* __restrict__ Cout, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
+    constexpr int STAGES = stages_for(BNT);
     constexpr int A_BYTES = TILE_BYTES;
     constexpr int B_BYTES = BNT * BK * 4;
     constexpr int PAIR = A_BYTES + B_BYTES;
@@ -646,12 +651,13 @@ gemm_tc_persistent_kernel(const tnk_gemm_task* __restrict__ tasks,
 }
 
 constexpr size_t smem_bytes_p(int passes, int bn) {
-    return 1024 + (size_t)STAGES * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) +
+    return 1024 + (size_t)stages_for(bn) * ((passes == 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) +
            4 * 32 * 33 * 4 + 256;
 }
 
 constexpr size_t smem_bytes(int passes, int bn) {
-    return 1024 + (size_t)STAGES * ((passes >= 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) + 256;
+    return 1024 + (size_t)stages_for(bn) * ((passes >= 3) ? 2 : 1) * (TILE_BYTES + bn * BK * 4) +
+           256;
     // (1024: alignment slack of the ring; 256: barriers, TMEM slot, abort flag, counters)
 }
 
