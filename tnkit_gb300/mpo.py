@@ -173,6 +173,24 @@ def random_block_mps(mpo: Sequence[BlockTensor], chi: int, charge, rng,
     return out
 
 
+def product_block_mps(mpo: Sequence[BlockTensor], states: Sequence[int],
+                      device="cuda") -> List[BlockTensor]:
+    """The product state with site n in the physical sector of charge `states[n]` (e.g. the Neel
+    state of a spin-1/2 S^z chain, charges +1 -1 +1 ...): bonds of one state each, the left
+    bond of site n carrying the charge of sites 0 .. n-1, every site one block holding 1. The
+    physical sectors must be one-dimensional."""
+    out = []
+    q = 0
+    for W, s in zip(mpo, states):
+        p = W.legs[2]
+        if s not in p.charges or p.dims[p.charges.index(s)] != 1:
+            raise ValueError(f"charge {s!r} is not a one-dimensional physical sector")
+        lay = layout_of((Leg((q,), (1,), 1), p, Leg((q + s,), (1,), -1)), 0)
+        out.append(BlockTensor(lay, torch.ones(lay.size, dtype=torch.float64, device=device)))
+        q += s
+    return out
+
+
 def random_dense_mps(N: int, chi: int, d: int, rng, device="cuda") -> List[BlockTensor]:
     """Dense random MPS drawn as the reference's `random_mps` (tnkit/_dmrg.py:253-261)."""
     dims = [1] + [min(chi, d ** min(i, N - i)) for i in range(1, N)] + [1]
