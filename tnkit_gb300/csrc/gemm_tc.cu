@@ -1,13 +1,14 @@
 // Grouped GEMM over charge blocks on the 5th-generation tensor cores (tcgen05, kind::tf32).
 //
-// One CTA computes one 128 x 128 output tile of one task, C = sum_seg A_seg * B_seg^T, where
-// every operand is a K-major FP32 block staged by the host planner in a 16-byte-aligned padded
-// layout. Operand tiles (128 rows x 32 FP32 = one 128-byte swizzle atom) arrive by TMA
-// (cp.async.bulk.tensor.2d, SWIZZLE_128B, out-of-bounds rows/columns zero-filled, so ragged
-// sector blocks need no masking) into a 3-stage shared-memory ring; one elected thread issues
-// tcgen05.mma with the accumulator in TMEM and releases each stage with tcgen05.commit; the
-// epilogue moves the accumulator TMEM -> registers (tcgen05.ld 32x32b) -> global, as FP32 (the
-// next stage's input) or FP64 (the Lanczos vector).
+// One CTA computes one 128 x BN output tile (BN = 128 or 64) of one task, C = sum_seg A_seg *
+// B_seg^T, where every operand is a K-major FP32 block staged by the host planner in a
+// 16-byte-aligned padded layout. Operand tiles (128 rows x 32 FP32 = one 128-byte swizzle atom)
+// arrive by TMA (cp.async.bulk.tensor.2d, SWIZZLE_128B, out-of-bounds rows/columns zero-filled,
+// so ragged sector blocks need no masking) into a shared-memory ring of stages_for(BN) slots;
+// one elected thread issues tcgen05.mma with the accumulator in TMEM and releases each slot with
+// tcgen05.commit; the epilogue moves the accumulator TMEM -> registers (tcgen05.ld 32x32b) ->
+// shared memory -> global, as FP32 (the next stage's input) or FP64 (the Lanczos vector). The
+// matvec launches it as a programmatic dependent of the kernel before it (griddepcontrol).
 //
 // PASSES = 3 is the split-precision product A*B ~ Ah*Bh + Ah*Bl + Al*Bh of TF32 "hi" and "lo"
 // parts (each operand stored twice: hi = tf32(x), lo = tf32(x - hi)), accurate to ~1e-6
