@@ -132,3 +132,17 @@ def test_product_block_mps_is_the_neel_basis_state():
     assert np.array_equal(v, ref)
     with pytest.raises(ValueError):
         product_block_mps(W, [2] + neel[1:], device="cpu")
+
+
+def test_auxiliary_mpos_are_shared_and_correct():
+    """The identity and Z MPOs the gradient contracts with are built once per chain and site
+    (plans are cached by MPO object) and hold the right operators."""
+    from tnkit_gb300.grad import _aux_mpo
+    W, _ = _block_chain(4, 4, 1, cplx=False)
+    assert _aux_mpo("id", W) is _aux_mpo("id", W)
+    assert _aux_mpo("z", W, 1) is _aux_mpo("z", W, 1)
+    assert _aux_mpo("z", W, 1) is not _aux_mpo("z", W, 2)
+    for n, (i, z) in enumerate(zip(_aux_mpo("id", W), _aux_mpo("z", W, 1))):
+        assert np.array_equal(i.to_dense()[0, 0], np.eye(2))
+        # sector order: charge -1, then +1; Z = 2 S^z
+        assert np.array_equal(z.to_dense()[0, 0], np.diag([-1.0, 1.0]) if n == 1 else np.eye(2))

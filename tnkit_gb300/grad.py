@@ -379,6 +379,20 @@ def quadrature_weights(n: int, dt: float) -> np.ndarray:
     return w
 
 
+_AUX_MPOS: dict = {}
+
+
+def _aux_mpo(kind: str, W: Sequence[BlockTensor], site: int = -1) -> List[BlockTensor]:
+    """The identity MPO (kind 'id') or the Pauli Z MPO on `site` (kind 'z') of the chain of `W`,
+    one object per (kind, physical legs, site, device): the matvec and environment plans are
+    cached by MPO object, so repeated evaluations reuse them."""
+    key = (kind, tuple(w.legs[2] for w in W), site, str(W[0].data.device))
+    got = _AUX_MPOS.get(key)
+    if got is None:
+        got = _AUX_MPOS[key] = _identity_mpo(W) if kind == "id" else _z_mpo(W, site)
+    return got
+
+
 def _z_mpo(W: Sequence[BlockTensor], site: int) -> List[BlockTensor]:
     """The MPO of Pauli Z on `site` (identity elsewhere) with the physical legs of `W`."""
     dense = []
@@ -394,8 +408,8 @@ def z_expectation(mps: Sequence[BlockTensor], mpo: Sequence[BlockTensor], site: 
     M = list(mps)
     if not M[0].data.is_complex():
         M = [BlockTensor(m.layout, m.data.to(torch.complex128)) for m in M]
-    Lz, _ = _complex_envs(M, _z_mpo(list(mpo), site))
-    Ln, _ = _complex_envs(M, _identity_mpo(list(mpo)))
+    Lz, _ = _complex_envs(M, _aux_mpo("z", list(mpo), site))
+    Ln, _ = _complex_envs(M, _aux_mpo("id", list(mpo)))
     return float(Lz[len(M)].data.sum().real / Ln[len(M)].data.sum().real)
 
 
@@ -432,7 +446,7 @@ def tdvp_observable_gradient(mps: Sequence[BlockTensor], mpo: Sequence[BlockTens
     _, bwd_rec = tdvp2_evolve(lam_t, W_neg, chi, dt, n_steps,
                               measure=clone_mps, meas_every=1, **kw)
     lam = [m for _, m in bwd_rec][::-1]
-    W_id = _identity_mpo(W)
+    W_id = _aux_mpo("id", W)
     value = z_expectation(psi[-1], W, site)
     g = np.stack([im_transition_values(lam[k], psi[k], W_id, bond_op)
                   for k in range(n_steps + 1)], axis=1)
